@@ -1,0 +1,533 @@
+// C ABI of the DDGI probe engine (include/ddgi.h): objects, argument checks and the per-frame pass
+// sequence. The exe lambdas of the three reference passes (IrradianceProbeTranslationPass.cpp:56-186,
+// IrradianceProbeRayTracingPass.cpp:95-165, IrradianceProbeConvolvePass.cpp:109-143) become
+// ddgi_translate / ddgi_trace / ddgi_convolve; their state (_lastProbeIdx, _currentLayer and the
+// "ProbeLayer" blackboard value) lives in the grid object.
+#include "ddgi_common.cuh"
+#include "kernels.h"
+#include "lbvh.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace ddgi;
+
+struct DdgiContext {
+  int device = 0;
+  int numSms = 0;
+  uint32_t* dErr = nullptr;  // sticky device error word
+  std::mutex mu;
+  std::string err;
+};
+
+struct DdgiScene {
+  DdgiContext* ctx = nullptr;
+  DdgiPackedVertex* vertices = nullptr;
+  uint32_t* indices = nullptr;
+  DdgiMeshInfo* meshes = nullptr;
+  InstanceGPU* instances = nullptr;
+  DdgiMaterialInfo* materials = nullptr;
+  LbvhResult bvh;
+  DdgiSceneInfo info{};
+  SceneGPU view{};
+};
+
+struct DdgiGrid {
+  DdgiContext* ctx = nullptr;
+  DdgiGridDesc desc{};
+  GridGPU g{};
+  void* atlas[2] = {nullptr, nullptr};  // current atlas and the translation temp (swapped on a move)
+  int cur = 0;
+  float4* rayRad = nullptr;
+  float4* rayDir = nullptr;
+  int* rayHit = nullptr;
+  float4* lattice = nullptr;
+  float* wt = nullptr;    // N x 64 convolution weights (transposed)
+  float* wsum = nullptr;  // 64 weight sums
+  int rayH = 0;
+  uint64_t atlasBytes = 0;
+  int lastProbeIdx[2] = {0, 0};  // IrradianceProbeTranslationPass.h:17
+  int currentLayer = 0;          // IrradianceProbeRayTracingPass _currentLayer
+  int tracedBegin = 0, tracedEnd = 0;  // the "ProbeLayer" blackboard value, as a range
+  bool latticeValid = false;
+};
+
+namespace {
+
+int fail(DdgiContext* ctx, int code, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+int cudaFail(DdgiContext* ctx, cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation)
+    return fail(ctx, DDGI_ENOMEM, "%s: %s", what, cudaGetErrorString(e));
+  return fail(ctx, DDGI_EDEVICE, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cudaFail(ctx, e_, what); \
+  } while (0)
+
+bool isPow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+int validateGridDesc(DdgiContext* ctx, const DdgiGridDesc* d) {
+  if (!d) return fail(ctx, DDGI_EINVAL, "grid desc is NULL");
+  for (int i = 0; i < 3; ++i)
+    if (d->dims[i] <= 0 || d->dims[i] > 4096) return fail(ctx, DDGI_EINVAL, "grid dims[%d]=%d out of range", i, d->dims[i]);
+  for (int i = 0; i < 3; ++i)
+    if (!(d->step[i] > 0.0f) || !std::isfinite(d->step[i])) return fail(ctx, DDGI_EINVAL, "grid step[%d] must be > 0", i);
+  if (!isPow2(d->raysPerProbe) || d->raysPerProbe < 16 || d->raysPerProbe > 1024)
+    return fail(ctx, DDGI_EINVAL, "raysPerProbe=%d must be a power of two in [16, 1024]", d->raysPerProbe);
+  if (d->atlasFormat != DDGI_FORMAT_RGBA32F && d->atlasFormat != DDGI_FORMAT_RGBA16F)
+    return fail(ctx, DDGI_EINVAL, "atlasFormat=%d unknown", d->atlasFormat);
+  if (!(d->hysteresis >= 0.0f && d->hysteresis <= 1.0f)) return fail(ctx, DDGI_EINVAL, "hysteresis must be in [0,1]");
+  if (d->options & ~(DDGI_GRID_EDGE_CLAMP | DDGI_GRID_WRITE_DIRS | DDGI_GRID_RECORD_HITS))
+    return fail(ctx, DDGI_EINVAL, "unknown grid option bits 0x%x", d->options);
+  long long aw = (long long)kProbePix * d->dims[0], ah = (long long)kProbePix * d->dims[2] * d->dims[1];
+  if (aw * ah > (1ll << 31)) return fail(ctx, DDGI_EINVAL, "atlas too large");
+  return DDGI_OK;
+}
+
+GridGPU makeGridGPU(const DdgiGridDesc& d) {
+  GridGPU g{};
+  g.X = d.dims[0];
+  g.Y = d.dims[1];
+  g.Z = d.dims[2];
+  g.N = d.raysPerProbe;
+  rayBlock(g.N, g.bw, g.bh);
+  g.step = f3(d.step[0], d.step[1], d.step[2]);
+  g.originY = d.originY;
+  g.atlasW = kProbePix * g.X;
+  g.atlasH = kProbePix * g.Z * g.Y;
+  g.atlasFmt = d.atlasFormat;
+  g.rayW = g.bw * g.X;
+  g.options = d.options;
+  return g;
+}
+
+int frameToGPU(DdgiContext* ctx, const DdgiFrame* f, FrameGPU& out) {
+  if (!f) return fail(ctx, DDGI_EINVAL, "frame is NULL");
+  out.camPos = f3(f->cameraPos[0], f->cameraPos[1], f->cameraPos[2]);
+  out.lightDir = f3(f->lightDir[0], f->lightDir[1], f->lightDir[2]);
+  out.skyColor = f3(f->skyColor[0], f->skyColor[1], f->skyColor[2]);
+  out.sunIntensity = f->sunIntensity;
+  out.skyIntensity = f->skyIntensity;
+  out.flags = f->flags;
+  for (int i = 0; i < 3; ++i) out.bakeTile[i] = f->bakeTileInfo[i];
+  if ((f->flags & DDGI_UBO_BAKE_MODE_ON_FLAG) && f->bakeTileInfo[2] <= 0)
+    return fail(ctx, DDGI_EINVAL, "bake mode needs bakeTileInfo[2] (tile size) > 0");
+  return DDGI_OK;
+}
+
+// Layer range of a frame: -1 all, >= 0 one layer, -2 the grid's round-robin layer.
+int layerRange(DdgiGrid* grid, int layer, bool advance, int& b, int& e) {
+  if (layer == -1) { b = 0; e = grid->g.Y; return DDGI_OK; }
+  if (layer == -2) {
+    b = grid->currentLayer;
+    e = b + 1;
+    if (advance) grid->currentLayer = (grid->currentLayer + 1) % grid->g.Y;
+    return DDGI_OK;
+  }
+  if (layer < 0 || layer >= grid->g.Y) return fail(grid->ctx, DDGI_EINVAL, "layer %d out of range", layer);
+  b = layer;
+  e = layer + 1;
+  return DDGI_OK;
+}
+
+bool invert3(const float* m12, float* out9) {
+  // inverse of the 3x3 part of a row-major 3x4 matrix, in double
+  double a[9] = {m12[0], m12[1], m12[2], m12[4], m12[5], m12[6], m12[8], m12[9], m12[10]};
+  double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8], c02 = a[3] * a[7] - a[4] * a[6];
+  double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  if (!(std::fabs(det) > 1e-30) || !std::isfinite(det)) return false;
+  double inv[9] = {c00, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4],
+                   c01, a[0] * a[8] - a[2] * a[6], a[2] * a[3] - a[0] * a[5],
+                   c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
+  for (int i = 0; i < 9; ++i) out9[i] = (float)(inv[i] / det);
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddgi_abi_version(void) { return DDGI_ABI_VERSION; }
+
+int ddgi_context_create(int device, DdgiContext** out) {
+  if (!out) return DDGI_EINVAL;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return DDGI_EDEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return DDGI_EDEVICE;
+  DdgiContext* ctx = new (std::nothrow) DdgiContext();
+  if (!ctx) return DDGI_ENOMEM;
+  ctx->device = device;
+  cudaDeviceGetAttribute(&ctx->numSms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaMalloc(&ctx->dErr, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(ctx->dErr, 0, sizeof(uint32_t)) != cudaSuccess) {
+    cudaFree(ctx->dErr);
+    delete ctx;
+    return DDGI_ENOMEM;
+  }
+  *out = ctx;
+  return DDGI_OK;
+}
+
+void ddgi_context_destroy(DdgiContext* ctx) {
+  if (!ctx) return;
+  cudaFree(ctx->dErr);
+  delete ctx;
+}
+
+const char* ddgi_last_error(const DdgiContext* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int ddgi_sync(DdgiContext* ctx, void* stream) {
+  if (!ctx) return DDGI_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaStreamSynchronize(s), "stream synchronize");
+  uint32_t w = 0;
+  CK(cudaMemcpy(&w, ctx->dErr, sizeof(w), cudaMemcpyDeviceToHost), "read device error word");
+  if (w) {
+    CK(cudaMemset(ctx->dErr, 0, sizeof(uint32_t)), "clear device error word");
+    if (w & DDGI_DEVERR_STACK_OVERFLOW) return fail(ctx, DDGI_EOVERFLOW, "traversal stack overflow (word 0x%x)", w);
+    if (w & DDGI_DEVERR_TIMEOUT) return fail(ctx, DDGI_ETIMEDOUT, "device wait timed out (word 0x%x)", w);
+    return fail(ctx, DDGI_EOVERFLOW, "device bounds check failed (word 0x%x)", w);
+  }
+  return DDGI_OK;
+}
+
+// ---- scene ------------------------------------------------------------------------------------------
+int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, DdgiScene** out) {
+  if (!ctx || !d || !out) return fail(ctx, DDGI_EINVAL, "NULL argument to ddgi_scene_create");
+  *out = nullptr;
+  if (d->numMeshes && !d->meshes) return fail(ctx, DDGI_EINVAL, "meshes is NULL");
+  if (d->numInstances && !d->instances) return fail(ctx, DDGI_EINVAL, "instances is NULL");
+  if (d->numMaterials && !d->materials) return fail(ctx, DDGI_EINVAL, "materials is NULL");
+  if (d->numVertices && !d->vertices) return fail(ctx, DDGI_EINVAL, "vertices is NULL");
+  if (d->numIndices && !d->indices) return fail(ctx, DDGI_EINVAL, "indices is NULL");
+  // meshes: ranges inside the arrays, every index inside its mesh's vertex range
+  for (uint32_t m = 0; m < d->numMeshes; ++m) {
+    const DdgiMeshInfo& mi = d->meshes[m];
+    if (mi.numIndices % 3) return fail(ctx, DDGI_EINVAL, "mesh %u: numIndices %u not a multiple of 3", m, mi.numIndices);
+    if ((uint64_t)mi.indexOffset + mi.numIndices > d->numIndices)
+      return fail(ctx, DDGI_EINVAL, "mesh %u: index range beyond numIndices", m);
+    if ((uint64_t)mi.vertexOffset + mi.numVertices > d->numVertices)
+      return fail(ctx, DDGI_EINVAL, "mesh %u: vertex range beyond numVertices", m);
+    for (uint32_t k = 0; k < mi.numIndices; ++k)
+      if (d->indices[(uint64_t)mi.indexOffset + k] >= mi.numVertices)
+        return fail(ctx, DDGI_EINVAL, "mesh %u: index %u out of its vertex range", m, k);
+  }
+  for (uint32_t m = 0; m < d->numMaterials; ++m)
+    for (int k = 0; k < 4; ++k)
+      if (d->materials[m].bindlessIndices[k] != -1)
+        return fail(ctx, DDGI_EUNSUPPORTED, "material %u: textures are not supported (bindlessIndices[%d] != -1)", m, k);
+  std::vector<InstanceGPU> inst(d->numInstances);
+  uint64_t tris = 0;
+  for (uint32_t i = 0; i < d->numInstances; ++i) {
+    const DdgiInstance& s = d->instances[i];
+    if (s.mesh >= d->numMeshes) return fail(ctx, DDGI_EINVAL, "instance %u: mesh %u out of range", i, s.mesh);
+    if (s.material >= d->numMaterials) return fail(ctx, DDGI_EINVAL, "instance %u: material %u out of range", i, s.material);
+    InstanceGPU& g = inst[i];
+    memcpy(g.o2w, s.transform, sizeof(g.o2w));
+    if (!invert3(s.transform, g.w2oLin)) return fail(ctx, DDGI_EINVAL, "instance %u: singular transform", i);
+    g.mesh = s.mesh;
+    g.material = s.material;
+    g.triOffset = (uint32_t)tris;
+    tris += d->meshes[s.mesh].numIndices / 3;
+  }
+  if (tris >= (1ull << 30)) return fail(ctx, DDGI_EINVAL, "too many triangles (%llu)", (unsigned long long)tris);
+  CK(cudaSetDevice(ctx->device), "set device");
+  cudaStream_t st = (cudaStream_t)stream;
+  DdgiScene* sc = new (std::nothrow) DdgiScene();
+  if (!sc) return fail(ctx, DDGI_ENOMEM, "host allocation");
+  sc->ctx = ctx;
+  auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = up((void**)&sc->vertices, d->vertices, sizeof(DdgiPackedVertex) * d->numVertices);
+  if (e == cudaSuccess) e = up((void**)&sc->indices, d->indices, sizeof(uint32_t) * d->numIndices);
+  if (e == cudaSuccess) e = up((void**)&sc->meshes, d->meshes, sizeof(DdgiMeshInfo) * d->numMeshes);
+  if (e == cudaSuccess) e = up((void**)&sc->instances, inst.data(), sizeof(InstanceGPU) * inst.size());
+  if (e == cudaSuccess) e = up((void**)&sc->materials, d->materials, sizeof(DdgiMaterialInfo) * d->numMaterials);
+  if (e == cudaSuccess)
+    e = lbvhBuild(sc->instances, (int)d->numInstances, sc->meshes, sc->indices, d->numIndices, sc->vertices,
+                  d->numVertices, (int)tris, ctx->dErr, st, &sc->bvh);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    ddgi_scene_destroy(sc);
+    return cudaFail(ctx, e, "scene upload / BVH build");
+  }
+  sc->view.nodes = sc->bvh.nodes;
+  sc->view.tris = sc->bvh.tris;
+  sc->view.numTris = (int)tris;
+  sc->view.vertices = sc->vertices;
+  sc->view.indices = sc->indices;
+  sc->view.meshes = sc->meshes;
+  sc->view.instances = sc->instances;
+  sc->view.materials = sc->materials;
+  sc->info.numTriangles = tris;
+  sc->info.numNodes = (uint64_t)sc->bvh.numNodes;
+  sc->info.deviceBytes = sizeof(DdgiPackedVertex) * d->numVertices + 4ull * d->numIndices +
+                         sizeof(DdgiMeshInfo) * d->numMeshes + sizeof(InstanceGPU) * inst.size() +
+                         sizeof(DdgiMaterialInfo) * d->numMaterials + 48ull * tris +
+                         64ull * (tris > 1 ? tris - 1 : 1);
+  for (int k = 0; k < 3; ++k) {
+    sc->info.boundsMin[k] = sc->bvh.centroidLo[k];
+    sc->info.boundsMax[k] = sc->bvh.centroidHi[k];
+  }
+  *out = sc;
+  return DDGI_OK;
+}
+
+void ddgi_scene_destroy(DdgiScene* s) {
+  if (!s) return;
+  cudaFree(s->vertices);
+  cudaFree(s->indices);
+  cudaFree(s->meshes);
+  cudaFree(s->instances);
+  cudaFree(s->materials);
+  lbvhFree(&s->bvh);
+  delete s;
+}
+
+int ddgi_scene_info(const DdgiScene* s, DdgiSceneInfo* info) {
+  if (!s || !info) return DDGI_EINVAL;
+  *info = s->info;
+  return DDGI_OK;
+}
+
+// ---- grid -------------------------------------------------------------------------------------------
+int ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out) {
+  if (!ctx || !out) return fail(ctx, DDGI_EINVAL, "NULL argument to ddgi_grid_create");
+  *out = nullptr;
+  int rc = validateGridDesc(ctx, desc);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device), "set device");
+  DdgiGrid* g = new (std::nothrow) DdgiGrid();
+  if (!g) return fail(ctx, DDGI_ENOMEM, "host allocation");
+  g->ctx = ctx;
+  g->desc = *desc;
+  g->g = makeGridGPU(*desc);
+  size_t texel = desc->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
+  g->atlasBytes = (uint64_t)g->g.atlasW * g->g.atlasH * texel;
+  g->rayH = g->g.bh * g->g.Z * g->g.Y;
+  size_t rayTexels = (size_t)g->g.rayW * g->rayH;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&g->atlas[0], g->atlasBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&g->atlas[1], g->atlasBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&g->rayRad, 16 * rayTexels);
+  if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = cudaMalloc(&g->rayDir, 16 * rayTexels);
+  if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = cudaMalloc(&g->rayHit, 4 * rayTexels);
+  if (e == cudaSuccess) e = cudaMalloc(&g->lattice, 16 * (size_t)g->g.N);
+  if (e == cudaSuccess) e = cudaMalloc(&g->wt, 4 * (size_t)g->g.N * kOctTexels);
+  if (e == cudaSuccess) e = cudaMalloc(&g->wsum, 4 * kOctTexels);
+  if (e == cudaSuccess) e = cudaMemset(g->rayRad, 0, 16 * rayTexels);
+  if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    ddgi_grid_destroy(g);
+    return cudaFail(ctx, e, "grid allocation");
+  }
+  *out = g;
+  return DDGI_OK;
+}
+
+void ddgi_grid_destroy(DdgiGrid* g) {
+  if (!g) return;
+  cudaFree(g->atlas[0]);
+  cudaFree(g->atlas[1]);
+  cudaFree(g->rayRad);
+  cudaFree(g->rayDir);
+  cudaFree(g->rayHit);
+  cudaFree(g->lattice);
+  cudaFree(g->wt);
+  cudaFree(g->wsum);
+  delete g;
+}
+
+int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
+  if (!g || !o) return DDGI_EINVAL;
+  o->atlas = g->atlas[g->cur];
+  o->rayRadiance = (float*)g->rayRad;
+  o->rayDirection = (float*)g->rayDir;
+  o->rayHit = g->rayHit;
+  o->lattice = (float*)g->lattice;
+  o->atlasWidth = g->g.atlasW;
+  o->atlasHeight = g->g.atlasH;
+  o->rayWidth = g->g.rayW;
+  o->rayHeight = g->rayH;
+  o->rayBlockW = g->g.bw;
+  o->rayBlockH = g->g.bh;
+  o->atlasBytes = g->atlasBytes;
+  return DDGI_OK;
+}
+
+int ddgi_grid_reset(DdgiGrid* g, void* stream) {
+  if (!g) return DDGI_EINVAL;
+  DdgiContext* ctx = g->ctx;
+  CK(launchClearAtlas(g->g, g->atlas[g->cur], (cudaStream_t)stream), "clear atlas");
+  g->lastProbeIdx[0] = g->lastProbeIdx[1] = 0;
+  g->currentLayer = 0;
+  return DDGI_OK;
+}
+
+int ddgi_translate(DdgiGrid* g, const float cameraPos[3], int* moved, void* stream) {
+  if (!g || !cameraPos) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_translate");
+  DdgiContext* ctx = g->ctx;
+  if (moved) *moved = 0;
+  // IrradianceProbeTranslationPass.cpp:61-80: int() truncation, shift by the sign of the difference
+  int ix = (int)(cameraPos[0] / g->desc.step[0]);
+  int iz = (int)(cameraPos[2] / g->desc.step[2]);
+  int dx = ix - g->lastProbeIdx[0], dz = iz - g->lastProbeIdx[1];
+  if (dx == 0 && dz == 0) return DDGI_OK;
+  g->lastProbeIdx[0] = ix;
+  g->lastProbeIdx[1] = iz;
+  int sx = dx > 0 ? 1 : (dx < 0 ? -1 : 0), sz = dz > 0 ? 1 : (dz < 0 ? -1 : 0);
+  CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, (cudaStream_t)stream), "translate");
+  g->cur = 1 - g->cur;
+  if (moved) *moved = 1;
+  return DDGI_OK;
+}
+
+int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void* stream) {
+  if (!g || !scene || !frame) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_trace");
+  DdgiContext* ctx = g->ctx;
+  if (scene->ctx != ctx) return fail(ctx, DDGI_EINVAL, "scene belongs to another context");
+  FrameGPU f{};
+  int rc = frameToGPU(ctx, frame, f);
+  if (rc) return rc;
+  int b, e;
+  rc = layerRange(g, frame->layer, true, b, e);
+  if (rc) return rc;
+  f.layerBegin = b;
+  f.layerEnd = e;
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(launchLattice(g->g.N, frame->rotation, g->lattice, st), "lattice");
+  CK(launchTraceShade(scene->view, g->g, f, g->lattice, g->atlas[g->cur], g->rayRad, g->rayDir, g->rayHit,
+                      ctx->dErr, st),
+     "trace");
+  g->tracedBegin = b;
+  g->tracedEnd = e;
+  g->latticeValid = true;
+  return DDGI_OK;
+}
+
+int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
+  if (!g || !frame) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_convolve");
+  DdgiContext* ctx = g->ctx;
+  if (!g->latticeValid) return fail(ctx, DDGI_EINVAL, "ddgi_convolve before any ddgi_trace on this grid");
+  int b, e;
+  if (frame->layer == -2) {  // the layer the last trace wrote (blackboard "ProbeLayer")
+    b = g->tracedBegin;
+    e = g->tracedEnd;
+  } else {
+    int rc = layerRange(g, frame->layer, false, b, e);
+    if (rc) return rc;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(launchConvWeights(g->g.N, g->lattice, g->wt, g->wsum, st), "conv weights");
+  CK(launchConvFp32(g->g, g->rayRad, g->wt, g->wsum, g->atlas[g->cur], b, e, g->desc.hysteresis, frame->flags, st),
+     "convolve");
+  return DDGI_OK;
+}
+
+int ddgi_update(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void* stream) {
+  if (!g || !scene || !frame) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_update");
+  int rc = DDGI_OK;
+  if (!(frame->flags & DDGI_UBO_BAKE_MODE_ON_FLAG)) {  // translation is skipped while baking (:59)
+    rc = ddgi_translate(g, frame->cameraPos, nullptr, stream);
+    if (rc) return rc;
+  }
+  rc = ddgi_trace(g, scene, frame, stream);
+  if (rc) return rc;
+  // layer -2 convolves the layer the trace just picked (the "ProbeLayer" blackboard value)
+  return ddgi_convolve(g, frame, stream);
+}
+
+int ddgi_atlas_download(DdgiGrid* g, void* host, uint64_t bytes, void* stream) {
+  if (!g || !host) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_download");
+  DdgiContext* ctx = g->ctx;
+  if (bytes != g->atlasBytes) return fail(ctx, DDGI_EINVAL, "atlas is %llu bytes, got %llu",
+                                          (unsigned long long)g->atlasBytes, (unsigned long long)bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(host, g->atlas[g->cur], bytes, cudaMemcpyDeviceToHost, st), "atlas download");
+  CK(cudaStreamSynchronize(st), "atlas download sync");
+  return DDGI_OK;
+}
+
+int ddgi_atlas_upload(DdgiGrid* g, const void* host, uint64_t bytes, void* stream) {
+  if (!g || !host) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_upload");
+  DdgiContext* ctx = g->ctx;
+  if (bytes != g->atlasBytes) return fail(ctx, DDGI_EINVAL, "atlas is %llu bytes, got %llu",
+                                          (unsigned long long)g->atlasBytes, (unsigned long long)bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(g->atlas[g->cur], host, bytes, cudaMemcpyHostToDevice, st), "atlas upload");
+  CK(cudaStreamSynchronize(st), "atlas upload sync");
+  return DDGI_OK;
+}
+
+int ddgi_rays_download(DdgiGrid* g, float* radiance, int32_t* hits, float* lattice, void* stream) {
+  if (!g) return DDGI_EINVAL;
+  DdgiContext* ctx = g->ctx;
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t texels = (size_t)g->g.rayW * g->rayH;
+  if (hits && !g->rayHit) return fail(ctx, DDGI_EINVAL, "grid was created without DDGI_GRID_RECORD_HITS");
+  if (radiance) CK(cudaMemcpyAsync(radiance, g->rayRad, 16 * texels, cudaMemcpyDeviceToHost, st), "ray download");
+  if (hits) CK(cudaMemcpyAsync(hits, g->rayHit, 4 * texels, cudaMemcpyDeviceToHost, st), "hit download");
+  if (lattice) CK(cudaMemcpyAsync(lattice, g->lattice, 16 * (size_t)g->g.N, cudaMemcpyDeviceToHost, st), "lattice download");
+  CK(cudaStreamSynchronize(st), "ray download sync");
+  return DDGI_OK;
+}
+
+// ---- raw kernels --------------------------------------------------------------------------------------
+int ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* stream) {
+  if (numRays <= 0 || numRays > (1 << 20) || !rot || !dirs) return DDGI_EINVAL;
+  return launchLattice(numRays, rot, (float4*)dirs, (cudaStream_t)stream) == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
+}
+
+int ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs, void* atlas,
+                      int layerBegin, int layerEnd, uint32_t flags, void* stream) {
+  if (validateGridDesc(nullptr, desc) != DDGI_OK || !rayRadiance || !dirs || !atlas) return DDGI_EINVAL;
+  if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return DDGI_EINVAL;
+  GridGPU g = makeGridGPU(*desc);
+  float* wt = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  // weights + sums in one scratch allocation, released after the stream has consumed it
+  if (cudaMallocAsync(&wt, 4 * ((size_t)g.N * kOctTexels + kOctTexels), st) != cudaSuccess) return DDGI_ENOMEM;
+  float* ws = wt + (size_t)g.N * kOctTexels;
+  cudaError_t e = launchConvWeights(g.N, (const float4*)dirs, wt, ws, st);
+  if (e == cudaSuccess)
+    e = launchConvFp32(g, (const float4*)rayRadiance, wt, ws, atlas, layerBegin, layerEnd, desc->hysteresis, flags, st);
+  cudaFreeAsync(wt, st);
+  return e == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
+}
+
+int ddgi_translate_raw(const DdgiGridDesc* desc, const void* atlasIn, void* atlasOut, int dx, int dz, void* stream) {
+  if (validateGridDesc(nullptr, desc) != DDGI_OK || !atlasIn || !atlasOut || atlasIn == atlasOut) return DDGI_EINVAL;
+  GridGPU g = makeGridGPU(*desc);
+  int sx = dx > 0 ? 1 : (dx < 0 ? -1 : 0), sz = dz > 0 ? 1 : (dz < 0 ? -1 : 0);
+  return launchTranslate(g, atlasIn, atlasOut, sx, sz, (cudaStream_t)stream) == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
+}
+
+}  // extern "C"

@@ -1,0 +1,20 @@
+// LBVH build interface (see lbvh.cu).
+#pragma once
+#include "ddgi_common.cuh"
+
+namespace ddgi {
+
+struct LbvhResult {
+  float4* nodes = nullptr;  // 4 float4 per internal node (numNodes of them), root = 0
+  float4* tris = nullptr;   // 3 float4 per leaf, leaf order
+  int numTris = 0;
+  int numNodes = 0;
+  float centroidLo[3] = {0, 0, 0}, centroidHi[3] = {0, 0, 0};
+};
+
+cudaError_t lbvhBuild(const InstanceGPU* dInst, int numInst, const DdgiMeshInfo* dMeshes,
+                      const uint32_t* dIndices, uint64_t numIndices, const DdgiPackedVertex* dVerts,
+                      uint64_t numVerts, int numTris, uint32_t* dErr, cudaStream_t stream, LbvhResult* out);
+void lbvhFree(LbvhResult* r);
+
+}  // namespace ddgi

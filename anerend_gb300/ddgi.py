@@ -1,0 +1,206 @@
+"""Python host mirror of the reference's probe-update passes over the C ABI (include/ddgi.h).
+
+The reference drives the path with three RenderPass objects
+(src/anerend/render/passes/IrradianceProbe{Translation,RayTracing,Convolve}Pass.cpp); the classes of the same
+names below keep their execution order and state (translation's last probe index, the round-robin layer,
+the "ProbeLayer" hand-off) but run on a ProbeGrid + Scene owned by a Context. Errors raise DdgiError with the
+library's status code and message; nothing here computes on the CPU."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+from .scenes import Scene as SceneArrays
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data if a is not None and a.size else 0
+
+
+class Context:
+    """DdgiContext on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = C.c_void_p()
+        rc = self.lib.ddgi_context_create(device, C.byref(h))
+        if rc != L.DDGI_OK:
+            raise L.DdgiError(rc, f"ddgi_context_create(device={device}) failed")
+        self.handle = h
+
+    def check(self, rc: int) -> None:
+        if rc != L.DDGI_OK:
+            msg = self.lib.ddgi_last_error(self.handle)
+            raise L.DdgiError(rc, msg.decode() if msg else "")
+
+    def sync(self, stream: int = 0) -> None:
+        self.check(self.lib.ddgi_sync(self.handle, stream))
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.ddgi_context_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Scene:
+    """Resident scene + LBVH (DdgiScene)."""
+
+    def __init__(self, ctx: Context, arrays: SceneArrays, stream: int = 0):
+        self.ctx = ctx
+        self.arrays = arrays
+        d = L.SceneDesc(_ptr(arrays.vertices), len(arrays.vertices), _ptr(arrays.indices), len(arrays.indices),
+                        _ptr(arrays.meshes), len(arrays.meshes), _ptr(arrays.instances), len(arrays.instances),
+                        _ptr(arrays.materials), len(arrays.materials))
+        h = C.c_void_p()
+        ctx.check(ctx.lib.ddgi_scene_create(ctx.handle, C.byref(d), stream, C.byref(h)))
+        self.handle = h
+
+    @property
+    def info(self) -> L.SceneInfo:
+        i = L.SceneInfo()
+        self.ctx.check(self.ctx.lib.ddgi_scene_info(self.handle, C.byref(i)))
+        return i
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.ddgi_scene_destroy(self.handle)
+            self.handle = None
+
+
+@dataclass
+class FrameParams:
+    """Per-frame UBO fields and push constants of the path (scene_ubo.glsl:14-37, rgen:26-29)."""
+    camera_pos: tuple = (0.0, 0.0, 0.0)
+    light_dir: tuple = (-0.3, -1.0, -0.2)
+    sun_intensity: float = 3.0
+    sky_color: tuple = (0.4, 0.5, 0.7)
+    sky_intensity: float = 1.0
+    flags: int = L.DDGI_UBO_DDGI_FLAG | L.DDGI_UBO_DDGI_MULTI_FLAG
+    rotation: np.ndarray = field(default_factory=lambda: np.eye(3, dtype=np.float32).reshape(-1))
+    layer: int = -1
+    bake_tile: tuple = (0, 0, 0)
+
+    def to_c(self) -> L.Frame:
+        f = L.Frame()
+        f.cameraPos[:] = [float(v) for v in self.camera_pos]
+        ld = np.asarray(self.light_dir, np.float64)
+        ld = ld / np.linalg.norm(ld)
+        f.lightDir[:] = [float(v) for v in ld.astype(np.float32)]
+        f.sunIntensity = self.sun_intensity
+        f.skyColor[:] = [float(v) for v in self.sky_color]
+        f.skyIntensity = self.sky_intensity
+        f.flags = self.flags
+        f.rotation[:] = [float(v) for v in np.asarray(self.rotation, np.float32).reshape(-1)]
+        f.layer = self.layer
+        f.bakeTileInfo[:] = list(self.bake_tile)
+        return f
+
+
+class ProbeGrid:
+    """Probe grid with its atlas, translation temp and ray images (DdgiGrid)."""
+
+    def __init__(self, ctx: Context, dims, step=(1.0, 2.0, 1.0), rays_per_probe: int = 256, origin_y: float = 0.0,
+                 hysteresis: float = 0.96, atlas_format: int = L.DDGI_FORMAT_RGBA32F, options: int = 0):
+        self.ctx = ctx
+        self.desc = L.GridDesc()
+        self.desc.dims[:] = list(dims)
+        self.desc.step[:] = list(step)
+        self.desc.originY = origin_y
+        self.desc.raysPerProbe = rays_per_probe
+        self.desc.atlasFormat = atlas_format
+        self.desc.hysteresis = hysteresis
+        self.desc.options = options
+        h = C.c_void_p()
+        ctx.check(ctx.lib.ddgi_grid_create(ctx.handle, C.byref(self.desc), C.byref(h)))
+        self.handle = h
+
+    @property
+    def buffers(self) -> L.GridBuffers:
+        b = L.GridBuffers()
+        self.ctx.check(self.ctx.lib.ddgi_grid_buffers(self.handle, C.byref(b)))
+        return b
+
+    def reset(self, stream: int = 0) -> None:
+        self.ctx.check(self.ctx.lib.ddgi_grid_reset(self.handle, stream))
+
+    def translate(self, camera_pos, stream: int = 0) -> bool:
+        cp = (C.c_float * 3)(*camera_pos)
+        moved = C.c_int(0)
+        self.ctx.check(self.ctx.lib.ddgi_translate(self.handle, cp, C.byref(moved), stream))
+        return bool(moved.value)
+
+    def trace(self, scene: Scene, frame: FrameParams, stream: int = 0) -> None:
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_trace(self.handle, scene.handle, C.byref(f), stream))
+
+    def convolve(self, frame: FrameParams, stream: int = 0) -> None:
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_convolve(self.handle, C.byref(f), stream))
+
+    def update(self, scene: Scene, frame: FrameParams, stream: int = 0) -> None:
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_update(self.handle, scene.handle, C.byref(f), stream))
+
+    def atlas_shape(self) -> tuple:
+        b = self.buffers
+        return (b.atlasHeight, b.atlasWidth, 4)
+
+    def download_atlas(self, stream: int = 0) -> np.ndarray:
+        b = self.buffers
+        dt = np.float32 if self.desc.atlasFormat == L.DDGI_FORMAT_RGBA32F else np.float16
+        out = np.empty((b.atlasHeight, b.atlasWidth, 4), dt)
+        self.ctx.check(self.ctx.lib.ddgi_atlas_download(self.handle, _ptr(out), out.nbytes, stream))
+        return out
+
+    def upload_atlas(self, arr: np.ndarray, stream: int = 0) -> None:
+        arr = np.ascontiguousarray(arr)
+        self.ctx.check(self.ctx.lib.ddgi_atlas_upload(self.handle, _ptr(arr), arr.nbytes, stream))
+
+    def download_rays(self, hits: bool = False, stream: int = 0):
+        b = self.buffers
+        rad = np.empty((b.rayHeight, b.rayWidth, 4), np.float32)
+        hit = np.empty((b.rayHeight, b.rayWidth), np.int32) if hits else None
+        lat = np.empty((self.desc.raysPerProbe, 4), np.float32)
+        self.ctx.check(self.ctx.lib.ddgi_rays_download(self.handle, _ptr(rad), _ptr(hit) if hits else None,
+                                                       _ptr(lat), stream))
+        return rad, hit, lat
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.ddgi_grid_destroy(self.handle)
+            self.handle = None
+
+
+# ---- the reference's three passes -----------------------------------------------------------------
+
+class IrradianceProbeTranslationPass:
+    """IrradianceProbeTranslationPass.cpp:56-186: shift the atlas when the camera's probe index changes.
+    Skipped while baking (:59)."""
+
+    def execute(self, grid: ProbeGrid, frame: FrameParams, stream: int = 0) -> bool:
+        if frame.flags & L.DDGI_UBO_BAKE_MODE_ON_FLAG:
+            return False
+        return grid.translate(frame.camera_pos, stream)
+
+
+class IrradianceProbeRayTracingPass:
+    """IrradianceProbeRayTracingPass.cpp:95-165: trace one layer (round robin, frame.layer == -2) or all."""
+
+    def execute(self, grid: ProbeGrid, scene: Scene, frame: FrameParams, stream: int = 0) -> None:
+        grid.trace(scene, frame, stream)
+
+
+class IrradianceProbeConvolvePass:
+    """IrradianceProbeConvolvePass.cpp:109-143: convolve the layer(s) the ray-tracing pass wrote."""
+
+    def execute(self, grid: ProbeGrid, frame: FrameParams, stream: int = 0) -> None:
+        grid.convolve(frame, stream)

@@ -1,0 +1,250 @@
+/*
+ * ddgi.h — C ABI of the GB300 (sm_103a) DDGI probe-update engine.
+ *
+ * This boundary replaces three render passes of AneRend and the GPU programs they launch:
+ *   IrradianceProbeTranslationPass  (src/anerend/render/passes/IrradianceProbeTranslationPass.cpp:56-186)
+ *   IrradianceProbeRayTracingPass   (src/anerend/render/passes/IrradianceProbeRayTracingPass.cpp:28-166,
+ *                                    assets/shaders/irradiance_probe_update.{rgen,rchit,rmiss})
+ *   IrradianceProbeConvolvePass     (src/anerend/render/passes/IrradianceProbeConvolvePass.cpp:9-143,
+ *                                    assets/shaders/probe_conv.comp)
+ * The reference drives them through RenderPass::registerToGraph + an exe lambda per frame
+ * (src/anerend/render/passes/RenderPass.h:14-35, FrameGraphBuilder.h:22-42); here every entry point is a
+ * plain C function that takes plain pointers and sizes and returns an int status (DDGI_OK or a negative
+ * DDGI_E* code). No exception crosses the boundary. The last error text is kept per context.
+ *
+ * Buffer layouts are the reference's:
+ *   - ray images ("ProbeRaysIrrTex"/"ProbeRaysDirTex", IrradianceProbeRayTracingPass.cpp:42-74): one RGBA
+ *     texel per ray, (bw*X) x (bh*Z) texels per probe layer, the N rays of probe (x,z) in a bw x bh block at
+ *     (bw*x, bh*z), ray index = row*bw + col (irradiance_probe_update.rgen:51-58). The reference has N=256,
+ *     bw=bh=16; for other N, bw = 2^ceil(log2(N)/2) and bh = N/bw. Layers are stacked vertically.
+ *   - atlas ("ProbeRaysConvTex", IrradianceProbeConvolvePass.cpp:62-99): RGBA, width 10*X, height 10*Z*Y,
+ *     the 8x8 interior of probe (x,y,z) at texel (10x+1, 10*Z*y + 10z + 1), one texel border, cleared to
+ *     (0,0,0,1) (clearConvTex, IrradianceProbeConvolvePass.cpp:9-47).
+ *   - scene records: PackedVertex (bindless.glsl:60-68), MeshInfo (bindless.glsl:51-58),
+ *     MaterialInfo (bindless.glsl:43-49 = GPUMaterialInfo, GpuBuffers.h:29-36).
+ *
+ * Streams are passed as void* (a cudaStream_t; NULL = the legacy default stream).
+ */
+#ifndef DDGI_H
+#define DDGI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DDGI_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------------------- */
+#define DDGI_OK            0
+#define DDGI_EINVAL       -1   /* bad argument (null pointer, size mismatch, unsupported value)      */
+#define DDGI_ENOMEM       -2   /* device or host allocation failed                                   */
+#define DDGI_ETIMEDOUT    -3   /* a bounded device wait gave up                                       */
+#define DDGI_EDEVICE      -4   /* CUDA runtime error                                                  */
+#define DDGI_EUNSUPPORTED -5   /* feature not available in this build (e.g. textured materials)      */
+#define DDGI_EOVERFLOW    -6   /* a device-side bound was hit (traversal stack); work was skipped     */
+#define DDGI_EBUSY        -7   /* admission refused (serving: memory budget / slots)                  */
+
+/* ---- scene UBO flag bits: the values of scene_ubo.glsl:1-12 (GpuBuffers.h:108-122) ---------------- */
+#define DDGI_UBO_DDGI_FLAG          (1u << 4)
+#define DDGI_UBO_DDGI_MULTI_FLAG    (1u << 5)   /* previous-frame probe lookup in the hit shader (rchit:208) */
+#define DDGI_UBO_BAKE_MODE_ON_FLAG  (1u << 11)  /* bake: tile origin + accumulate (probe_conv.comp:307-319) */
+
+/* ---- texel formats ----------------------------------------------------------------------------- */
+#define DDGI_FORMAT_RGBA32F 0   /* 16 B per texel                                                    */
+#define DDGI_FORMAT_RGBA16F 1   /* 8 B per texel, the reference's VK_FORMAT_R16G16B16A16_SFLOAT      */
+
+/* ---- grid options (DdgiGridDesc.options) --------------------------------------------------------- */
+#define DDGI_GRID_EDGE_CLAMP   (1u << 0) /* clamp the +1 lookup neighbour at the grid edge instead of
+                                            wrapping like the reference's REPEAT sampler does          */
+#define DDGI_GRID_WRITE_DIRS   (1u << 1) /* also write the per-ray direction image (ProbeRaysDirTex)     */
+#define DDGI_GRID_RECORD_HITS  (1u << 2) /* keep a per-ray hit record (global triangle id, shadow bit)   */
+
+/* ---- scene records --------------------------------------------------------------------------------- */
+
+/* PackedVertex, bindless.glsl:60-68 (96 B): pos=d0.xyz, color=(d0.w,d1.xy), normal=(d1.zw,d2.x),
+ * tangent=(d2.yzw,d3.x), jointWeights=(d3.yzw,d4.x), uv=d4.yz, jointIds=d5 (unpackVertex, :98-109). */
+typedef struct DdgiPackedVertex {
+  float   d0[4], d1[4], d2[4], d3[4], d4[4];
+  int32_t d5[4];
+} DdgiPackedVertex;
+
+/* MeshInfo, bindless.glsl:51-58 (48 B). The reference's 8-byte blasRef slot carries the mesh's index and
+ * vertex counts here, because this engine builds its own BVH instead of referencing a driver BLAS. */
+typedef struct DdgiMeshInfo {
+  float    minPos[4];
+  float    maxPos[4];
+  uint32_t vertexOffset;   /* in vertices */
+  uint32_t indexOffset;    /* in indices  */
+  uint32_t numIndices;     /* multiple of 3 */
+  uint32_t numVertices;
+} DdgiMeshInfo;
+
+/* MaterialInfo, bindless.glsl:43-49 / GPUMaterialInfo, GpuBuffers.h:29-36 (64 B).
+ * Textures are not part of this path: every bindlessIndices entry must be -1 (getSurfaceDataFromMat,
+ * bindless.glsl:181-237, then takes baseColFac / metRough / emissive directly). */
+typedef struct DdgiMaterialInfo {
+  float   baseColFac[4];
+  float   emissive[4];        /* rgb * w is the emitted radiance */
+  int32_t bindlessIndices[4]; /* metRough, albedo, normal, emissive: all -1 */
+  float   metRough[4];        /* r metallic, g roughness */
+} DdgiMaterialInfo;
+
+/* One TLAS instance (tlas_update.comp:57-98): a 3x4 row-major object-to-world matrix (VkTransformMatrix
+ * order), the mesh and the material. The reference packs material into customIndex bits 0-9 and mesh into
+ * bits 10-23 (tlas_update.comp:87-92, decoded at irradiance_probe_update.rchit:137-138); here they are
+ * separate 32-bit fields. All instances are double-sided opaque triangles (facing-cull disabled, :87). */
+typedef struct DdgiInstance {
+  float    transform[12];
+  uint32_t mesh;
+  uint32_t material;
+  uint32_t reserved[2];
+} DdgiInstance;
+
+typedef struct DdgiSceneDesc {
+  const DdgiPackedVertex* vertices;  uint64_t numVertices;
+  const uint32_t*         indices;   uint64_t numIndices;
+  const DdgiMeshInfo*     meshes;    uint32_t numMeshes;
+  const DdgiInstance*     instances; uint32_t numInstances;
+  const DdgiMaterialInfo* materials; uint32_t numMaterials;
+} DdgiSceneDesc;
+
+typedef struct DdgiSceneInfo {
+  uint64_t numTriangles;   /* instance triangles after flattening */
+  uint64_t numNodes;       /* internal BVH nodes */
+  uint64_t deviceBytes;    /* device memory held by the scene */
+  float    boundsMin[3], boundsMax[3];
+} DdgiSceneInfo;
+
+/* ---- probe grid ------------------------------------------------------------------------------------ */
+
+/* Replaces the compile-time constants of probe_helpers.glsl:1-7 (64 x 8 x 64, step (1,2,1), N = 256,
+ * 16x16 ray block, 8x8 octahedral texels) and the literals of the three passes. */
+typedef struct DdgiGridDesc {
+  int32_t  dims[3];        /* X, Y (layers), Z: the reference's NUM_PROBES_PER_PLANE, NUM_PROBE_PLANES, NUM_PROBES_PER_PLANE */
+  float    step[3];        /* PROBE_STEP */
+  float    originY;        /* world y of layer 0; the reference's grid starts at y = 0 */
+  int32_t  raysPerProbe;   /* N, a power of two in [16, 1024]; the reference uses 256 */
+  int32_t  atlasFormat;    /* DDGI_FORMAT_* */
+  float    hysteresis;     /* probe_conv.comp:325 uses 0.96 */
+  uint32_t options;        /* DDGI_GRID_* */
+} DdgiGridDesc;
+
+/* Per-frame inputs: the scene UBO fields this path reads (scene_ubo.glsl:14-37, filled at
+ * VulkanRenderer.cpp:1201-1242) and the push constants (irradiance_probe_update.rgen:26-29,
+ * probe_conv.comp:16-18). */
+typedef struct DdgiFrame {
+  float    cameraPos[3];
+  float    lightDir[3];     /* direction the light travels (the shader lights along -lightDir) */
+  float    sunIntensity;
+  float    skyColor[3];
+  float    skyIntensity;
+  uint32_t flags;           /* DDGI_UBO_* bits */
+  float    rotation[9];     /* mat3(randomRot), column-major as glm stores it */
+  int32_t  layer;           /* probe layer to update, or -1 for every layer */
+  int32_t  bakeTileInfo[3]; /* x, y: tile index, z: tile size (bake mode only) */
+} DdgiFrame;
+
+/* Device views of the grid's buffers (owned by the grid). */
+typedef struct DdgiGridBuffers {
+  void*    atlas;           /* current atlas, atlasFormat texels, atlasWidth x atlasHeight */
+  float*   rayRadiance;     /* RGBA32F ray image, rayWidth x rayHeight (all layers stacked) */
+  float*   rayDirection;    /* RGBA32F ray image, or NULL without DDGI_GRID_WRITE_DIRS */
+  int32_t* rayHit;          /* per ray (same texel order): global triangle id or -1; NULL unless RECORD_HITS */
+  float*   lattice;         /* N x float4 rotated ray directions of the last trace */
+  int32_t  atlasWidth, atlasHeight;
+  int32_t  rayWidth, rayHeight;
+  int32_t  rayBlockW, rayBlockH;
+  uint64_t atlasBytes;
+} DdgiGridBuffers;
+
+typedef struct DdgiContext DdgiContext;
+typedef struct DdgiScene   DdgiScene;
+typedef struct DdgiGrid    DdgiGrid;
+
+/* ---- context ------------------------------------------------------------------------------------- */
+
+/* Selects `device` and creates the context (the analogue of the renderer's device + frame-graph state).
+ * Reference: VulkanRenderer::init, VulkanRenderer.cpp:295-407. */
+int         ddgi_context_create(int device, DdgiContext** out);
+void        ddgi_context_destroy(DdgiContext* ctx);
+/* Text of the last failure on this context ("" if none). Valid until the next call on the context. */
+const char* ddgi_last_error(const DdgiContext* ctx);
+/* Waits for `stream` and returns DDGI_EOVERFLOW / DDGI_ETIMEDOUT if a kernel raised the sticky device
+ * error word since the last call (the word is cleared), DDGI_EDEVICE on a CUDA error. */
+int         ddgi_sync(DdgiContext* ctx, void* stream);
+int         ddgi_abi_version(void);
+
+/* ---- scene (replaces BLAS/TLAS builds, VulkanRenderer.cpp:1265-1490, UpdateTLASPass.cpp:128-248) ---- */
+
+/* Copies the host arrays to the device, flattens instances to world-space triangles and builds an LBVH
+ * (Morton codes, radix sort, Karras hierarchy, bottom-up bounds). Triangle t of instance i gets the
+ * global id triOffset(i) + t, instances in array order. Returns when the build has finished. */
+int  ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* desc, void* stream, DdgiScene** out);
+void ddgi_scene_destroy(DdgiScene* scene);
+int  ddgi_scene_info(const DdgiScene* scene, DdgiSceneInfo* info);
+
+/* ---- grid ---------------------------------------------------------------------------------------- */
+
+/* Allocates the atlas (cleared to (0,0,0,1)), the translation temp ("TempProbeTex"), the ray images and
+ * the lattice. The translation state (_lastProbeIdx, IrradianceProbeTranslationPass.h:17) starts at (0,0)
+ * and the round-robin layer at 0. */
+int  ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out);
+void ddgi_grid_destroy(DdgiGrid* grid);
+int  ddgi_grid_buffers(const DdgiGrid* grid, DdgiGridBuffers* out);
+/* Clears the atlas to (0,0,0,1) and the translation state to (0,0). */
+int  ddgi_grid_reset(DdgiGrid* grid, void* stream);
+
+/* IrradianceProbeTranslationPass exe (IrradianceProbeTranslationPass.cpp:56-186): camera probe index by
+ * int() truncation of cameraPos.xz/step; if it changed, shift every layer plane of the atlas by
+ * sign(dx), sign(dz) probes (10 texels), keeping stale texels on the vacated edge. *moved (may be NULL)
+ * receives 1 when a shift was made. */
+int  ddgi_translate(DdgiGrid* grid, const float cameraPos[3], int* moved, void* stream);
+
+/* IrradianceProbeRayTracingPass exe + irradiance_probe_update.{rgen,rchit,rmiss}: traces the rays of
+ * frame->layer (or of every layer if it is -1) against `scene`, shading hits with Cook-Torrance direct
+ * light, a shadow ray and (with DDGI_UBO_DDGI_MULTI_FLAG) the previous-frame probe lookup, and writes the
+ * ray-radiance image. */
+int  ddgi_trace(DdgiGrid* grid, const DdgiScene* scene, const DdgiFrame* frame, void* stream);
+
+/* IrradianceProbeConvolvePass exe + probe_conv.comp: cosine-weighted sum of the rays of each probe into
+ * its 8x8 octahedral texels and the hysteresis blend (bake mode: weighted accumulation). */
+int  ddgi_convolve(DdgiGrid* grid, const DdgiFrame* frame, void* stream);
+
+/* translate + trace + convolve, in the reference's pass order (VulkanRenderer.cpp:4473-4475). With
+ * frame->layer == -2 the grid picks the layer round-robin like IrradianceProbeRayTracingPass.cpp:111-164. */
+int  ddgi_update(DdgiGrid* grid, const DdgiScene* scene, const DdgiFrame* frame, void* stream);
+
+/* Atlas readback / restore in the grid's atlas format (downloadDDGIAtlas, VulkanRenderer.cpp:2706-2771).
+ * `bytes` must equal DdgiGridBuffers.atlasBytes. The download is complete when the call returns. */
+int  ddgi_atlas_download(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
+int  ddgi_atlas_upload(DdgiGrid* grid, const void* host, uint64_t bytes, void* stream);
+
+/* Reads back the grid's ray buffers into host memory (any pointer may be NULL): radiance is
+ * rayWidth*rayHeight RGBA floats, hits rayWidth*rayHeight int32 (needs DDGI_GRID_RECORD_HITS; global triangle
+ * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
+int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
+
+/* ---- raw kernels on caller-owned device memory ------------------------------------------------------- */
+
+/* The golden-angle ray set of irradiance_probe_update.rgen:35-46 rotated by mat3(rot) (rgen:87-88),
+ * computed in FP64 on the device and stored as N float4 (x, y, z, 0). */
+int  ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* stream);
+
+/* probe_conv.comp on device buffers: rayRadiance in the RGBA32F ray-image layout of `desc`, dirs = N float4
+ * lattice, atlas in desc->atlasFormat. Updates layers [layerBegin, layerEnd). flags: DDGI_UBO_* bits. */
+int  ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs, void* atlas,
+                       int layerBegin, int layerEnd, uint32_t flags, void* stream);
+
+/* The translation copy of IrradianceProbeTranslationPass.cpp:83-168 from atlasIn to atlasOut (distinct
+ * buffers, desc->atlasFormat): atlasOut = atlasIn shifted by (sign(dx), sign(dz)) probes per layer plane. */
+int  ddgi_translate_raw(const DdgiGridDesc* desc, const void* atlasIn, void* atlasOut, int dx, int dz,
+                        void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DDGI_H */
