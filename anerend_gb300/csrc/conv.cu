@@ -29,16 +29,24 @@ __global__ void k_conv_weights(int n, const float4* __restrict__ dirs, float* __
   wsum[t] = s;
 }
 
+// kSmemW: the N x 64 weight table is staged in shared memory (N <= 512); otherwise it is read from global
+// memory, where it stays L1/L2-resident (256 KB at N = 1024).
+template <bool kSmemW>
 __global__ void __launch_bounds__(kConvThreads) k_conv_fp32(GridGPU g, const float4* __restrict__ rayRad,
                                                             const float* __restrict__ wt,
                                                             const float* __restrict__ wsum,
                                                             void* __restrict__ atlas, int layerBegin,
                                                             int layerEnd, float hysteresis, uint32_t flags) {
   extern __shared__ float4 smem4[];
-  float* sW = reinterpret_cast<float*>(smem4);           // N * 64
-  float4* sR = smem4 + (g.N * kOctTexels) / 4;           // kConvProbes * N
   const int N = g.N;
-  for (int i = threadIdx.x; i < N * kOctTexels; i += blockDim.x) sW[i] = wt[i];
+  const float* sW = wt;
+  float4* sR = smem4;  // kConvProbes * N
+  if (kSmemW) {
+    float* w = reinterpret_cast<float*>(smem4);  // N * 64
+    for (int i = threadIdx.x; i < N * kOctTexels; i += blockDim.x) w[i] = wt[i];
+    sW = w;
+    sR = smem4 + (N * kOctTexels) / 4;
+  }
   const int t = threadIdx.x % kOctTexels;
   const int q = threadIdx.x / kOctTexels;
   const float ws = wsum[t];
@@ -112,8 +120,11 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream) {
   if (layerEnd <= layerBegin) return cudaSuccess;
-  size_t smem = sizeof(float) * (size_t)g.N * kOctTexels + sizeof(float4) * (size_t)kConvProbes * g.N;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const bool smemW = g.N <= 512;
+  size_t smem = sizeof(float4) * (size_t)kConvProbes * g.N;
+  if (smemW) smem += sizeof(float) * (size_t)g.N * kOctTexels;
+  auto kern = smemW ? k_conv_fp32<true> : k_conv_fp32<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -123,8 +134,8 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
   long long grid = (long long)sms * perSm;
   if (grid > groups) grid = groups;
   if (grid < 1) grid = 1;
-  k_conv_fp32<<<(unsigned)grid, kConvThreads, smem, stream>>>(g, rayRad, wt, wsum, atlas, layerBegin, layerEnd,
-                                                             hysteresis, flags);
+  kern<<<(unsigned)grid, kConvThreads, smem, stream>>>(g, rayRad, wt, wsum, atlas, layerBegin, layerEnd, hysteresis,
+                                                      flags);
   return cudaGetLastError();
 }
 

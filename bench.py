@@ -1,0 +1,360 @@
+"""Benchmark of the DDGI probe update on the 32x8x32-probe / 256-ray / 262,144-triangle single-grid workload.
+
+One step = one probe update of the whole grid: translation (when the camera's probe index changes), the
+rotated golden-angle lattice, trace + shade of all 2,097,152 rays, and the convolution + hysteresis of all
+8192 probes. The camera moves +1 in x every 10 frames, as in the workload definition.
+
+  value      probe rays/s, device-timed (CUDA events on the launching stream), inputs resident in HBM
+  e2e        the same metric through the C ABI from the host: ddgi_update + ddgi_atlas_download into pinned
+             host memory, wall clock per step (host frame parameters in, atlas out)
+  roofline   of the dominant kernel (trace + shade): algorithmic bytes / its event-timed duration vs the
+             measured HBM copy bandwidth
+  cpu_baseline  the FP64 oracle on all host cores over a bounded sample (rank 0, N = 1 only)
+
+--impl reference times the CPU implementation of the path (the oracle restatement; the reference's GLSL
+cannot run on this machine) on the same workload and metric.
+
+Multi-GPU (torchrun): probe grids are independent, so each rank updates its own replica of the grid
+(weak scaling, no data-path collective); a barrier brackets the timed region and the max over ranks is
+reported."""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+METRIC = "probe rays/s"
+UNIT = "rays/s"
+# compulsory bytes of the trace + shade kernel (per primary hit / per miss): 3 indices (12 B), three full
+# 96-byte vertex records (288 B), the material (64 B), the 8-probe x 4-texel FP32 atlas gather (512 B) and
+# the radiance write (12 B); a miss writes the radiance only.
+BYTES_PER_HIT = 12 + 3 * 96 + 64 + 8 * 4 * 16 + 12
+BYTES_PER_MISS = 12
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    return dict(PEAKS_FALLBACK, source="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = open(ROOT / "gpurun_out" / f".clocks_{os.getpid()}.csv", "w") if (ROOT / "gpurun_out").exists() \
+                else open(f"/tmp/.clocks_{os.getpid()}.csv", "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.close()
+        lines = Path(self.out.name).read_text().strip().splitlines()
+        Path(self.out.name).unlink(missing_ok=True)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not dist.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, local, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(w, arrays, frames: int, threads: int = 0):
+    """FP64 oracle on `frames` full probe updates; returns (rays/s, seconds, threads used)."""
+    from anerend_gb300 import _lib as L
+    from anerend_gb300.ddgi import FrameParams
+    from oracle import oracle
+
+    d = L.GridDesc()
+    d.dims[:] = list(w.dims)
+    d.step[:] = list(w.step)
+    d.originY = w.origin_y
+    d.raysPerProbe = w.rays
+    d.hysteresis = w.hysteresis
+    osc = oracle.OracleScene(arrays, L.SceneDesc)
+    og = oracle.OracleGrid(d, threads=threads)
+    t0 = time.perf_counter()
+    from anerend_gb300 import scenes
+
+    for f in range(frames):
+        og.update(osc, FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f)).to_c())
+    dt = time.perf_counter() - t0
+    osc.close()
+    used = threads if threads > 0 else (os.cpu_count() or 1)
+    return frames * w.probes * w.rays / dt, dt, used
+
+
+def run_reference(args, rank, world):
+    """CPU implementation of the path (the FP64 oracle restatement on all host threads), same metric."""
+    from anerend_gb300 import scenes
+
+    if rank != 0:
+        return
+    w = scenes.SINGLE_GRID
+    arrays = scenes.build_scene(w)
+    # each step: one full probe update of the grid is ~3 s on 8 cores; a step here is one layer (1/8 of a
+    # frame: 262,144 rays), so warm-up + steps stay within a few minutes
+    from anerend_gb300 import _lib as L
+    from anerend_gb300.ddgi import FrameParams
+    from oracle import oracle
+
+    d = L.GridDesc()
+    d.dims[:] = list(w.dims)
+    d.step[:] = list(w.step)
+    d.originY = w.origin_y
+    d.raysPerProbe = w.rays
+    d.hysteresis = w.hysteresis
+    osc = oracle.OracleScene(arrays, L.SceneDesc)
+    og = oracle.OracleGrid(d)
+    times = []
+    for s in range(args.warmup + args.steps):
+        fp = FrameParams(camera_pos=scenes.camera(w, s), rotation=scenes.rotation(w.seed, s), layer=s % w.dims[1])
+        t0 = time.perf_counter()
+        og.update(osc, fp.to_c())
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    rays = w.dims[0] * w.dims[2] * w.rays
+    total = sum(times)
+    value = rays * len(times) / total
+    cores = os.cpu_count() or 1
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "probes": w.probes, "rays_per_probe": w.rays,
+                       "triangles": w.num_tris, "step_unit": "one probe layer (32x32 probes x 256 rays)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} single-layer updates of 262,144 rays, FP64 oracle, std::thread x {cores}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    osc.close()
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, local, world):
+    import torch
+
+    from anerend_gb300 import _lib as L
+    from anerend_gb300 import ddgi, scenes
+
+    torch.cuda.set_device(local)
+    w = scenes.SINGLE_GRID
+    arrays = scenes.build_scene(w)
+    ctx = ddgi.Context(local)
+    scene = ddgi.Scene(ctx, arrays)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    # hit fraction of the workload's rays (for the algorithmic bytes), from one recorded trace
+    probe_grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis,
+                                options=L.DDGI_GRID_RECORD_HITS)
+    probe_grid.trace(scene, ddgi.FrameParams(rotation=scenes.rotation(w.seed, 0)), stream)
+    ctx.sync(stream)
+    _, hits, _ = probe_grid.download_rays(hits=True)
+    hit_frac = float((hits >= 0).mean())
+    probe_grid.close()
+
+    grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    rays_per_step = w.probes * w.rays
+
+    def frame(f):
+        return ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f))
+
+    f = 0
+    for _ in range(args.warmup):
+        grid.update(scene, frame(f), stream)
+        f += 1
+    torch.cuda.synchronize()
+
+    # ---- device-timed steps (per-phase events on the launching stream, L2 flushed between steps) ----
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    launches = 0
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.zero_()
+        fp = frame(f)
+        e = ev[s]
+        e[0].record()
+        moved = grid.translate(fp.camera_pos, stream)
+        e[1].record()
+        grid.trace(scene, fp, stream)
+        e[2].record()
+        grid.convolve(fp, stream)
+        e[3].record()
+        launches += 4 + (1 if moved else 0)  # lattice, trace, weights, convolve (+ translate)
+        f += 1
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    barrier(world)
+    clocks = sampler.stop()
+    ctx.sync(stream)
+    step_ms = [e[0].elapsed_time(e[3]) for e in ev]
+    trace_ms = [e[1].elapsed_time(e[2]) for e in ev]
+    conv_ms = [e[2].elapsed_time(e[3]) for e in ev]
+    total_ms = max_over_ranks(sum(step_ms), world)
+    ms_per_step = total_ms / args.steps
+    value = world * rays_per_step * args.steps / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI: host frame in, atlas out into pinned host memory ----
+    atlas_host = torch.empty(grid.buffers.atlasBytes // 4, dtype=torch.float32).pin_memory()
+    lib = L.load()
+    e2e_times = []
+    barrier(world)
+    for s in range(args.steps):
+        fp = frame(f).to_c()
+        t0 = time.perf_counter()
+        ctx.check(lib.ddgi_update(grid.handle, scene.handle, fp, stream))
+        ctx.check(lib.ddgi_atlas_download(grid.handle, atlas_host.data_ptr(), grid.buffers.atlasBytes, stream))
+        e2e_times.append(time.perf_counter() - t0)
+        f += 1
+    e2e_total = max_over_ranks(sum(e2e_times), world)
+    e2e_value = world * rays_per_step * args.steps / e2e_total
+
+    peaks = load_peaks()
+    trace_avg_s = sum(trace_ms) / len(trace_ms) / 1e3
+    alg_bytes = rays_per_step * (hit_frac * BYTES_PER_HIT + (1 - hit_frac) * BYTES_PER_MISS)
+    achieved = alg_bytes / trace_avg_s / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "trace_shade_traffic.json"
+    if tp.exists():
+        traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        frames = 4
+        v, dt, cores = cpu_sample(w, arrays, frames)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{frames} full probe updates ({frames * rays_per_step} rays), FP64 oracle, {dt:.1f} s"}
+    if rank == 0:
+        srt = sorted(step_ms)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "probes": w.probes, "grid": list(w.dims), "rays_per_probe": w.rays,
+                       "triangles": w.num_tris, "materials": 1024, "atlas": "RGBA32F", "hysteresis": w.hysteresis,
+                       "camera": "+1 x every 10 frames", "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{world}"},
+            "probe_updates_per_s": value / w.rays,
+            "p50_ms": srt[len(srt) // 2], "p99_ms": srt[min(len(srt) - 1, int(0.99 * len(srt)))],
+            "phase_ms": {"trace_shade": sum(trace_ms) / len(trace_ms), "convolve": sum(conv_ms) / len(conv_ms),
+                         "translate_and_lattice": sum(e[0].elapsed_time(e[1]) for e in ev) / len(ev)},
+            "hit_fraction": hit_frac,
+            "wall_s": wall,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 116,
+                    "d2h_bytes_per_step": int(grid.buffers.atlasBytes)},
+            "roofline": {"kernel": "k_trace_shade", "bound": "hbm", "achieved": achieved,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": traffic, "peak_source": peaks["source"],
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    grid.close()
+    scene.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, local, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        from anerend_gb300 import build
+
+        if rank == 0:
+            build.build()
+        barrier(world)
+        run_ours(args, rank, local, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -195,6 +195,7 @@ def convolve(desc, ray_rad: np.ndarray, dirs: np.ndarray, atlas: np.ndarray, lay
 
 def translate(desc, atlas: np.ndarray, dx: int, dz: int) -> np.ndarray:
     a = np.ascontiguousarray(atlas)
+    assert a.ndim == 3, "atlas must be (height, width, texel components or bytes)"
     out = np.empty_like(a)
-    load().oracle_translate(C.addressof(desc), _p(a), _p(out), dx, dz, a.itemsize * 4)
+    load().oracle_translate(C.addressof(desc), _p(a), _p(out), dx, dz, a.itemsize * a.shape[-1])
     return out
