@@ -105,7 +105,11 @@ SIGNATURES = {
     "ddgi_convolve_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                     C.c_uint32, C.c_void_p]),
     "ddgi_translate_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "ddgi_convolve_raw_noalloc": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                            C.c_int, C.c_uint32, C.c_void_p]),
 }
+
+DDGI_NOALLOC_MAX_RAYS = 512
 
 _lib = None
 

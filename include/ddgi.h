@@ -238,6 +238,18 @@ int  ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* 
 int  ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs, void* atlas,
                        int layerBegin, int layerEnd, uint32_t flags, void* stream);
 
+/* ddgi_convolve_raw for callers that cannot allocate device memory while they update probes (renderers
+ * that reserve all memory before the frame loop and forbid allocation inside a frame; processes whose
+ * device memory is committed to a budget). It has no counterpart in the reference. The weight scratch
+ * lives in a static device array of DDGI_NOALLOC_MAX_RAYS x 64 + 64 floats (132,352 bytes, held on every
+ * GPU that loads the library until exit); the call allocates nothing. Returns DDGI_EINVAL when
+ * desc->raysPerProbe exceeds DDGI_NOALLOC_MAX_RAYS. The first call on a device looks up the array's
+ * address: make it before any stream capture. All calls share the array; calls that overlap on the GPU
+ * race on it and must be ordered by the caller. */
+#define DDGI_NOALLOC_MAX_RAYS 512
+int  ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs,
+                               void* atlas, int layerBegin, int layerEnd, uint32_t flags, void* stream);
+
 /* The translation copy of IrradianceProbeTranslationPass.cpp:83-168 from atlasIn to atlasOut (distinct
  * buffers, desc->atlasFormat): atlasOut = atlasIn shifted by (sign(dx), sign(dz)) probes per layer plane. */
 int  ddgi_translate_raw(const DdgiGridDesc* desc, const void* atlasIn, void* atlasOut, int dx, int dz,
