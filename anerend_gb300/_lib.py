@@ -7,7 +7,9 @@ from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "libddgi.so"
+import os
+
+LIB_PATH = Path(os.environ.get("DDGI_LIB", Path(__file__).resolve().parent / "libddgi.so"))
 
 DDGI_OK = 0
 DDGI_EINVAL = -1
@@ -72,6 +74,11 @@ class Frame(C.Structure):
                 ("rotation", C.c_float * 9), ("layer", C.c_int32), ("bakeTileInfo", C.c_int32 * 3)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
+
+
 class GridBuffers(C.Structure):
     _fields_ = [("atlas", C.c_void_p), ("rayRadiance", C.c_void_p), ("rayDirection", C.c_void_p),
                 ("rayHit", C.c_void_p), ("lattice", C.c_void_p),
@@ -94,6 +101,8 @@ SIGNATURES = {
     "ddgi_grid_destroy": (None, [C.c_void_p]),
     "ddgi_grid_buffers": (C.c_int, [C.c_void_p, C.POINTER(GridBuffers)]),
     "ddgi_grid_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ddgi_grid_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "ddgi_grid_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ddgi_translate": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_void_p]),
     "ddgi_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Frame), C.c_void_p]),
     "ddgi_convolve": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p]),

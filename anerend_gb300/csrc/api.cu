@@ -7,6 +7,7 @@
 #include "kernels.h"
 #include "lbvh.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -36,6 +37,12 @@ struct DdgiScene {
   LbvhResult bvh;
   DdgiSceneInfo info{};
   SceneGPU view{};
+  std::vector<InstanceGPU> hostInst;  // host copy (composed into the shadow BVH's transforms)
+  uint64_t numIndices = 0, numVertices = 0;
+  LbvhResult shadowBvh;               // built for shadowLight, rebuilt when the light direction changes
+  float shadowLight[3] = {0, 0, 0};
+  bool shadowValid = false;
+  std::mutex mu;
 };
 
 struct DdgiGrid {
@@ -48,6 +55,8 @@ struct DdgiGrid {
   float4* rayDir = nullptr;
   int* rayHit = nullptr;
   float4* lattice = nullptr;
+  int* order = nullptr;   // trace-kernel direction order (N ints)
+  DdgiTuning tuning{};
   float* wt = nullptr;    // N x 64 convolution weights (transposed)
   float* wsum = nullptr;  // 64 weight sums
   int rayH = 0;
@@ -119,7 +128,52 @@ GridGPU makeGridGPU(const DdgiGridDesc& d) {
   g.atlasFmt = d.atlasFormat;
   g.rayW = g.bw * g.X;
   g.options = d.options;
+  g.warpProbes = 1;
   return g;
+}
+
+// Order of the N lattice directions along a Morton curve of their octahedral coordinates, so that
+// consecutive slots are neighbours on the sphere (rotations preserve neighbourhoods, so the order is
+// computed once from the unrotated lattice of worldDirFromFibonacciIndex, rgen:35-46).
+std::vector<int> mortonRayOrder(int n) {
+  std::vector<std::pair<uint64_t, int>> keys(n);
+  for (int i = 0; i < n; ++i) {
+    double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
+    double phi = std::acos(1.0 - 2.0 * ((double)i + 0.5) / (double)n);
+    double x = std::cos(theta) * std::sin(phi), y = std::sin(theta) * std::sin(phi), z = std::cos(phi);
+    double l1 = std::fabs(x) + std::fabs(y) + std::fabs(z);
+    double u = x / l1, v = y / l1;
+    if (z < 0) {
+      double nu = (1 - std::fabs(v)) * (u >= 0 ? 1 : -1), nv = (1 - std::fabs(u)) * (v >= 0 ? 1 : -1);
+      u = nu;
+      v = nv;
+    }
+    uint32_t qu = (uint32_t)std::min(65535.0, std::max(0.0, (u + 1) * 0.5 * 65536.0));
+    uint32_t qv = (uint32_t)std::min(65535.0, std::max(0.0, (v + 1) * 0.5 * 65536.0));
+    uint64_t key = 0;
+    for (int b = 0; b < 16; ++b) key |= (uint64_t)((qu >> b) & 1u) << (2 * b) | (uint64_t)((qv >> b) & 1u) << (2 * b + 1);
+    keys[i] = {key, i};
+  }
+  std::sort(keys.begin(), keys.end());
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = keys[i].second;
+  return order;
+}
+
+int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
+  DdgiContext* ctx = g->ctx;
+  int minWp = std::max(1, 32 / g->g.N);
+  if (t.warpProbes < minWp || t.warpProbes > 32 || (t.warpProbes & (t.warpProbes - 1)))
+    return fail(ctx, DDGI_EINVAL, "warpProbes %d must be a power of two in [%d, 32]", t.warpProbes, minWp);
+  if (t.rayOrder != 0 && t.rayOrder != 1) return fail(ctx, DDGI_EINVAL, "rayOrder %d unknown", t.rayOrder);
+  if (t.shadowMode != 0 && t.shadowMode != 1) return fail(ctx, DDGI_EINVAL, "shadowMode %d unknown", t.shadowMode);
+  std::vector<int> order(g->g.N);
+  if (t.rayOrder == 1) order = mortonRayOrder(g->g.N);
+  else for (int i = 0; i < g->g.N; ++i) order[i] = i;
+  CK(cudaMemcpy(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice), "ray order upload");
+  g->tuning = t;
+  g->g.warpProbes = t.warpProbes;
+  return DDGI_OK;
 }
 
 int frameToGPU(DdgiContext* ctx, const DdgiFrame* f, FrameGPU& out) {
@@ -162,6 +216,74 @@ bool invert3(const float* m12, float* out9) {
                    c02, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]};
   for (int i = 0; i < 9; ++i) out9[i] = (float)(inv[i] / det);
   return true;
+}
+
+// Woop shear of a direction: kz = dominant axis, (kx, ky) the others (swapped when d[kz] < 0),
+// S = (d[kx]/d[kz], d[ky]/d[kz], 1/d[kz]). shear(v) = (v[kx] - Sx v[kz], v[ky] - Sy v[kz], Sz v[kz]) maps d
+// to (0, 0, 1) and keeps distances along d.
+void shearOf(const double d[3], int k[3], double S[3]) {
+  double ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+  if (d[kz] < 0) std::swap(kx, ky);
+  k[0] = kx; k[1] = ky; k[2] = kz;
+  S[0] = d[kx] / d[kz];
+  S[1] = d[ky] / d[kz];
+  S[2] = 1.0 / d[kz];
+}
+
+// Builds (or reuses) the shadow BVH of `sc` for light direction lightDir: the instance transforms are
+// composed with the shear of L = normalize(-lightDir) on the host (FP64) and the LBVH is built over the
+// sheared triangles. Synchronizes `st` when it builds.
+int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
+  DdgiContext* ctx = sc->ctx;
+  std::lock_guard<std::mutex> lk(sc->mu);
+  if (sc->shadowValid && sc->shadowLight[0] == lightDir[0] && sc->shadowLight[1] == lightDir[1] &&
+      sc->shadowLight[2] == lightDir[2])
+    return DDGI_OK;
+  if (sc->view.numTris == 0) return DDGI_OK;
+  double n = std::sqrt((double)lightDir[0] * lightDir[0] + (double)lightDir[1] * lightDir[1] +
+                       (double)lightDir[2] * lightDir[2]);
+  if (!(n > 0)) return fail(ctx, DDGI_EINVAL, "lightDir has zero length");
+  double L[3] = {-lightDir[0] / n, -lightDir[1] / n, -lightDir[2] / n};
+  int k[3];
+  double S[3];
+  shearOf(L, k, S);
+  double Sm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  Sm[0][k[0]] = 1.0; Sm[0][k[2]] = -S[0];
+  Sm[1][k[1]] = 1.0; Sm[1][k[2]] = -S[1];
+  Sm[2][k[2]] = S[2];
+  std::vector<InstanceGPU> sh = sc->hostInst;
+  for (InstanceGPU& in : sh) {
+    double m[12];
+    for (int i = 0; i < 12; ++i) m[i] = in.o2w[i];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 4; ++c) {
+        double v = 0;
+        for (int q = 0; q < 3; ++q) v += Sm[r][q] * m[4 * q + c];
+        in.o2w[4 * r + c] = (float)v;
+      }
+  }
+  InstanceGPU* dInst = nullptr;
+  CK(cudaMalloc(&dInst, sizeof(InstanceGPU) * sh.size()), "shadow instances");
+  cudaError_t e = cudaMemcpyAsync(dInst, sh.data(), sizeof(InstanceGPU) * sh.size(), cudaMemcpyHostToDevice, st);
+  LbvhResult r;
+  if (e == cudaSuccess)
+    e = lbvhBuild(dInst, (int)sh.size(), sc->meshes, sc->indices, sc->numIndices, sc->vertices, sc->numVertices,
+                  sc->view.numTris, ctx->dErr, st, &r);
+  cudaFree(dInst);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "shadow BVH build");
+  lbvhFree(&sc->shadowBvh);
+  sc->shadowBvh = r;
+  for (int i = 0; i < 3; ++i) {
+    sc->shadowLight[i] = lightDir[i];
+    sc->view.shearK[i] = k[i];
+    sc->view.shearS[i] = (float)S[i];
+  }
+  sc->view.shadowNodes = r.nodes;
+  sc->view.shadowTris = r.tris;
+  sc->shadowValid = true;
+  return DDGI_OK;
 }
 
 }  // namespace
@@ -296,6 +418,9 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
     sc->info.boundsMin[k] = sc->bvh.centroidLo[k];
     sc->info.boundsMax[k] = sc->bvh.centroidHi[k];
   }
+  sc->hostInst = inst;
+  sc->numIndices = d->numIndices;
+  sc->numVertices = d->numVertices;
   *out = sc;
   return DDGI_OK;
 }
@@ -308,6 +433,7 @@ void ddgi_scene_destroy(DdgiScene* s) {
   cudaFree(s->instances);
   cudaFree(s->materials);
   lbvhFree(&s->bvh);
+  lbvhFree(&s->shadowBvh);
   delete s;
 }
 
@@ -340,6 +466,7 @@ int ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out)
   if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = cudaMalloc(&g->rayDir, 16 * rayTexels);
   if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = cudaMalloc(&g->rayHit, 4 * rayTexels);
   if (e == cudaSuccess) e = cudaMalloc(&g->lattice, 16 * (size_t)g->g.N);
+  if (e == cudaSuccess) e = cudaMalloc(&g->order, sizeof(int) * (size_t)g->g.N);
   if (e == cudaSuccess) e = cudaMalloc(&g->wt, 4 * (size_t)g->g.N * kOctTexels);
   if (e == cudaSuccess) e = cudaMalloc(&g->wsum, 4 * kOctTexels);
   if (e == cudaSuccess) e = cudaMemset(g->rayRad, 0, 16 * rayTexels);
@@ -348,6 +475,15 @@ int ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out)
   if (e != cudaSuccess) {
     ddgi_grid_destroy(g);
     return cudaFail(ctx, e, "grid allocation");
+  }
+  DdgiTuning t{};
+  t.warpProbes = std::max(1, 32 / g->g.N);
+  t.rayOrder = 1;
+  t.shadowMode = 1;
+  int rc2 = applyTuning(g, t);
+  if (rc2 != DDGI_OK) {
+    ddgi_grid_destroy(g);
+    return rc2;
   }
   *out = g;
   return DDGI_OK;
@@ -361,6 +497,7 @@ void ddgi_grid_destroy(DdgiGrid* g) {
   cudaFree(g->rayDir);
   cudaFree(g->rayHit);
   cudaFree(g->lattice);
+  cudaFree(g->order);
   cudaFree(g->wt);
   cudaFree(g->wsum);
   delete g;
@@ -381,6 +518,17 @@ int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
   o->rayBlockH = g->g.bh;
   o->atlasBytes = g->atlasBytes;
   return DDGI_OK;
+}
+
+int ddgi_grid_get_tuning(const DdgiGrid* g, DdgiTuning* out) {
+  if (!g || !out) return DDGI_EINVAL;
+  *out = g->tuning;
+  return DDGI_OK;
+}
+
+int ddgi_grid_set_tuning(DdgiGrid* g, const DdgiTuning* t) {
+  if (!g || !t) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_grid_set_tuning");
+  return applyTuning(g, *t);
 }
 
 int ddgi_grid_reset(DdgiGrid* g, void* stream) {
@@ -423,8 +571,17 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   f.layerBegin = b;
   f.layerEnd = e;
   cudaStream_t st = (cudaStream_t)stream;
+  SceneGPU view = scene->view;
+  if (g->tuning.shadowMode == 1) {
+    rc = ensureShadowBvh(const_cast<DdgiScene*>(scene), frame->lightDir, st);
+    if (rc) return rc;
+    view = scene->view;
+  } else {
+    view.shadowNodes = nullptr;
+    view.shadowTris = nullptr;
+  }
   CK(launchLattice(g->g.N, frame->rotation, g->lattice, st), "lattice");
-  CK(launchTraceShade(scene->view, g->g, f, g->lattice, g->atlas[g->cur], g->rayRad, g->rayDir, g->rayHit,
+  CK(launchTraceShade(view, g->g, f, g->lattice, g->order, g->atlas[g->cur], g->rayRad, g->rayDir, g->rayHit,
                       ctx->dErr, st),
      "trace");
   g->tracedBegin = b;

@@ -204,6 +204,13 @@ struct SceneGPU {
   const DdgiMeshInfo* meshes;
   const InstanceGPU* instances;
   const DdgiMaterialInfo* materials;
+  // Shadow BVH in the sheared ray space of the light direction (Woop et al.'s per-ray shear, fixed for
+  // every shadow ray of a frame): a shadow ray from p is the line through shear(p) along +z, so the same
+  // watertight test and traversal run on it with direction (0, 0, 1). Null when not built.
+  const float4* shadowNodes;
+  const float4* shadowTris;
+  int shearK[3];      // kx, ky, kz
+  float shearS[3];    // Sx, Sy, Sz
 };
 
 struct GridGPU {
@@ -213,6 +220,7 @@ struct GridGPU {
   int atlasW, atlasH, atlasFmt;
   int rayW;
   uint32_t options;
+  int warpProbes;  // probes per warp (power of two, 32 / warpProbes <= N)
 };
 
 struct FrameGPU {

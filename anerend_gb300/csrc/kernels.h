@@ -12,8 +12,8 @@ struct Mat3 {
 
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);
 cudaError_t launchTraceShade(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* lattice,
-                             const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit, uint32_t* err,
-                             cudaStream_t stream);
+                             const int* order, const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit,
+                             uint32_t* err, cudaStream_t stream);
 
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream);

@@ -273,23 +273,30 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 }
 
 // ---------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTraceThreads) k_trace_shade(SceneGPU s, GridGPU g, FrameGPU f,
-                                                               const float4* __restrict__ lattice,
-                                                               const void* __restrict__ atlasPrev,
-                                                               float4* __restrict__ rayRad,
-                                                               float4* __restrict__ rayDir,
-                                                               int* __restrict__ rayHit,
-                                                               uint32_t* __restrict__ err) {
-  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int lane = (int)(tid & 31);
-  long long rest = tid >> 5;
-  int j = (int)(rest % g.N);
-  long long tileLin = rest / g.N;
-  int tilesPerLayer = (g.X * g.Z + 31) / 32;
-  int layer = f.layerBegin + (int)(tileLin / tilesPerLayer);
+// Warp shape: a warp traces D = 32 / warpProbes directions for each of warpProbes consecutive probes of a
+// layer; consecutive direction slots k map to lattice rays j = order[k]. With the octahedral Morton order
+// the D directions of a warp are neighbours on the sphere, so the warp's rays share traversal paths near
+// their common origin.
+#ifndef DDGI_TRACE_MIN_BLOCKS
+#define DDGI_TRACE_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+    k_trace_shade(SceneGPU s, GridGPU g, FrameGPU f, const float4* __restrict__ lattice,
+                  const int* __restrict__ order, const void* __restrict__ atlasPrev, float4* __restrict__ rayRad,
+                  float4* __restrict__ rayDir, int* __restrict__ rayHit, uint32_t* __restrict__ err) {
+  long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  const int D = 32 / g.warpProbes;                // directions per warp
+  const int dirChunks = g.N / D;
+  const int probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
+  int dc = (int)(warp % dirChunks);
+  long long rest = warp / dirChunks;
+  int pg = (int)(rest % probeGroups);
+  int layer = f.layerBegin + (int)(rest / probeGroups);
   if (layer >= f.layerEnd) return;
-  int p = (int)(tileLin % tilesPerLayer) * 32 + lane;
+  int p = pg * g.warpProbes + lane / D;
   if (p >= g.X * g.Z) return;
+  int j = __ldg(&order[dc * D + lane % D]);
   int px = p % g.X, pz = p / g.X;
 
   // ray generation (rgen:51-88)
@@ -327,10 +334,21 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_shade(SceneGPU s, GridG
                     m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
 
     // shadow ray toward the sun (rchit:155-176), any hit in [0.1, 50]
-    float3 shadowDir = normalize3(-f.lightDir);
-    WRay sray = makeRay(pos, shadowDir);
+    bool shadowed;
     HitInfo shit;
-    bool shadowed = traverse<true>(s, sray, kTMin, kTMax, shit, err);
+    if (s.shadowNodes) {
+      // the light's sheared space: the ray is the +z line through shear(pos)
+      float pk[3] = {pos.x, pos.y, pos.z};
+      float pz = pk[s.shearK[2]];
+      float3 o = f3(pk[s.shearK[0]] - s.shearS[0] * pz, pk[s.shearK[1]] - s.shearS[1] * pz, s.shearS[2] * pz);
+      SceneGPU ls = s;
+      ls.nodes = s.shadowNodes;
+      ls.tris = s.shadowTris;
+      shadowed = traverse<true>(ls, makeRay(o, f3(0.f, 0.f, 1.f)), kTMin, kTMax, shit, err);
+    } else {
+      float3 shadowDir = normalize3(-f.lightDir);
+      shadowed = traverse<true>(s, makeRay(pos, shadowDir), kTMin, kTMax, shit, err);
+    }
 
     // surface (rchit:179-187, getSurfaceDataFromMat bindless.glsl:181-237 without textures)
     const DdgiMaterialInfo& mat = s.materials[in.material];
@@ -375,14 +393,15 @@ cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t s
 }
 
 cudaError_t launchTraceShade(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* lattice,
-                             const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit, uint32_t* err,
-                             cudaStream_t stream) {
+                             const int* order, const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit,
+                             uint32_t* err, cudaStream_t stream) {
   int layers = f.layerEnd - f.layerBegin;
   if (layers <= 0) return cudaSuccess;
-  long long tilesPerLayer = (g.X * g.Z + 31) / 32;
-  long long threads = tilesPerLayer * layers * g.N * 32;
-  long long nblocks = (threads + kTraceThreads - 1) / kTraceThreads;
-  k_trace_shade<<<(unsigned)nblocks, kTraceThreads, 0, stream>>>(s, g, f, lattice, atlasPrev, rayRad, rayDir,
+  const int D = 32 / g.warpProbes;
+  long long probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
+  long long warps = probeGroups * layers * (g.N / D);
+  long long nblocks = (warps * 32 + kTraceThreads - 1) / kTraceThreads;
+  k_trace_shade<<<(unsigned)nblocks, kTraceThreads, 0, stream>>>(s, g, f, lattice, order, atlasPrev, rayRad, rayDir,
                                                                  rayHit, err);
   return cudaGetLastError();
 }

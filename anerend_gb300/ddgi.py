@@ -129,6 +129,23 @@ class ProbeGrid:
         self.ctx.check(self.ctx.lib.ddgi_grid_buffers(self.handle, C.byref(b)))
         return b
 
+    @property
+    def tuning(self) -> L.Tuning:
+        t = L.Tuning()
+        self.ctx.check(self.ctx.lib.ddgi_grid_get_tuning(self.handle, C.byref(t)))
+        return t
+
+    def set_tuning(self, warp_probes: int | None = None, ray_order: int | None = None,
+                   shadow_mode: int | None = None) -> None:
+        t = self.tuning
+        if warp_probes is not None:
+            t.warpProbes = warp_probes
+        if ray_order is not None:
+            t.rayOrder = ray_order
+        if shadow_mode is not None:
+            t.shadowMode = shadow_mode
+        self.ctx.check(self.ctx.lib.ddgi_grid_set_tuning(self.handle, C.byref(t)))
+
     def reset(self, stream: int = 0) -> None:
         self.ctx.check(self.ctx.lib.ddgi_grid_reset(self.handle, stream))
 

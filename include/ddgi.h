@@ -147,6 +147,16 @@ typedef struct DdgiFrame {
   int32_t  bakeTileInfo[3]; /* x, y: tile index, z: tile size (bake mode only) */
 } DdgiFrame;
 
+/* Launch shape of a grid's trace kernel, picked by the autotuner; the defaults are valid for every grid.
+ * No counterpart in the reference (its launch shape is fixed by vkCmdTraceRaysKHR). */
+typedef struct DdgiTuning {
+  int32_t warpProbes;   /* probes sharing one warp: a power of two in [max(1, 32/N), 32]; default 1 */
+  int32_t rayOrder;     /* 0: lattice order; 1: octahedral Morton order of the directions (default) */
+  int32_t shadowMode;   /* 0: shadow rays traverse the scene BVH; 1: a BVH built in the sheared ray space of
+                           the light direction, rebuilt when the direction changes (default) */
+  int32_t reserved[5];
+} DdgiTuning;
+
 /* Device views of the grid's buffers (owned by the grid). */
 typedef struct DdgiGridBuffers {
   void*    atlas;           /* current atlas, atlasFormat texels, atlasWidth x atlasHeight */
@@ -196,6 +206,9 @@ void ddgi_grid_destroy(DdgiGrid* grid);
 int  ddgi_grid_buffers(const DdgiGrid* grid, DdgiGridBuffers* out);
 /* Clears the atlas to (0,0,0,1) and the translation state to (0,0). */
 int  ddgi_grid_reset(DdgiGrid* grid, void* stream);
+/* Reads / sets the grid's launch shape (results do not depend on it). */
+int  ddgi_grid_get_tuning(const DdgiGrid* grid, DdgiTuning* out);
+int  ddgi_grid_set_tuning(DdgiGrid* grid, const DdgiTuning* tuning);
 
 /* IrradianceProbeTranslationPass exe (IrradianceProbeTranslationPass.cpp:56-186): camera probe index by
  * int() truncation of cameraPos.xz/step; if it changed, shift every layer plane of the atlas by

@@ -114,11 +114,13 @@ def test_convolve_fp32(ctx, n, bake):
 
 # ---- full update: trace + shade + convolve against the oracle ---------------------------------------
 
-def _run_lockstep(ctx, w, frames, options=0, layer=-1, fmt=L.DDGI_FORMAT_RGBA32F, check_rays=True):
+def _run_lockstep(ctx, w, frames, options=0, layer=-1, fmt=L.DDGI_FORMAT_RGBA32F, check_rays=True, tuning=None):
     arrays = scenes.build_scene(w)
     scene = ddgi.Scene(ctx, arrays)
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, atlas_format=fmt,
                           options=options | L.DDGI_GRID_RECORD_HITS)
+    if tuning:
+        grid.set_tuning(**tuning)
     osc = oracle.OracleScene(arrays, L.SceneDesc)
     og = oracle.OracleGrid(grid.desc)
     stats = []
@@ -150,9 +152,14 @@ def g_rows(og):
     return og.geom.ray_hw[0] // og.geom.Y
 
 
-def test_cpu_reference_workload_8_frames(ctx):
+@pytest.mark.parametrize("tuning", [
+    dict(shadow_mode=1, ray_order=1, warp_probes=2),   # light-space shadow BVH, Morton direction order
+    dict(shadow_mode=0, ray_order=0, warp_probes=32),  # scene-BVH shadow rays, 32 parallel rays per warp
+    dict(shadow_mode=1, ray_order=0, warp_probes=1),
+])
+def test_cpu_reference_workload_8_frames(ctx, tuning):
     w = scenes.CPU_REFERENCE
-    atlas, want, stats = _run_lockstep(ctx, w, w.frames)
+    atlas, want, stats = _run_lockstep(ctx, w, w.frames, tuning=tuning)
     for s in stats:
         assert s["hit_mismatch"] == 0, s
         assert s["certain"] > 0.99, s
