@@ -31,6 +31,9 @@ DDGI_GRID_EDGE_CLAMP = 1 << 0
 DDGI_GRID_WRITE_DIRS = 1 << 1
 DDGI_GRID_RECORD_HITS = 1 << 2
 
+DDGI_ELEM_F16 = 0
+DDGI_ELEM_BF16 = 1
+
 ERROR_NAMES = {
     DDGI_EINVAL: "DDGI_EINVAL", DDGI_ENOMEM: "DDGI_ENOMEM", DDGI_ETIMEDOUT: "DDGI_ETIMEDOUT",
     DDGI_EDEVICE: "DDGI_EDEVICE", DDGI_EUNSUPPORTED: "DDGI_EUNSUPPORTED", DDGI_EOVERFLOW: "DDGI_EOVERFLOW",
@@ -76,7 +79,7 @@ class Frame(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("convMode", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class GridBuffers(C.Structure):
@@ -114,6 +117,9 @@ SIGNATURES = {
     "ddgi_convolve_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                     C.c_uint32, C.c_void_p]),
     "ddgi_translate_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "ddgi_convolve_tc_raw": (C.c_int, [C.c_void_p, C.POINTER(GridDesc), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_int, C.c_uint32, C.c_void_p]),
+    "ddgi_pack_rays16": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "ddgi_convolve_raw_noalloc": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                             C.c_int, C.c_uint32, C.c_void_p]),
 }

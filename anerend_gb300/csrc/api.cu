@@ -57,6 +57,8 @@ struct DdgiGrid {
   float4* lattice = nullptr;
   int* order = nullptr;   // trace-kernel direction order (N ints)
   DdgiTuning tuning{};
+  void* rad16 = nullptr;  // planar 16-bit radiance for the tensor-core convolution (3 x P x N)
+  void* tcScratch = nullptr;
   float* wt = nullptr;    // N x 64 convolution weights (transposed)
   float* wsum = nullptr;  // 64 weight sums
   int rayH = 0;
@@ -167,6 +169,14 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
     return fail(ctx, DDGI_EINVAL, "warpProbes %d must be a power of two in [%d, 32]", t.warpProbes, minWp);
   if (t.rayOrder != 0 && t.rayOrder != 1) return fail(ctx, DDGI_EINVAL, "rayOrder %d unknown", t.rayOrder);
   if (t.shadowMode != 0 && t.shadowMode != 1) return fail(ctx, DDGI_EINVAL, "shadowMode %d unknown", t.shadowMode);
+  if (t.convMode < 0 || t.convMode > 2) return fail(ctx, DDGI_EINVAL, "convMode %d unknown", t.convMode);
+  if (t.convMode != 0 && g->g.N % 64)
+    return fail(ctx, DDGI_EINVAL, "tensor-core convolution needs raysPerProbe %% 64 == 0 (N = %d)", g->g.N);
+  if (t.convMode != 0 && !g->rad16) {
+    size_t bytes = (size_t)3 * g->g.X * g->g.Y * g->g.Z * g->g.N * 2;
+    CK(cudaMalloc(&g->rad16, bytes), "16-bit radiance buffer");
+    CK(cudaMalloc(&g->tcScratch, tcScratchBytes(g->g.N)), "tensor-core weight scratch");
+  }
   std::vector<int> order(g->g.N);
   if (t.rayOrder == 1) order = mortonRayOrder(g->g.N);
   else for (int i = 0; i < g->g.N; ++i) order[i] = i;
@@ -498,6 +508,8 @@ void ddgi_grid_destroy(DdgiGrid* g) {
   cudaFree(g->rayHit);
   cudaFree(g->lattice);
   cudaFree(g->order);
+  cudaFree(g->rad16);
+  cudaFree(g->tcScratch);
   cudaFree(g->wt);
   cudaFree(g->wsum);
   delete g;
@@ -603,6 +615,15 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
     if (rc) return rc;
   }
   cudaStream_t st = (cudaStream_t)stream;
+  if (g->tuning.convMode != 0) {
+    int fmt = g->tuning.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
+    int pTotal = g->g.X * g->g.Y * g->g.Z;
+    CK(launchPackRays16(g->g, fmt, g->rayRad, g->rad16, b, e, pTotal, st), "pack rays");
+    CK(launchConvTc(g->g, fmt, g->rad16, pTotal, g->lattice, g->tcScratch, g->atlas[g->cur], b, e, g->desc.hysteresis,
+                    frame->flags, ctx->dErr, st),
+       "tensor-core convolve");
+    return DDGI_OK;
+  }
   CK(launchConvWeights(g->g.N, g->lattice, g->wt, g->wsum, st), "conv weights");
   CK(launchConvFp32(g->g, g->rayRad, g->wt, g->wsum, g->atlas[g->cur], b, e, g->desc.hysteresis, frame->flags, st),
      "convolve");
@@ -678,6 +699,37 @@ int ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const 
     e = launchConvFp32(g, (const float4*)rayRadiance, wt, ws, atlas, layerBegin, layerEnd, desc->hysteresis, flags, st);
   cudaFreeAsync(wt, st);
   return e == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
+}
+
+int ddgi_convolve_tc_raw(DdgiContext* ctx, const DdgiGridDesc* desc, const void* radiance16, int elemFormat,
+                         const float* dirs, void* atlas, int layerBegin, int layerEnd, uint32_t flags, void* stream) {
+  if (!ctx) return DDGI_EINVAL;
+  int rc = validateGridDesc(ctx, desc);
+  if (rc) return rc;
+  if (!radiance16 || !dirs || !atlas) return fail(ctx, DDGI_EINVAL, "NULL buffer to ddgi_convolve_tc_raw");
+  if (elemFormat != DDGI_ELEM_F16 && elemFormat != DDGI_ELEM_BF16) return fail(ctx, DDGI_EINVAL, "elemFormat unknown");
+  if (desc->raysPerProbe % 64) return fail(ctx, DDGI_EINVAL, "raysPerProbe must be a multiple of 64");
+  if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return fail(ctx, DDGI_EINVAL, "layer range");
+  if (((uintptr_t)radiance16) & 15) return fail(ctx, DDGI_EINVAL, "radiance16 must be 16-byte aligned");
+  GridGPU g = makeGridGPU(*desc);
+  cudaStream_t st = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  CK(cudaMallocAsync(&scratch, tcScratchBytes(g.N), st), "tensor-core weight scratch");
+  cudaError_t e = launchConvTc(g, elemFormat, radiance16, g.X * g.Y * g.Z, (const float4*)dirs, scratch, atlas,
+                               layerBegin, layerEnd, desc->hysteresis, flags, ctx->dErr, st);
+  cudaFreeAsync(scratch, st);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "tensor-core convolve");
+  return DDGI_OK;
+}
+
+int ddgi_pack_rays16(const DdgiGridDesc* desc, const float* rayRadiance, void* radiance16, int elemFormat,
+                     int layerBegin, int layerEnd, void* stream) {
+  if (validateGridDesc(nullptr, desc) != DDGI_OK || !rayRadiance || !radiance16) return DDGI_EINVAL;
+  if (elemFormat != DDGI_ELEM_F16 && elemFormat != DDGI_ELEM_BF16) return DDGI_EINVAL;
+  if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return DDGI_EINVAL;
+  GridGPU g = makeGridGPU(*desc);
+  return launchPackRays16(g, elemFormat, (const float4*)rayRadiance, radiance16, layerBegin, layerEnd,
+                          g.X * g.Y * g.Z, (cudaStream_t)stream) == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
 }
 
 int ddgi_translate_raw(const DdgiGridDesc* desc, const void* atlasIn, void* atlasOut, int dx, int dz, void* stream) {

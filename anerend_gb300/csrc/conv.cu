@@ -15,18 +15,26 @@ namespace {
 constexpr int kConvProbes = 4;                       // probes per group
 constexpr int kConvThreads = kConvProbes * kOctTexels;  // 256
 
-__global__ void k_conv_weights(int n, const float4* __restrict__ dirs, float* __restrict__ wt,
-                               float* __restrict__ wsum) {
-  int t = threadIdx.x;  // 64 threads: one texel each
+__global__ void __launch_bounds__(256) k_conv_weights(int n, const float4* __restrict__ dirs, float* __restrict__ wt,
+                                                      float* __restrict__ wsum) {
+  // one block per texel, threads over the rays, the weight sum through a shared-memory tree
+  __shared__ float part[256];
+  int t = blockIdx.x;
   float3 omega = texelDirection(t % kOct, t / kOct);
   float s = 0.0f;
-  for (int j = 0; j < n; ++j) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
     float w = fmaxf(0.0f, dot3(xyz(dirs[j]), omega));
     if (!(w > 1e-6f)) w = 0.0f;
     wt[j * kOctTexels + t] = w;
     s += w;
   }
-  wsum[t] = s;
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wsum[t] = part[0];
 }
 
 // kSmemW: the N x 64 weight table is staged in shared memory (N <= 512); otherwise it is read from global
@@ -112,7 +120,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_fp32(GridGPU g, const flo
 }  // namespace
 
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream) {
-  k_conv_weights<<<1, kOctTexels, 0, stream>>>(n, dirs, wt, wsum);
+  k_conv_weights<<<kOctTexels, 256, 0, stream>>>(n, dirs, wt, wsum);
   return cudaGetLastError();
 }
 

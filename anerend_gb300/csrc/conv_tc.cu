@@ -1,0 +1,463 @@
+// Probe convolution on the tcgen05 tensor cores (probe_conv.comp:21-90 as a GEMM).
+//
+// All probes of a dispatch share the N ray directions, so the convolution of channel c is the product
+//   D_c[probe][texel] = sum_j R_c[probe][j] * W[texel][j],   W[t][j] = max(0, d_j . omega_t) (0 if <= 1e-6)
+// with R_c the 16-bit (FP16 or BF16) radiance of channel c, stored planar: row c * P + p, N rays per row.
+// One CTA per SM walks tiles of 128 probes. Per tile and 64-ray K-chunk a TMA producer warp loads the three
+// 128 x 64 radiance tiles and the 64 x 64 weight tile (SWIZZLE_128B); one thread of the MMA warp issues
+// 4 K-steps x 3 channels of tcgen05.mma (M = 128 probes, N = 64 texels, K = 16) into FP32 accumulators in
+// TMEM (3 x 64 columns, double-buffered = 384 of 512 columns). Four epilogue warps read the accumulators with
+// tcgen05.ld (thread = probe), normalise by the texel's weight sum and apply the hysteresis blend (or the
+// bake accumulation) in FP32 against the old atlas texel.
+//
+// Every mbarrier wait is bounded: on timeout the kernel raises DDGI_DEVERR_TIMEOUT, stops issuing work,
+// waits (bounded) for its own TMA loads and MMAs in flight, frees its TMEM and returns.
+#include "ddgi_common.cuh"
+#include "kernels.h"
+
+#include <cuda_bf16.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+namespace ddgi {
+
+namespace {
+
+constexpr int kTileP = 128;                  // probes per tile (MMA M)
+constexpr int kChunkK = 64;                  // rays per K-chunk (128 bytes of 16-bit values)
+constexpr int kStages = 4;  // 4 x 56 KB = 224 KB of operand staging
+constexpr int kATileBytes = kTileP * kChunkK * 2;   // 16 KB per channel
+constexpr int kWTileBytes = kOctTexels * kChunkK * 2;  // 8 KB
+constexpr int kStageBytes = 3 * kATileBytes + kWTileBytes;  // 56 KB
+constexpr int kTmemCols = 512;
+constexpr int kThreadsTc = 192;              // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+DDGI_D uint32_t smemU32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+DDGI_D void mbarInit(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemU32(bar)), "r"(count) : "memory");
+}
+DDGI_D void mbarExpectTx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemU32(bar)), "r"(bytes) : "memory");
+}
+DDGI_D void mbarArrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemU32(bar)) : "memory");
+}
+DDGI_D bool mbarTryWait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smemU32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false after kSpinLimit attempts.
+DDGI_D bool mbarWait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (mbarTryWait(bar, parity)) return true;
+    if (i > 32) __nanosleep(64);
+  }
+  return false;
+}
+
+DDGI_D void tmaLoad2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smemU32(dst)),
+      "l"((uint64_t)map), "r"(smemU32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+DDGI_D void tmemAlloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemU32(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+DDGI_D void tmemDealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+DDGI_D void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+DDGI_D void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+DDGI_D void mmaF16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          dTmem),
+      "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+DDGI_D void mmaCommit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemU32(bar))
+               : "memory");
+}
+
+// 32 lanes x 16 consecutive 32-bit columns: thread t gets lane (base lane + t), columns col .. col + 15.
+DDGI_D void tmemLoad16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor of a K-major, SWIZZLE_128B operand tile whose rows are 128 bytes and
+// whose 8-row swizzle atoms are 1024 bytes apart (start address 1024-byte aligned, advanced by 32 bytes per
+// K step of 16 elements inside the atom).
+DDGI_D uint64_t smemDesc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
+  d |= (uint64_t)(16 >> 4) << 16;                // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)2 << 61;                        // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulate, A and B both FP16 (fmt 0) or BF16 (fmt 1),
+// both K-major, M = 128, N = 64.
+__host__ __device__ constexpr uint32_t instrDesc(uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+struct TcParams {
+  GridGPU g;
+  const float* wsum16;  // 64 sums of the rounded weights (normalisation)
+  const float* wsum32;  // 64 sums of the FP32 weights (the .w channel)
+  void* atlas;
+  int pBegin, pEnd;     // probe range (linear over the whole grid)
+  int pTotal;           // rows per channel in the radiance matrix
+  int numChunks;        // N / 64
+  float hysteresis;
+  uint32_t flags;
+  uint32_t* err;
+};
+
+template <int kFmt>
+__global__ void __launch_bounds__(kThreadsTc, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap tmR, const __grid_constant__ CUtensorMap tmW, TcParams p) {
+  extern __shared__ uint8_t smemRaw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smemRaw + 1023) & ~(uintptr_t)1023);
+  __shared__ uint64_t fullBar[kStages], emptyBar[kStages], accFull[2], accEmpty[2], drainBar;
+  __shared__ uint32_t tmemSlot;
+  __shared__ int abortFlag;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles = (p.pEnd - p.pBegin + kTileP - 1) / kTileP;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) { mbarInit(&fullBar[s], 1); mbarInit(&emptyBar[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbarInit(&accFull[b], 1); mbarInit(&accEmpty[b], 128); }
+    mbarInit(&drainBar, 1);
+    abortFlag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmemAlloc(&tmemSlot, kTmemCols);
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = tmemSlot;
+
+  auto fail = [&]() {
+    atomicOr(p.err, DDGI_DEVERR_TIMEOUT);
+    atomicExch(&abortFlag, 1);
+  };
+  auto aborted = [&]() { return *(volatile int*)&abortFlag != 0; };
+
+  if (warp == 0) {
+    // ---- TMA producer ----
+    if (lane == 0) {
+      bool pending[kStages] = {};
+      uint32_t pendingParity[kStages] = {};
+      int s = 0;
+      uint32_t phase = 0;
+      for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x) {
+        int p0 = p.pBegin + t * kTileP;
+        for (int kc = 0; kc < p.numChunks; ++kc) {
+          if (!mbarWait(&emptyBar[s], phase ^ 1)) { fail(); break; }
+          pending[s] = false;
+          uint8_t* st = smem + (size_t)s * kStageBytes;
+          mbarExpectTx(&fullBar[s], kStageBytes);
+          for (int c = 0; c < 3; ++c) tmaLoad2d(st + c * kATileBytes, &tmR, &fullBar[s], kc * kChunkK, c * p.pTotal + p0);
+          tmaLoad2d(st + 3 * kATileBytes, &tmW, &fullBar[s], kc * kChunkK, 0);
+          pending[s] = true;
+          pendingParity[s] = phase;
+          if (++s == kStages) { s = 0; phase ^= 1; }
+        }
+      }
+      if (aborted()) {  // let loads in flight land before the CTA exits
+        for (int k = 0; k < kStages; ++k)
+          if (pending[k]) mbarWait(&fullBar[k], pendingParity[k]);
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      const uint32_t idesc = instrDesc(kFmt);
+      int s = 0;
+      uint32_t phase = 0;
+      int local = 0;
+      bool issued = false;
+      for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
+        int b = local & 1;
+        uint32_t accPhase = (local >> 1) & 1;
+        if (!mbarWait(&accEmpty[b], accPhase ^ 1)) { fail(); break; }
+        tcFenceAfter();
+        const uint32_t dBase = tmem + (uint32_t)(b * 3 * kOctTexels);
+        bool ok = true;
+        for (int kc = 0; kc < p.numChunks; ++kc) {
+          if (!mbarWait(&fullBar[s], phase)) { fail(); ok = false; break; }
+          tcFenceAfter();
+          uint32_t st = smemU32(smem + (size_t)s * kStageBytes);
+#pragma unroll
+          for (int kk = 0; kk < kChunkK / 16; ++kk) {
+            uint64_t bDesc = smemDesc(st + 3 * kATileBytes + kk * 32);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              uint64_t aDesc = smemDesc(st + c * kATileBytes + kk * 32);
+              mmaF16(dBase + c * kOctTexels, aDesc, bDesc, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+            }
+          }
+          issued = true;
+          mmaCommit(&emptyBar[s]);  // stage free once these MMAs have read it
+          if (++s == kStages) { s = 0; phase ^= 1; }
+        }
+        if (!ok) break;
+        mmaCommit(&accFull[b]);
+      }
+      if (issued) {  // drain: every MMA issued by this thread has completed
+        mmaCommit(&drainBar);
+        mbarWait(&drainBar, 0);
+      }
+    }
+  } else {
+    // ---- epilogue: warps 2..5, thread = probe row of the tile ----
+    const int quarter = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = quarter * 32 + lane;
+    const bool bake = (p.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
+    const float h = p.hysteresis, a = 1.0f - h;
+    int local = 0;
+    for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
+      int b = local & 1;
+      uint32_t accPhase = (local >> 1) & 1;
+      if (!mbarWait(&accFull[b], accPhase)) { fail(); break; }
+      tcFenceAfter();
+      const int probe = p.pBegin + t * kTileP + row;
+      const bool live = probe < p.pEnd;
+      int px = 0, pzAll = 0;
+      if (live) {
+        px = probe % p.g.X;
+        pzAll = probe / p.g.X;  // layer * Z + z
+      }
+      const uint32_t laneAddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 3 * kOctTexels);
+#pragma unroll 1
+      for (int blk = 0; blk < kOctTexels / 16; ++blk) {
+        float cr[16], cg[16], cb[16];
+        tmemLoad16(laneAddr + 0 * kOctTexels + blk * 16, cr);
+        tmemLoad16(laneAddr + 1 * kOctTexels + blk * 16, cg);
+        tmemLoad16(laneAddr + 2 * kOctTexels + blk * 16, cb);
+        if (!live) continue;
+        // the 16 old texels (two texel rows) are loaded before any store, so the loads overlap instead of
+        // each waiting behind the previous texel's store to the same buffer
+        float4 olds[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          int tex = blk * 16 + i;
+          size_t ai = (size_t)(kProbePix * pzAll + 1 + tex / kOct) * p.g.atlasW + (kProbePix * px + 1 + tex % kOct);
+          olds[i] = loadTexel(p.atlas, p.g.atlasFmt, ai);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          int tex = blk * 16 + i;
+          int tx = tex % kOct, ty = tex / kOct;
+          size_t ai = (size_t)(kProbePix * pzAll + 1 + ty) * p.g.atlasW + (kProbePix * px + 1 + tx);
+          float4 old = olds[i];
+          float s16 = __ldg(&p.wsum16[tex]), s32 = __ldg(&p.wsum32[tex]);
+          float4 out;
+          if (bake) {
+            float tw = old.w + s32;
+            float rr = cr[i] + old.x * old.w, gg = cg[i] + old.y * old.w, bb = cb[i] + old.z * old.w;
+            if (tw > 1e-6f) { rr /= tw; gg /= tw; bb /= tw; }
+            out = make_float4(rr, gg, bb, tw);
+          } else {
+            float rr = cr[i], gg = cg[i], bb = cb[i];
+            if (s16 > 1e-6f) { float inv = 1.0f / s16; rr *= inv; gg *= inv; bb *= inv; }
+            out = make_float4(rr * a + old.x * h, gg * a + old.y * h, bb * a + old.z * h, s32 * a + old.w * h);
+          }
+          storeTexel(p.atlas, p.g.atlasFmt, ai, out);
+        }
+      }
+      tcFenceBefore();
+      mbarArrive(&accEmpty[b]);
+    }
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 1) tmemDealloc(tmem, kTmemCols);
+}
+
+// W[t][j] in 16-bit (rows = texels, K-major), the sums of the rounded weights and of the FP32 weights.
+template <int kFmt>
+__global__ void __launch_bounds__(256) k_tc_weights(int n, const float4* __restrict__ dirs, uint16_t* __restrict__ w16,
+                                                    float* __restrict__ s16, float* __restrict__ s32) {
+  // one block per texel, threads over the rays, block sums through shared memory
+  __shared__ float r16[256], r32[256];
+  int t = blockIdx.x;
+  float3 omega = texelDirection(t % kOct, t / kOct);
+  float a16 = 0.f, a32 = 0.f;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    float w = fmaxf(0.0f, dot3(xyz(dirs[j]), omega));
+    if (!(w > 1e-6f)) w = 0.0f;
+    float r;
+    uint16_t bits;
+    if (kFmt == 0) {
+      __half hv = __float2half_rn(w);
+      bits = __half_as_ushort(hv);
+      r = __half2float(hv);
+    } else {
+      __nv_bfloat16 bv = __float2bfloat16_rn(w);
+      bits = __bfloat16_as_ushort(bv);
+      r = __bfloat162float(bv);
+    }
+    w16[(size_t)t * n + j] = bits;
+    a16 += r;
+    a32 += w;
+  }
+  r16[threadIdx.x] = a16;
+  r32[threadIdx.x] = a32;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      r16[threadIdx.x] += r16[threadIdx.x + o];
+      r32[threadIdx.x] += r32[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s16[t] = r16[0];
+    s32[t] = r32[0];
+  }
+}
+
+// RGBA32F ray image -> planar 16-bit radiance, row c * pTotal + p (p linear over the grid), N rays per row.
+template <int kFmt>
+__global__ void k_pack_rays16(GridGPU g, const float4* __restrict__ rayRad, uint16_t* __restrict__ out, int pBegin,
+                              int pEnd, int pTotal) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)(pEnd - pBegin) * g.N;
+  if (i >= total) return;
+  int p = pBegin + (int)(i / g.N), j = (int)(i % g.N);
+  int px = p % g.X, pzAll = p / g.X;
+  int rx = px * g.bw + (j % g.bw);
+  int ry = pzAll * g.bh + (j / g.bw);
+  float4 v = rayRad[(size_t)ry * g.rayW + rx];
+  float c[3] = {v.x, v.y, v.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    uint16_t bits = kFmt == 0 ? __half_as_ushort(__float2half_rn(c[k])) : __bfloat16_as_ushort(__float2bfloat16_rn(c[k]));
+    out[((size_t)k * pTotal + p) * g.N + j] = bits;
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  });
+  return fn;
+}
+
+// rows x cols matrix of 16-bit values (row-major), boxes of boxRows x 64 with SWIZZLE_128B
+bool makeMap(CUtensorMap* m, int fmt, const void* base, uint64_t rows, uint64_t cols, uint32_t boxRows) {
+  auto fn = encodeFn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kChunkK, boxRows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, fmt == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad, void* out16, int layerBegin,
+                             int layerEnd, int pTotal, cudaStream_t stream) {
+  int pBegin = layerBegin * g.X * g.Z, pEnd = layerEnd * g.X * g.Z;
+  long long total = (long long)(pEnd - pBegin) * g.N;
+  if (total <= 0) return cudaSuccess;
+  unsigned blocks = (unsigned)((total + 255) / 256);
+  if (elemFmt == 0) k_pack_rays16<0><<<blocks, 256, 0, stream>>>(g, rayRad, (uint16_t*)out16, pBegin, pEnd, pTotal);
+  else k_pack_rays16<1><<<blocks, 256, 0, stream>>>(g, rayRad, (uint16_t*)out16, pBegin, pEnd, pTotal);
+  return cudaGetLastError();
+}
+
+size_t tcScratchBytes(int n) { return (size_t)kOctTexels * n * 2 + 2 * kOctTexels * sizeof(float); }
+
+cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
+                         void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
+                         uint32_t* err, cudaStream_t stream) {
+  if (layerEnd <= layerBegin) return cudaSuccess;
+  if (g.N % kChunkK) return cudaErrorInvalidValue;
+  uint16_t* w16 = (uint16_t*)scratch;
+  float* s16 = (float*)((uint8_t*)scratch + (size_t)kOctTexels * g.N * 2);
+  float* s32 = s16 + kOctTexels;
+  if (elemFmt == 0) k_tc_weights<0><<<kOctTexels, 256, 0, stream>>>(g.N, dirs, w16, s16, s32);
+  else k_tc_weights<1><<<kOctTexels, 256, 0, stream>>>(g.N, dirs, w16, s16, s32);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  CUtensorMap tmR, tmW;
+  if (!makeMap(&tmR, elemFmt, rad16, (uint64_t)3 * pTotal, (uint64_t)g.N, kTileP)) return cudaErrorInvalidValue;
+  if (!makeMap(&tmW, elemFmt, w16, kOctTexels, (uint64_t)g.N, kOctTexels)) return cudaErrorInvalidValue;
+  TcParams p;
+  p.g = g;
+  p.wsum16 = s16;
+  p.wsum32 = s32;
+  p.atlas = atlas;
+  p.pBegin = layerBegin * g.X * g.Z;
+  p.pEnd = layerEnd * g.X * g.Z;
+  p.pTotal = pTotal;
+  p.numChunks = g.N / kChunkK;
+  p.hysteresis = hysteresis;
+  p.flags = flags;
+  p.err = err;
+  size_t smem = (size_t)kStages * kStageBytes + 1024;
+  auto kern = elemFmt == 0 ? k_conv_tc<0> : k_conv_tc<1>;
+  // per-process, per-device launch setup (the attribute is a property of the function on each device)
+  static std::mutex mu;
+  static int sms[64] = {};
+  static bool attrSet[64][2] = {};
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!attrSet[dev][elemFmt]) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+      attrSet[dev][elemFmt] = true;
+    }
+  }
+  int tiles = (p.pEnd - p.pBegin + kTileP - 1) / kTileP;
+  int grid = tiles < sms[dev] ? tiles : sms[dev];
+  kern<<<grid, kThreadsTc, smem, stream>>>(tmR, tmW, p);
+  return cudaGetLastError();
+}
+
+}  // namespace ddgi

@@ -22,6 +22,15 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream);
 
+// Tensor-core convolution (conv_tc.cu). rad16: planar 16-bit radiance (elemFmt 0 FP16, 1 BF16), row
+// c * pTotal + p; N a multiple of 64. scratch: tcScratchBytes(N) bytes (16-bit weights + two sum rows).
+size_t tcScratchBytes(int n);
+cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
+                         void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
+                         uint32_t* err, cudaStream_t stream);
+cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad, void* out16, int layerBegin,
+                             int layerEnd, int pTotal, cudaStream_t stream);
+
 // Translation copy (IrradianceProbeTranslationPass.cpp:83-168): out = in shifted by (sx, sz) probes.
 cudaError_t launchTranslate(const GridGPU& g, const void* in, void* out, int sx, int sz, cudaStream_t stream);
 // Fill every texel of the atlas with (0,0,0,1) (clearConvTex, IrradianceProbeConvolvePass.cpp:9-47).

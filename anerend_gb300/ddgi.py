@@ -136,7 +136,7 @@ class ProbeGrid:
         return t
 
     def set_tuning(self, warp_probes: int | None = None, ray_order: int | None = None,
-                   shadow_mode: int | None = None) -> None:
+                   shadow_mode: int | None = None, conv_mode: int | None = None) -> None:
         t = self.tuning
         if warp_probes is not None:
             t.warpProbes = warp_probes
@@ -144,6 +144,8 @@ class ProbeGrid:
             t.rayOrder = ray_order
         if shadow_mode is not None:
             t.shadowMode = shadow_mode
+        if conv_mode is not None:
+            t.convMode = conv_mode
         self.ctx.check(self.ctx.lib.ddgi_grid_set_tuning(self.handle, C.byref(t)))
 
     def reset(self, stream: int = 0) -> None:

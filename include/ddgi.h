@@ -154,7 +154,10 @@ typedef struct DdgiTuning {
   int32_t rayOrder;     /* 0: lattice order; 1: octahedral Morton order of the directions (default) */
   int32_t shadowMode;   /* 0: shadow rays traverse the scene BVH; 1: a BVH built in the sheared ray space of
                            the light direction, rebuilt when the direction changes (default) */
-  int32_t reserved[5];
+  int32_t convMode;     /* 0: FP32 convolution on CUDA cores (default); 1: tcgen05 tensor cores with FP16
+                           radiance and weights; 2: tensor cores with BF16. Tensor-core modes need N % 64 == 0;
+                           accumulation and the hysteresis blend stay FP32 */
+  int32_t reserved[4];
 } DdgiTuning;
 
 /* Device views of the grid's buffers (owned by the grid). */
@@ -262,6 +265,22 @@ int  ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const
 #define DDGI_NOALLOC_MAX_RAYS 512
 int  ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs,
                                void* atlas, int layerBegin, int layerEnd, uint32_t flags, void* stream);
+
+/* 16-bit element formats of the tensor-core convolution's radiance and weights */
+#define DDGI_ELEM_F16  0
+#define DDGI_ELEM_BF16 1
+
+/* probe_conv.comp as a tcgen05 tensor-core GEMM: D_c[probe][texel] = sum_j R_c[probe][j] W[texel][j] per
+ * channel c, FP32 accumulation in tensor memory, then the FP32 normalisation and hysteresis blend (or bake
+ * accumulation) into `atlas`. radiance16: planar 16-bit radiance, 3 x P rows of N values, row c * P + p
+ * with p = (layer * Z + z) * X + x and P = X * Y * Z (see ddgi_pack_rays16). desc->raysPerProbe must be a
+ * multiple of 64. Timeouts of the kernel's bounded waits are reported by ddgi_sync(ctx). */
+int  ddgi_convolve_tc_raw(DdgiContext* ctx, const DdgiGridDesc* desc, const void* radiance16, int elemFormat,
+                          const float* dirs, void* atlas, int layerBegin, int layerEnd, uint32_t flags,
+                          void* stream);
+/* Converts the RGBA32F ray image of layers [layerBegin, layerEnd) into the planar 16-bit layout above. */
+int  ddgi_pack_rays16(const DdgiGridDesc* desc, const float* rayRadiance, void* radiance16, int elemFormat,
+                      int layerBegin, int layerEnd, void* stream);
 
 /* The translation copy of IrradianceProbeTranslationPass.cpp:83-168 from atlasIn to atlasOut (distinct
  * buffers, desc->atlasFormat): atlasOut = atlasIn shifted by (sign(dx), sign(dz)) probes per layer plane. */

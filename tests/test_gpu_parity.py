@@ -189,6 +189,41 @@ def test_fp16_atlas(ctx):
     assert np.percentile(err, 99) <= 5e-3
 
 
+def test_bake_mode_matches_oracle(ctx):
+    """Bake mode (rgen:61-73 tile origin, pbr_light.glsl:276-293 tile lookup, probe_conv.comp:307-319
+    accumulation, translation skipped): four accumulated frames against the oracle."""
+    w = scenes.Workload("bake_8x2x8_n64", (8, 2, 8), (1.0, 1.0, 1.0), 0.0, 64, 1500, (0, -1, 0), (16, 3, 16), 1, 0,
+                        -1.5, 20.0, 4, 0.96)
+    arrays = scenes.build_scene(w)
+    scene = ddgi.Scene(ctx, arrays)
+    grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=L.DDGI_GRID_RECORD_HITS)
+    osc = oracle.OracleScene(arrays, L.SceneDesc)
+    og = oracle.OracleGrid(grid.desc)
+    try:
+        zero = np.zeros(grid.atlas_shape(), np.float32)  # bake starts from an empty accumulation
+        grid.upload_atlas(zero)
+        og.atlas[...] = 0.0
+        for f in range(w.frames):
+            fp = ddgi.FrameParams(camera_pos=(3.7, 0.0, -2.2), rotation=scenes.rotation(9, f),
+                                  flags=L.DDGI_UBO_DDGI_FLAG | L.DDGI_UBO_DDGI_MULTI_FLAG | L.DDGI_UBO_BAKE_MODE_ON_FLAG,
+                                  bake_tile=(0, 0, 16))
+            grid.update(scene, fp)  # ddgi_update skips the translation while baking (TranslationPass.cpp:59)
+            og.trace(osc, fp.to_c())
+            og.convolve(fp.to_c())
+            ctx.sync()
+            _, hits, _ = grid.download_rays(hits=True)
+            certain = og.uncertain == 0
+            assert np.array_equal(hits[certain], og.hits[certain])
+        atlas = grid.download_atlas().astype(np.float64)
+        err = np.abs(atlas - og.atlas) / np.maximum(np.abs(og.atlas), 1e-3)
+        assert np.percentile(err, 99.9) <= 1e-3, np.percentile(err, [50, 99, 99.9, 100])
+        assert atlas[1:9, 1:9, 3].min() > 0  # accumulated weight
+    finally:
+        osc.close()
+        grid.close()
+        scene.close()
+
+
 def test_closed_octahedron_is_watertight(ctx):
     # one probe inside a closed octahedron: every ray of every rotation must hit (no leak at edges/vertices)
     X, Y, Z = 1, 1, 1
