@@ -82,6 +82,21 @@ class Tuning(C.Structure):
                 ("convMode", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("grid", C.c_void_p), ("scene", C.c_void_p)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
+                ("convMode", C.c_int32), ("blocksPerSm", C.c_int32), ("warpsPerFetch", C.c_int32),
+                ("useGraph", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("translations", C.c_uint32), ("graphLaunches", C.c_uint32),
+                ("eagerLaunches", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class GridBuffers(C.Structure):
     _fields_ = [("atlas", C.c_void_p), ("rayRadiance", C.c_void_p), ("rayDirection", C.c_void_p),
                 ("rayHit", C.c_void_p), ("lattice", C.c_void_p),
@@ -113,6 +128,12 @@ SIGNATURES = {
     "ddgi_atlas_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_atlas_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_rays_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ddgi_batch_create": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int, C.POINTER(C.c_void_p)]),
+    "ddgi_batch_destroy": (None, [C.c_void_p]),
+    "ddgi_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    "ddgi_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    "ddgi_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
+    "ddgi_batch_update": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p]),
     "ddgi_fibonacci_lattice": (C.c_int, [C.c_int, C.POINTER(C.c_float), C.c_void_p, C.c_void_p]),
     "ddgi_convolve_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                     C.c_uint32, C.c_void_p]),

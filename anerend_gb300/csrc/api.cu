@@ -3,73 +3,17 @@
 // IrradianceProbeRayTracingPass.cpp:95-165, IrradianceProbeConvolvePass.cpp:109-143) become
 // ddgi_translate / ddgi_trace / ddgi_convolve; their state (_lastProbeIdx, _currentLayer and the
 // "ProbeLayer" blackboard value) lives in the grid object.
-#include "ddgi_common.cuh"
-#include "kernels.h"
-#include "lbvh.h"
+#include "objects.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <new>
-#include <string>
-#include <vector>
 
-using namespace ddgi;
-
-struct DdgiContext {
-  int device = 0;
-  int numSms = 0;
-  uint32_t* dErr = nullptr;  // sticky device error word
-  std::mutex mu;
-  std::string err;
-};
-
-struct DdgiScene {
-  DdgiContext* ctx = nullptr;
-  DdgiPackedVertex* vertices = nullptr;
-  uint32_t* indices = nullptr;
-  DdgiMeshInfo* meshes = nullptr;
-  InstanceGPU* instances = nullptr;
-  DdgiMaterialInfo* materials = nullptr;
-  LbvhResult bvh;
-  DdgiSceneInfo info{};
-  SceneGPU view{};
-  std::vector<InstanceGPU> hostInst;  // host copy (composed into the shadow BVH's transforms)
-  uint64_t numIndices = 0, numVertices = 0;
-  LbvhResult shadowBvh;               // built for shadowLight, rebuilt when the light direction changes
-  float shadowLight[3] = {0, 0, 0};
-  bool shadowValid = false;
-  std::mutex mu;
-};
-
-struct DdgiGrid {
-  DdgiContext* ctx = nullptr;
-  DdgiGridDesc desc{};
-  GridGPU g{};
-  void* atlas[2] = {nullptr, nullptr};  // current atlas and the translation temp (swapped on a move)
-  int cur = 0;
-  float4* rayRad = nullptr;
-  float4* rayDir = nullptr;
-  int* rayHit = nullptr;
-  float4* lattice = nullptr;
-  int* order = nullptr;   // trace-kernel direction order (N ints)
-  DdgiTuning tuning{};
-  void* rad16 = nullptr;  // planar 16-bit radiance for the tensor-core convolution (3 x P x N)
-  void* tcScratch = nullptr;
-  float* wt = nullptr;    // N x 64 convolution weights (transposed)
-  float* wsum = nullptr;  // 64 weight sums
-  int rayH = 0;
-  uint64_t atlasBytes = 0;
-  int lastProbeIdx[2] = {0, 0};  // IrradianceProbeTranslationPass.h:17
-  int currentLayer = 0;          // IrradianceProbeRayTracingPass _currentLayer
-  int tracedBegin = 0, tracedEnd = 0;  // the "ProbeLayer" blackboard value, as a range
-  bool latticeValid = false;
-};
-
-namespace {
+namespace ddgi {
+namespace detail {
 
 int fail(DdgiContext* ctx, int code, const char* fmt, ...) {
   if (ctx) {
@@ -90,11 +34,6 @@ int cudaFail(DdgiContext* ctx, cudaError_t e, const char* what) {
   return fail(ctx, DDGI_EDEVICE, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CK(call, what)                                  \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cudaFail(ctx, e_, what); \
-  } while (0)
 
 bool isPow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
@@ -296,7 +235,28 @@ int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
   return DDGI_OK;
 }
 
-}  // namespace
+
+int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_t st) {
+  DdgiContext* ctx = g->ctx;
+  if (moved) *moved = 0;
+  // IrradianceProbeTranslationPass.cpp:61-80: int() truncation, shift by the sign of the difference
+  int ix = (int)(cameraPos[0] / g->desc.step[0]);
+  int iz = (int)(cameraPos[2] / g->desc.step[2]);
+  int dx = ix - g->lastProbeIdx[0], dz = iz - g->lastProbeIdx[1];
+  if (dx == 0 && dz == 0) return DDGI_OK;
+  g->lastProbeIdx[0] = ix;
+  g->lastProbeIdx[1] = iz;
+  int sx = dx > 0 ? 1 : (dx < 0 ? -1 : 0), sz = dz > 0 ? 1 : (dz < 0 ? -1 : 0);
+  CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, st), "translate");
+  g->cur = 1 - g->cur;
+  if (moved) *moved = 1;
+  return DDGI_OK;
+}
+
+}  // namespace detail
+}  // namespace ddgi
+
+using namespace ddgi::detail;
 
 extern "C" {
 
@@ -477,6 +437,12 @@ int ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out)
   if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = cudaMalloc(&g->rayHit, 4 * rayTexels);
   if (e == cudaSuccess) e = cudaMalloc(&g->lattice, 16 * (size_t)g->g.N);
   if (e == cudaSuccess) e = cudaMalloc(&g->order, sizeof(int) * (size_t)g->g.N);
+  // dTrace is followed by the rotation: one staging copy carries both
+  if (e == cudaSuccess) e = cudaMalloc(&g->dTrace, sizeof(TraceItem) + sizeof(Mat3));
+  if (e == cudaSuccess) g->dRot = reinterpret_cast<Mat3*>(reinterpret_cast<unsigned char*>(g->dTrace) + sizeof(TraceItem));
+  if (e == cudaSuccess) e = cudaMalloc(&g->dQueue, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&g->dConv, sizeof(ConvItem));
+  if (e == cudaSuccess) e = g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem)));
   if (e == cudaSuccess) e = cudaMalloc(&g->wt, 4 * (size_t)g->g.N * kOctTexels);
   if (e == cudaSuccess) e = cudaMalloc(&g->wsum, 4 * kOctTexels);
   if (e == cudaSuccess) e = cudaMemset(g->rayRad, 0, 16 * rayTexels);
@@ -508,6 +474,10 @@ void ddgi_grid_destroy(DdgiGrid* g) {
   cudaFree(g->rayHit);
   cudaFree(g->lattice);
   cudaFree(g->order);
+  cudaFree(g->dTrace);
+  cudaFree(g->dQueue);
+  cudaFree(g->dConv);
+  g->ring.release();
   cudaFree(g->rad16);
   cudaFree(g->tcScratch);
   cudaFree(g->wt);
@@ -554,20 +524,7 @@ int ddgi_grid_reset(DdgiGrid* g, void* stream) {
 
 int ddgi_translate(DdgiGrid* g, const float cameraPos[3], int* moved, void* stream) {
   if (!g || !cameraPos) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_translate");
-  DdgiContext* ctx = g->ctx;
-  if (moved) *moved = 0;
-  // IrradianceProbeTranslationPass.cpp:61-80: int() truncation, shift by the sign of the difference
-  int ix = (int)(cameraPos[0] / g->desc.step[0]);
-  int iz = (int)(cameraPos[2] / g->desc.step[2]);
-  int dx = ix - g->lastProbeIdx[0], dz = iz - g->lastProbeIdx[1];
-  if (dx == 0 && dz == 0) return DDGI_OK;
-  g->lastProbeIdx[0] = ix;
-  g->lastProbeIdx[1] = iz;
-  int sx = dx > 0 ? 1 : (dx < 0 ? -1 : 0), sz = dz > 0 ? 1 : (dz < 0 ? -1 : 0);
-  CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, (cudaStream_t)stream), "translate");
-  g->cur = 1 - g->cur;
-  if (moved) *moved = 1;
-  return DDGI_OK;
+  return translateGrid(g, cameraPos, moved, (cudaStream_t)stream);
 }
 
 int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void* stream) {
@@ -592,13 +549,36 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
     view.shadowNodes = nullptr;
     view.shadowTris = nullptr;
   }
-  CK(launchLattice(g->g.N, frame->rotation, g->lattice, st), "lattice");
-  CK(launchTraceShade(view, g->g, f, g->lattice, g->order, g->atlas[g->cur], g->rayRad, g->rayDir, g->rayHit,
-                      ctx->dErr, st),
+  GridGPU gg = g->g;
+  g->rad16Written = false;
+  if (g->tuning.convMode != 0) {
+    gg.rad16 = g->rad16;
+    gg.rad16Fmt = g->tuning.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
+    gg.pTotal = g->g.X * g->g.Y * g->g.Z;
+  }
+  // the persistent batched kernels with one item (the same code the batched form runs)
+  int slot = 0;
+  unsigned char* h = g->ring.acquire(&slot);
+  TraceItem& ti = *reinterpret_cast<TraceItem*>(h);
+  ti.s = view;
+  ti.g = gg;
+  ti.f = f;
+  ti.lattice = g->lattice;
+  ti.order = g->order;
+  ti.atlasPrev = g->atlas[g->cur];
+  ti.rayRad = g->rayRad;
+  ti.rayDir = g->rayDir;
+  ti.rayHit = g->rayHit;
+  ti.warpBegin = 0;
+  Mat3& rot = *reinterpret_cast<Mat3*>(h + sizeof(TraceItem));
+  memcpy(rot.m, frame->rotation, sizeof(rot.m));
+  CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
+  CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, ctx->numSms * 8, 4, ctx->dErr, st),
      "trace");
   g->tracedBegin = b;
   g->tracedEnd = e;
   g->latticeValid = true;
+  g->rad16Written = gg.rad16 != nullptr;
   return DDGI_OK;
 }
 
@@ -618,15 +598,28 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
   if (g->tuning.convMode != 0) {
     int fmt = g->tuning.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
     int pTotal = g->g.X * g->g.Y * g->g.Z;
-    CK(launchPackRays16(g->g, fmt, g->rayRad, g->rad16, b, e, pTotal, st), "pack rays");
+    if (!g->rad16Written || b < g->tracedBegin || e > g->tracedEnd)
+      CK(launchPackRays16(g->g, fmt, g->rayRad, g->rad16, b, e, pTotal, st), "pack rays");
     CK(launchConvTc(g->g, fmt, g->rad16, pTotal, g->lattice, g->tcScratch, g->atlas[g->cur], b, e, g->desc.hysteresis,
                     frame->flags, ctx->dErr, st),
        "tensor-core convolve");
     return DDGI_OK;
   }
-  CK(launchConvWeights(g->g.N, g->lattice, g->wt, g->wsum, st), "conv weights");
-  CK(launchConvFp32(g->g, g->rayRad, g->wt, g->wsum, g->atlas[g->cur], b, e, g->desc.hysteresis, frame->flags, st),
-     "convolve");
+  int slot = 0;
+  ConvItem& ci = *reinterpret_cast<ConvItem*>(g->ring.acquire(&slot));
+  ci.g = g->g;
+  ci.rayRad = g->rayRad;
+  ci.dirs = g->lattice;
+  ci.wt = g->wt;
+  ci.wsum = g->wsum;
+  ci.atlas = g->atlas[g->cur];
+  ci.layerBegin = b;
+  ci.layerEnd = e;
+  ci.hysteresis = g->desc.hysteresis;
+  ci.flags = frame->flags;
+  ci.groupBegin = 0;
+  CK(g->ring.copy(slot, g->dConv, sizeof(ConvItem), st), "convolve record");
+  CK(launchConvFp32Batch(g->dConv, 1, convGroups(g->g, b, e), st), "convolve");
   return DDGI_OK;
 }
 

@@ -117,7 +117,100 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_fp32(GridGPU g, const flo
   }
 }
 
+// ---- many grids in one launch -------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_conv_weights_batch(const ConvItem* __restrict__ items) {
+  __shared__ float part[256];
+  const ConvItem& it = items[blockIdx.y];
+  const int n = it.g.N;
+  int t = blockIdx.x;
+  float3 omega = texelDirection(t % kOct, t / kOct);
+  float s = 0.0f;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    float w = fmaxf(0.0f, dot3(xyz(it.dirs[j]), omega));
+    if (!(w > 1e-6f)) w = 0.0f;
+    it.wt[j * kOctTexels + t] = w;
+    s += w;
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) it.wsum[t] = part[0];
+}
+
+// Each block takes a contiguous range of probe groups (4 probes x 64 texels), so a block mostly stays
+// inside one item; the item's N x 64 weight table is read through L1.
+__global__ void __launch_bounds__(kConvThreads) k_conv_fp32_batch(const ConvItem* __restrict__ items, int numItems,
+                                                                  long long totalGroups) {
+  const int t = threadIdx.x % kOctTexels;
+  const int q = threadIdx.x / kOctTexels;
+  long long per = (totalGroups + gridDim.x - 1) / gridDim.x;
+  long long g0 = (long long)blockIdx.x * per, g1 = min(totalGroups, g0 + per);
+  for (long long grp = g0; grp < g1; ++grp) {
+    int lo = 0, hi = numItems - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (items[mid].groupBegin <= grp) lo = mid; else hi = mid - 1;
+    }
+    const ConvItem& it = items[lo];
+    const GridGPU& g = it.g;
+    const int probesPerLayer = g.X * g.Z;
+    long long pl = (grp - it.groupBegin) * kConvProbes + q;
+    long long total = (long long)(it.layerEnd - it.layerBegin) * probesPerLayer;
+    if (pl >= total) continue;
+    int layer = it.layerBegin + (int)(pl / probesPerLayer);
+    int p = (int)(pl % probesPerLayer);
+    int px = p % g.X, pz = p / g.X;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const float* W = it.wt;
+    for (int j = 0; j < g.N; ++j) {
+      int rx = px * g.bw + (j % g.bw);
+      int ry = (layer * g.Z + pz) * g.bh + (j / g.bw);
+      float4 L = __ldg(&it.rayRad[(size_t)ry * g.rayW + rx]);
+      float w = __ldg(&W[j * kOctTexels + t]);
+      ax = fmaf(w, L.x, ax);
+      ay = fmaf(w, L.y, ay);
+      az = fmaf(w, L.z, az);
+    }
+    const float ws = __ldg(&it.wsum[t]);
+    int tx = t % kOct, ty = t / kOct;
+    size_t ai = (size_t)(kProbePix * (layer * g.Z + pz) + 1 + ty) * g.atlasW + (kProbePix * px + 1 + tx);
+    float4 old = loadTexel(it.atlas, g.atlasFmt, ai);
+    float4 out;
+    if (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) {
+      float tw = old.w + ws;
+      float3 tot = f3(ax, ay, az) + xyz(old) * old.w;
+      if (tw > 1e-6f) tot = tot / tw;
+      out = make_float4(tot.x, tot.y, tot.z, tw);
+    } else {
+      float3 res = f3(ax, ay, az);
+      if (ws > 1e-6f) res = res / ws;
+      float h = it.hysteresis, a = 1.0f - h;
+      out = make_float4(res.x * a + old.x * h, res.y * a + old.y * h, res.z * a + old.z * h, ws * a + old.w * h);
+    }
+    storeTexel(it.atlas, g.atlasFmt, ai, out);
+  }
+}
+
 }  // namespace
+
+long long convGroups(const GridGPU& g, int layerBegin, int layerEnd) {
+  return ((long long)(layerEnd - layerBegin) * g.X * g.Z + kConvProbes - 1) / kConvProbes;
+}
+
+cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream) {
+  if (numItems <= 0 || totalGroups <= 0) return cudaSuccess;
+  k_conv_weights_batch<<<dim3(kOctTexels, numItems), 256, 0, stream>>>(dItems);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long grid = (long long)sms * 8;
+  if (grid > totalGroups) grid = totalGroups;
+  k_conv_fp32_batch<<<(unsigned)grid, kConvThreads, 0, stream>>>(dItems, numItems, totalGroups);
+  return cudaGetLastError();
+}
 
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream) {
   k_conv_weights<<<kOctTexels, 256, 0, stream>>>(n, dirs, wt, wsum);

@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstring>
 #include <mutex>
 
 namespace ddgi {
@@ -127,22 +128,53 @@ __host__ __device__ constexpr uint32_t instrDesc(uint32_t fmt) {
   return (1u << 4) | (fmt << 7) | (fmt << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 }
 
-struct TcParams {
-  GridGPU g;
-  const float* wsum16;  // 64 sums of the rounded weights (normalisation)
-  const float* wsum32;  // 64 sums of the FP32 weights (the .w channel)
-  void* atlas;
-  int pBegin, pEnd;     // probe range (linear over the whole grid)
-  int pTotal;           // rows per channel in the radiance matrix
-  int numChunks;        // N / 64
+constexpr int kMaxTcItems = 64;
+
+// Per-grid record of a (batched) tensor-core convolution, in device memory so that per-frame values (atlas
+// after a translation, layer range, flags) can change between replays of a captured launch.
+struct TcItem {
+  int X, atlasW, atlasFmt;
+  int pBegin, pEnd;       // probe range (linear over the grid, layer-major)
+  int pTotal;             // rows per channel of the radiance matrix
+  int numChunks;          // N / 64
+  int tileBegin;          // first batch tile of this item
   float hysteresis;
   uint32_t flags;
-  uint32_t* err;
+  void* atlas;
+  const float4* dirs;     // lattice of the frame
+  uint16_t* w16;          // 64 x N weights (written by k_tc_weights)
+  float* wsum16;          // sums of the rounded weights (normalisation)
+  float* wsum32;          // sums of the FP32 weights (the .w channel)
+  int n;
 };
+
+// Tensor maps of every item (radiance R, weights W); static for a batch, passed as a kernel parameter.
+struct TcMaps {
+  CUtensorMap r[kMaxTcItems];
+  CUtensorMap w[kMaxTcItems];
+};
+
+// Item records are kTcItemStride bytes apart in device memory (the host stages them in 128-byte slots).
+constexpr int kTcItemStride = 128;
+static_assert(sizeof(TcItem) <= kTcItemStride, "TcItem must fit its 128-byte record slot");
+
+DDGI_HD const TcItem& tcItem(const unsigned char* recs, int i) {
+  return *reinterpret_cast<const TcItem*>(recs + (size_t)i * kTcItemStride);
+}
+
+DDGI_D int tcItemOf(const unsigned char* items, int numItems, int tile) {
+  int lo = 0, hi = numItems - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (tcItem(items, mid).tileBegin <= tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
 
 template <int kFmt>
 __global__ void __launch_bounds__(kThreadsTc, 1)
-    k_conv_tc(const __grid_constant__ CUtensorMap tmR, const __grid_constant__ CUtensorMap tmW, TcParams p) {
+    k_conv_tc(const __grid_constant__ TcMaps maps, const unsigned char* __restrict__ items, int numItems, int totalTiles,
+              uint32_t* __restrict__ err) {
   extern __shared__ uint8_t smemRaw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smemRaw + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t fullBar[kStages], emptyBar[kStages], accFull[2], accEmpty[2], drainBar;
@@ -150,7 +182,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   __shared__ int abortFlag;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles = (p.pEnd - p.pBegin + kTileP - 1) / kTileP;
+  const int tiles = totalTiles;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) { mbarInit(&fullBar[s], 1); mbarInit(&emptyBar[s], 1); }
@@ -166,7 +198,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   const uint32_t tmem = tmemSlot;
 
   auto fail = [&]() {
-    atomicOr(p.err, DDGI_DEVERR_TIMEOUT);
+    atomicOr(err, DDGI_DEVERR_TIMEOUT);
     atomicExch(&abortFlag, 1);
   };
   auto aborted = [&]() { return *(volatile int*)&abortFlag != 0; };
@@ -179,14 +211,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       int s = 0;
       uint32_t phase = 0;
       for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x) {
-        int p0 = p.pBegin + t * kTileP;
-        for (int kc = 0; kc < p.numChunks; ++kc) {
+        const int ii = tcItemOf(items, numItems, t);
+        const TcItem& it = tcItem(items, ii);
+        const int p0 = it.pBegin + (t - it.tileBegin) * kTileP;
+        for (int kc = 0; kc < it.numChunks; ++kc) {
           if (!mbarWait(&emptyBar[s], phase ^ 1)) { fail(); break; }
           pending[s] = false;
           uint8_t* st = smem + (size_t)s * kStageBytes;
           mbarExpectTx(&fullBar[s], kStageBytes);
-          for (int c = 0; c < 3; ++c) tmaLoad2d(st + c * kATileBytes, &tmR, &fullBar[s], kc * kChunkK, c * p.pTotal + p0);
-          tmaLoad2d(st + 3 * kATileBytes, &tmW, &fullBar[s], kc * kChunkK, 0);
+          for (int c = 0; c < 3; ++c)
+            tmaLoad2d(st + c * kATileBytes, &maps.r[ii], &fullBar[s], kc * kChunkK, c * it.pTotal + p0);
+          tmaLoad2d(st + 3 * kATileBytes, &maps.w[ii], &fullBar[s], kc * kChunkK, 0);
           pending[s] = true;
           pendingParity[s] = phase;
           if (++s == kStages) { s = 0; phase ^= 1; }
@@ -206,13 +241,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       int local = 0;
       bool issued = false;
       for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
+        const int numChunks = tcItem(items, tcItemOf(items, numItems, t)).numChunks;
         int b = local & 1;
         uint32_t accPhase = (local >> 1) & 1;
         if (!mbarWait(&accEmpty[b], accPhase ^ 1)) { fail(); break; }
         tcFenceAfter();
         const uint32_t dBase = tmem + (uint32_t)(b * 3 * kOctTexels);
         bool ok = true;
-        for (int kc = 0; kc < p.numChunks; ++kc) {
+        for (int kc = 0; kc < numChunks; ++kc) {
           if (!mbarWait(&fullBar[s], phase)) { fail(); ok = false; break; }
           tcFenceAfter();
           uint32_t st = smemU32(smem + (size_t)s * kStageBytes);
@@ -241,20 +277,21 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     // ---- epilogue: warps 2..5, thread = probe row of the tile ----
     const int quarter = warp & 3;  // TMEM lane quarter this warp may access
     const int row = quarter * 32 + lane;
-    const bool bake = (p.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
-    const float h = p.hysteresis, a = 1.0f - h;
     int local = 0;
     for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
+      const TcItem& it = tcItem(items, tcItemOf(items, numItems, t));
+      const bool bake = (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
+      const float h = it.hysteresis, a = 1.0f - h;
       int b = local & 1;
       uint32_t accPhase = (local >> 1) & 1;
       if (!mbarWait(&accFull[b], accPhase)) { fail(); break; }
       tcFenceAfter();
-      const int probe = p.pBegin + t * kTileP + row;
-      const bool live = probe < p.pEnd;
+      const int probe = it.pBegin + (t - it.tileBegin) * kTileP + row;
+      const bool live = probe < it.pEnd;
       int px = 0, pzAll = 0;
       if (live) {
-        px = probe % p.g.X;
-        pzAll = probe / p.g.X;  // layer * Z + z
+        px = probe % it.X;
+        pzAll = probe / it.X;  // layer * Z + z
       }
       const uint32_t laneAddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 3 * kOctTexels);
 #pragma unroll 1
@@ -270,16 +307,16 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           int tex = blk * 16 + i;
-          size_t ai = (size_t)(kProbePix * pzAll + 1 + tex / kOct) * p.g.atlasW + (kProbePix * px + 1 + tex % kOct);
-          olds[i] = loadTexel(p.atlas, p.g.atlasFmt, ai);
+          size_t ai = (size_t)(kProbePix * pzAll + 1 + tex / kOct) * it.atlasW + (kProbePix * px + 1 + tex % kOct);
+          olds[i] = loadTexel(it.atlas, it.atlasFmt, ai);
         }
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           int tex = blk * 16 + i;
           int tx = tex % kOct, ty = tex / kOct;
-          size_t ai = (size_t)(kProbePix * pzAll + 1 + ty) * p.g.atlasW + (kProbePix * px + 1 + tx);
+          size_t ai = (size_t)(kProbePix * pzAll + 1 + ty) * it.atlasW + (kProbePix * px + 1 + tx);
           float4 old = olds[i];
-          float s16 = __ldg(&p.wsum16[tex]), s32 = __ldg(&p.wsum32[tex]);
+          float s16 = __ldg(&it.wsum16[tex]), s32 = __ldg(&it.wsum32[tex]);
           float4 out;
           if (bake) {
             float tw = old.w + s32;
@@ -291,7 +328,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
             if (s16 > 1e-6f) { float inv = 1.0f / s16; rr *= inv; gg *= inv; bb *= inv; }
             out = make_float4(rr * a + old.x * h, gg * a + old.y * h, bb * a + old.z * h, s32 * a + old.w * h);
           }
-          storeTexel(p.atlas, p.g.atlasFmt, ai, out);
+          storeTexel(it.atlas, it.atlasFmt, ai, out);
         }
       }
       tcFenceBefore();
@@ -305,16 +342,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
 }
 
 // W[t][j] in 16-bit (rows = texels, K-major), the sums of the rounded weights and of the FP32 weights.
+// W[t][j] in 16-bit (rows = texels, K-major), the sums of the rounded weights and of the FP32 weights;
+// one block per (texel, item), threads over the rays.
 template <int kFmt>
-__global__ void __launch_bounds__(256) k_tc_weights(int n, const float4* __restrict__ dirs, uint16_t* __restrict__ w16,
-                                                    float* __restrict__ s16, float* __restrict__ s32) {
-  // one block per texel, threads over the rays, block sums through shared memory
+__global__ void __launch_bounds__(256) k_tc_weights(const unsigned char* __restrict__ items) {
   __shared__ float r16[256], r32[256];
+  const TcItem& it = tcItem(items, blockIdx.y);
+  const int n = it.n;
   int t = blockIdx.x;
   float3 omega = texelDirection(t % kOct, t / kOct);
   float a16 = 0.f, a32 = 0.f;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    float w = fmaxf(0.0f, dot3(xyz(dirs[j]), omega));
+    float w = fmaxf(0.0f, dot3(xyz(it.dirs[j]), omega));
     if (!(w > 1e-6f)) w = 0.0f;
     float r;
     uint16_t bits;
@@ -327,7 +366,7 @@ __global__ void __launch_bounds__(256) k_tc_weights(int n, const float4* __restr
       bits = __bfloat16_as_ushort(bv);
       r = __bfloat162float(bv);
     }
-    w16[(size_t)t * n + j] = bits;
+    it.w16[(size_t)t * n + j] = bits;
     a16 += r;
     a32 += w;
   }
@@ -342,8 +381,8 @@ __global__ void __launch_bounds__(256) k_tc_weights(int n, const float4* __restr
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    s16[t] = r16[0];
-    s32[t] = r32[0];
+    it.wsum16[t] = r16[0];
+    it.wsum32[t] = r32[0];
   }
 }
 
@@ -407,35 +446,60 @@ cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad
   return cudaGetLastError();
 }
 
-size_t tcScratchBytes(int n) { return (size_t)kOctTexels * n * 2 + 2 * kOctTexels * sizeof(float); }
+size_t tcScratchBytes(int n) { return (size_t)kOctTexels * n * 2 + 2 * kOctTexels * sizeof(float) + 256; }
 
-cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
-                         void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
-                         uint32_t* err, cudaStream_t stream) {
-  if (layerEnd <= layerBegin) return cudaSuccess;
-  if (g.N % kChunkK) return cudaErrorInvalidValue;
-  uint16_t* w16 = (uint16_t*)scratch;
-  float* s16 = (float*)((uint8_t*)scratch + (size_t)kOctTexels * g.N * 2);
-  float* s32 = s16 + kOctTexels;
-  if (elemFmt == 0) k_tc_weights<0><<<kOctTexels, 256, 0, stream>>>(g.N, dirs, w16, s16, s32);
-  else k_tc_weights<1><<<kOctTexels, 256, 0, stream>>>(g.N, dirs, w16, s16, s32);
+int tcMaxItems() { return kMaxTcItems; }
+
+// Fills the item record and its two tensor maps for one grid; scratch = tcScratchBytes(N) bytes.
+bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs, void* scratch,
+                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int tileBegin,
+                   TcItemHost* out) {
+  if (g.N % kChunkK) return false;
+  TcItem& it = *reinterpret_cast<TcItem*>(out->item);
+  static_assert(sizeof(TcItem) <= sizeof(out->item), "TcItemHost too small");
+  it.X = g.X;
+  it.atlasW = g.atlasW;
+  it.atlasFmt = g.atlasFmt;
+  it.pBegin = layerBegin * g.X * g.Z;
+  it.pEnd = layerEnd * g.X * g.Z;
+  it.pTotal = pTotal;
+  it.numChunks = g.N / kChunkK;
+  it.tileBegin = tileBegin;
+  it.hysteresis = hysteresis;
+  it.flags = flags;
+  it.atlas = atlas;
+  it.dirs = dirs;
+  it.w16 = (uint16_t*)scratch;
+  it.wsum16 = (float*)((uint8_t*)scratch + (size_t)kOctTexels * g.N * 2);
+  it.wsum32 = it.wsum16 + kOctTexels;
+  it.n = g.N;
+  out->tiles = (it.pEnd - it.pBegin + kTileP - 1) / kTileP;
+  if (!makeMap(reinterpret_cast<CUtensorMap*>(out->mapR), elemFmt, rad16, (uint64_t)3 * pTotal, (uint64_t)g.N, kTileP))
+    return false;
+  if (!makeMap(reinterpret_cast<CUtensorMap*>(out->mapW), elemFmt, it.w16, kOctTexels, (uint64_t)g.N, kOctTexels))
+    return false;
+  return true;
+}
+
+// Weights of every item, then the tensor-core convolution of all items' tiles in one launch.
+// dItems: numItems TcItem records in device memory (copied from the TcItemHost.item bytes).
+cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
+                              int totalTiles, uint32_t* err, cudaStream_t stream) {
+  if (numItems <= 0 || totalTiles <= 0) return cudaSuccess;
+  if (numItems > kMaxTcItems) return cudaErrorInvalidValue;
+  const unsigned char* items = (const unsigned char*)dItems;
+  dim3 wg(kOctTexels, numItems);
+  if (elemFmt == 0) k_tc_weights<0><<<wg, 256, 0, stream>>>(items);
+  else k_tc_weights<1><<<wg, 256, 0, stream>>>(items);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  CUtensorMap tmR, tmW;
-  if (!makeMap(&tmR, elemFmt, rad16, (uint64_t)3 * pTotal, (uint64_t)g.N, kTileP)) return cudaErrorInvalidValue;
-  if (!makeMap(&tmW, elemFmt, w16, kOctTexels, (uint64_t)g.N, kOctTexels)) return cudaErrorInvalidValue;
-  TcParams p;
-  p.g = g;
-  p.wsum16 = s16;
-  p.wsum32 = s32;
-  p.atlas = atlas;
-  p.pBegin = layerBegin * g.X * g.Z;
-  p.pEnd = layerEnd * g.X * g.Z;
-  p.pTotal = pTotal;
-  p.numChunks = g.N / kChunkK;
-  p.hysteresis = hysteresis;
-  p.flags = flags;
-  p.err = err;
+  static TcMaps maps;  // host staging of the kernel parameter (copied at launch)
+  static std::mutex mapsMu;
+  std::lock_guard<std::mutex> lk(mapsMu);
+  for (int i = 0; i < numItems; ++i) {
+    memcpy(&maps.r[i], hostItems[i].mapR, sizeof(CUtensorMap));
+    memcpy(&maps.w[i], hostItems[i].mapW, sizeof(CUtensorMap));
+  }
   size_t smem = (size_t)kStages * kStageBytes + 1024;
   auto kern = elemFmt == 0 ? k_conv_tc<0> : k_conv_tc<1>;
   // per-process, per-device launch setup (the attribute is a property of the function on each device)
@@ -446,7 +510,7 @@ cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int p
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   {
-    std::lock_guard<std::mutex> lk(mu);
+    std::lock_guard<std::mutex> lk2(mu);
     if (!attrSet[dev][elemFmt]) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -454,10 +518,23 @@ cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int p
       attrSet[dev][elemFmt] = true;
     }
   }
-  int tiles = (p.pEnd - p.pBegin + kTileP - 1) / kTileP;
-  int grid = tiles < sms[dev] ? tiles : sms[dev];
-  kern<<<grid, kThreadsTc, smem, stream>>>(tmR, tmW, p);
+  int grid = totalTiles < sms[dev] ? totalTiles : sms[dev];
+  kern<<<grid, kThreadsTc, smem, stream>>>(maps, items, numItems, totalTiles, err);
   return cudaGetLastError();
+}
+
+// One grid: the item record lives at the end of the scratch buffer.
+cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
+                         void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
+                         uint32_t* err, cudaStream_t stream) {
+  if (layerEnd <= layerBegin) return cudaSuccess;
+  TcItemHost h;
+  if (!tcPrepareItem(g, elemFmt, rad16, pTotal, dirs, scratch, atlas, layerBegin, layerEnd, hysteresis, flags, 0, &h))
+    return cudaErrorInvalidValue;
+  void* dItem = (uint8_t*)scratch + tcScratchBytes(g.N) - 256;
+  cudaError_t e = cudaMemcpyAsync(dItem, h.item, sizeof(h.item), cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return e;
+  return launchConvTcItems(elemFmt, &h, dItem, 1, h.tiles, err, stream);
 }
 
 }  // namespace ddgi

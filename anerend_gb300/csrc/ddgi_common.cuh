@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
+#include <cuda_bf16.h>
 #include <stdint.h>
 #include "../../include/ddgi.h"
 
@@ -221,6 +222,9 @@ struct GridGPU {
   int rayW;
   uint32_t options;
   int warpProbes;  // probes per warp (power of two, 32 / warpProbes <= N)
+  void* rad16;     // when set, the trace also writes planar 16-bit radiance (row c * pTotal + p, N per row)
+  int rad16Fmt;    // 0 FP16, 1 BF16
+  int pTotal;      // probes of the grid (rows per channel of rad16)
 };
 
 struct FrameGPU {

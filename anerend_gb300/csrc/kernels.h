@@ -10,10 +10,29 @@ struct Mat3 {
   float m[9];
 };
 
+
+// Everything the trace of one grid needs; an array of these drives the persistent batched trace.
+struct TraceItem {
+  SceneGPU s;
+  GridGPU g;
+  FrameGPU f;
+  const float4* lattice;  // written by the batched lattice kernel
+  const int* order;
+  const void* atlasPrev;
+  float4* rayRad;
+  float4* rayDir;
+  int* rayHit;
+  long long warpBegin;    // first queue warp of this item
+};
+
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);
-cudaError_t launchTraceShade(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* lattice,
-                             const int* order, const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit,
-                             uint32_t* err, cudaStream_t stream);
+// Warps of one grid's trace for frame f (the queue length of its item).
+long long traceWarps(const GridGPU& g, const FrameGPU& f);
+// Lattices of every item (rotation per item), then the persistent trace of all items' rays.
+cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
+                             unsigned long long* dQueue, int blocks, int warpsPerFetch, uint32_t* err,
+                             cudaStream_t stream);
+
 
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream);
@@ -22,9 +41,38 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream);
 
+// FP32 convolution of many grids in one launch (conv.cu).
+struct ConvItem {
+  GridGPU g;
+  const float4* rayRad;
+  const float4* dirs;
+  float* wt;        // N x 64 weights of this item (written by the weights kernel)
+  float* wsum;
+  void* atlas;
+  int layerBegin, layerEnd;
+  float hysteresis;
+  uint32_t flags;
+  long long groupBegin;  // first 4-probe group of this item
+};
+long long convGroups(const GridGPU& g, int layerBegin, int layerEnd);
+cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream);
+
 // Tensor-core convolution (conv_tc.cu). rad16: planar 16-bit radiance (elemFmt 0 FP16, 1 BF16), row
 // c * pTotal + p; N a multiple of 64. scratch: tcScratchBytes(N) bytes (16-bit weights + two sum rows).
 size_t tcScratchBytes(int n);
+int tcMaxItems();
+// Host image of one tensor-core item: the device record bytes and its two tensor maps.
+struct TcItemHost {
+  alignas(64) unsigned char mapR[128];
+  alignas(64) unsigned char mapW[128];
+  alignas(16) unsigned char item[128];
+  int tiles;
+};
+bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs, void* scratch,
+                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int tileBegin,
+                   TcItemHost* out);
+cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
+                              int totalTiles, uint32_t* err, cudaStream_t stream);
 cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
                          void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                          uint32_t* err, cudaStream_t stream);

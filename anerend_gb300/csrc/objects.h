@@ -1,0 +1,131 @@
+// Internal objects of the C ABI (context, scene, grid) and the host helpers shared by api.cu and batch.cu.
+#pragma once
+
+#include "ddgi_common.cuh"
+#include "kernels.h"
+#include "lbvh.h"
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace ddgi;
+
+// Pinned host staging for per-launch records copied to the device with cudaMemcpyAsync: a ring of slots,
+// each reused only after the copy that last read it has executed (an event per slot).
+struct StagingRing {
+  static constexpr int kSlots = 4;
+  unsigned char* host = nullptr;
+  size_t slotBytes = 0;
+  cudaEvent_t done[kSlots] = {};
+  int next = 0;
+
+  cudaError_t init(size_t bytes) {
+    slotBytes = (bytes + 255) & ~(size_t)255;
+    cudaError_t e = cudaMallocHost(&host, slotBytes * kSlots);
+    for (int i = 0; i < kSlots && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+    return e;
+  }
+  void release() {
+    for (int i = 0; i < kSlots; ++i)
+      if (done[i]) cudaEventDestroy(done[i]);
+    if (host) cudaFreeHost(host);
+    host = nullptr;
+  }
+  // A slot whose previous copy has finished (waits for it on the host).
+  unsigned char* acquire(int* slot) {
+    int s = next;
+    next = (next + 1) % kSlots;
+    cudaEventSynchronize(done[s]);
+    *slot = s;
+    return host + s * slotBytes;
+  }
+  // Copies `bytes` of slot `slot` to `dst` on `st` and marks the slot busy until the copy has run.
+  cudaError_t copy(int slot, void* dst, size_t bytes, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(dst, host + slot * slotBytes, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(done[slot], st);
+    return e;
+  }
+};
+
+
+struct DdgiContext {
+  int device = 0;
+  int numSms = 0;
+  uint32_t* dErr = nullptr;  // sticky device error word
+  std::mutex mu;
+  std::string err;
+};
+
+struct DdgiScene {
+  DdgiContext* ctx = nullptr;
+  DdgiPackedVertex* vertices = nullptr;
+  uint32_t* indices = nullptr;
+  DdgiMeshInfo* meshes = nullptr;
+  InstanceGPU* instances = nullptr;
+  DdgiMaterialInfo* materials = nullptr;
+  LbvhResult bvh;
+  DdgiSceneInfo info{};
+  SceneGPU view{};
+  std::vector<InstanceGPU> hostInst;  // host copy (composed into the shadow BVH's transforms)
+  uint64_t numIndices = 0, numVertices = 0;
+  LbvhResult shadowBvh;               // built for shadowLight, rebuilt when the light direction changes
+  float shadowLight[3] = {0, 0, 0};
+  bool shadowValid = false;
+  std::mutex mu;
+};
+
+struct DdgiGrid {
+  DdgiContext* ctx = nullptr;
+  DdgiGridDesc desc{};
+  GridGPU g{};
+  void* atlas[2] = {nullptr, nullptr};  // current atlas and the translation temp (swapped on a move)
+  int cur = 0;
+  float4* rayRad = nullptr;
+  float4* rayDir = nullptr;
+  int* rayHit = nullptr;
+  float4* lattice = nullptr;
+  int* order = nullptr;   // trace-kernel direction order (N ints)
+  DdgiTuning tuning{};
+  void* rad16 = nullptr;  // planar 16-bit radiance for the tensor-core convolution (3 x P x N)
+  void* tcScratch = nullptr;
+  float* wt = nullptr;    // N x 64 convolution weights (transposed)
+  float* wsum = nullptr;  // 64 weight sums
+  int rayH = 0;
+  uint64_t atlasBytes = 0;
+  int lastProbeIdx[2] = {0, 0};  // IrradianceProbeTranslationPass.h:17
+  int currentLayer = 0;          // IrradianceProbeRayTracingPass _currentLayer
+  int tracedBegin = 0, tracedEnd = 0;  // the "ProbeLayer" blackboard value, as a range
+  bool latticeValid = false;
+  bool rad16Written = false;  // the last trace also wrote the 16-bit radiance of its layers
+  // single-item records of the trace and FP32 convolution (the grid runs the batched kernels with one item)
+  TraceItem* dTrace = nullptr;
+  Mat3* dRot = nullptr;
+  unsigned long long* dQueue = nullptr;
+  ConvItem* dConv = nullptr;
+  StagingRing ring;
+};
+
+namespace ddgi {
+namespace detail {
+
+int fail(DdgiContext* ctx, int code, const char* fmt, ...);
+int cudaFail(DdgiContext* ctx, cudaError_t e, const char* what);
+int validateGridDesc(DdgiContext* ctx, const DdgiGridDesc* d);
+GridGPU makeGridGPU(const DdgiGridDesc& d);
+int applyTuning(DdgiGrid* g, const DdgiTuning& t);
+int frameToGPU(DdgiContext* ctx, const DdgiFrame* f, FrameGPU& out);
+int layerRange(DdgiGrid* grid, int layer, bool advance, int& b, int& e);
+int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st);
+// translation state update of ddgi_translate without the C-ABI argument checks
+int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_t st);
+
+}  // namespace detail
+}  // namespace ddgi
+
+#define CK(call, what)                                               \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) return ::ddgi::detail::cudaFail(ctx, e_, what); \
+  } while (0)
+

@@ -280,12 +280,11 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 #ifndef DDGI_TRACE_MIN_BLOCKS
 #define DDGI_TRACE_MIN_BLOCKS 8
 #endif
-__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
-    k_trace_shade(SceneGPU s, GridGPU g, FrameGPU f, const float4* __restrict__ lattice,
-                  const int* __restrict__ order, const void* __restrict__ atlasPrev, float4* __restrict__ rayRad,
-                  float4* __restrict__ rayDir, int* __restrict__ rayHit, uint32_t* __restrict__ err) {
-  long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+// One warp of probe rays (warp index `warp` of the grid's trace, lanes past the grid's rays idle).
+DDGI_D void traceWarp(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* __restrict__ lattice,
+                      const int* __restrict__ order, const void* __restrict__ atlasPrev,
+                      float4* __restrict__ rayRad, float4* __restrict__ rayDir, int* __restrict__ rayHit,
+                      uint32_t* __restrict__ err, long long warp, int lane) {
   const int D = 32 / g.warpProbes;                // directions per warp
   const int dirChunks = g.N / D;
   const int probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
@@ -382,6 +381,61 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
   rayRad[idx] = make_float4(L.x, L.y, L.z, 1.0f);
   if (rayDir) rayDir[idx] = make_float4(dir.x, dir.y, dir.z, 1.0f);
   if (rayHit) rayHit[idx] = hitCode;
+  if (g.rad16) {  // operand of the tensor-core convolution
+    size_t base = ((size_t)(layer * g.Z + pz) * g.X + px) * g.N + j;
+    size_t plane = (size_t)g.pTotal * g.N;
+    uint16_t* o = (uint16_t*)g.rad16;
+    float c[3] = {L.x, L.y, L.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      o[base + k * plane] = g.rad16Fmt == 0 ? __half_as_ushort(__float2half_rn(c[k]))
+                                            : __bfloat16_as_ushort(__float2bfloat16_rn(c[k]));
+  }
+}
+
+// Persistent trace over many grids: warps take `warpsPerFetch` warps of work at a time from one queue that
+// spans every item's rays (item i owns warps [warpBegin_i, warpBegin_i + numWarps_i)).
+__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+    k_trace_batch(const TraceItem* __restrict__ items, int numItems, long long totalWarps,
+                  unsigned long long* __restrict__ queue, int warpsPerFetch, uint32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(queue, (unsigned long long)warpsPerFetch);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((long long)base >= totalWarps) break;
+    for (int k = 0; k < warpsPerFetch; ++k) {
+      long long w = (long long)base + k;
+      if (w >= totalWarps) break;
+      int lo = 0, hi = numItems - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (items[mid].warpBegin <= w) lo = mid; else hi = mid - 1;
+      }
+      const TraceItem& it = items[lo];
+      traceWarp(it.s, it.g, it.f, it.lattice, it.order, it.atlasPrev, it.rayRad, it.rayDir, it.rayHit, err,
+                w - it.warpBegin, lane);
+      __syncwarp();
+    }
+  }
+}
+
+// Rotated lattices of many grids: one block row per item.
+__global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3* __restrict__ rots) {
+  const TraceItem& it = items[blockIdx.y];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= it.g.N) return;
+  double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
+  double phi = acos(1.0 - 2.0 * ((double)i + 0.5) / (double)it.g.N);
+  double sp = sin(phi);
+  double v[3] = {cos(theta) * sp, sin(theta) * sp, cos(phi)};
+  double len = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  v[0] /= len; v[1] /= len; v[2] /= len;
+  const float* m = rots[blockIdx.y].m;
+  double r[3];
+  for (int row = 0; row < 3; ++row)
+    r[row] = (double)m[row] * v[0] + (double)m[3 + row] * v[1] + (double)m[6 + row] * v[2];
+  const_cast<float4*>(it.lattice)[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -392,17 +446,23 @@ cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t s
   return cudaGetLastError();
 }
 
-cudaError_t launchTraceShade(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* lattice,
-                             const int* order, const void* atlasPrev, float4* rayRad, float4* rayDir, int* rayHit,
-                             uint32_t* err, cudaStream_t stream) {
+long long traceWarps(const GridGPU& g, const FrameGPU& f) {
   int layers = f.layerEnd - f.layerBegin;
-  if (layers <= 0) return cudaSuccess;
+  if (layers <= 0) return 0;
   const int D = 32 / g.warpProbes;
   long long probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
-  long long warps = probeGroups * layers * (g.N / D);
-  long long nblocks = (warps * 32 + kTraceThreads - 1) / kTraceThreads;
-  k_trace_shade<<<(unsigned)nblocks, kTraceThreads, 0, stream>>>(s, g, f, lattice, order, atlasPrev, rayRad, rayDir,
-                                                                 rayHit, err);
+  return probeGroups * layers * (g.N / D);
+}
+
+cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
+                             unsigned long long* dQueue, int blocks, int warpsPerFetch, uint32_t* err,
+                             cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(dQueue, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  dim3 lg((maxN + 127) / 128, numItems);
+  k_lattice_batch<<<lg, 128, 0, stream>>>(dItems, dRots);
+  if (totalWarps > 0)
+    k_trace_batch<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, totalWarps, dQueue, warpsPerFetch, err);
   return cudaGetLastError();
 }
 

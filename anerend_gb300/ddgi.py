@@ -223,3 +223,48 @@ class IrradianceProbeConvolvePass:
 
     def execute(self, grid: ProbeGrid, frame: FrameParams, stream: int = 0) -> None:
         grid.convolve(frame, stream)
+
+
+class Batch:
+    """Many (grid, scene) items updated with one persistent trace launch and one convolution launch
+    (DdgiBatch), replayed from a CUDA graph once the batch's shape repeats."""
+
+    def __init__(self, ctx: Context, items):
+        self.ctx = ctx
+        self.items = list(items)
+        arr = (L.BatchItem * len(self.items))(*[L.BatchItem(g.handle.value, s.handle.value) for g, s in self.items])
+        h = C.c_void_p()
+        ctx.check(ctx.lib.ddgi_batch_create(ctx.handle, arr, len(self.items), C.byref(h)))
+        self.handle = h
+        self._frames = (L.Frame * len(self.items))()
+
+    @property
+    def tuning(self) -> L.BatchTuning:
+        t = L.BatchTuning()
+        self.ctx.check(self.ctx.lib.ddgi_batch_get_tuning(self.handle, C.byref(t)))
+        return t
+
+    def set_tuning(self, **kw) -> None:
+        t = self.tuning
+        names = {"warp_probes": "warpProbes", "ray_order": "rayOrder", "shadow_mode": "shadowMode",
+                 "conv_mode": "convMode", "blocks_per_sm": "blocksPerSm", "warps_per_fetch": "warpsPerFetch",
+                 "use_graph": "useGraph"}
+        for k, v in kw.items():
+            setattr(t, names.get(k, k), int(v))
+        self.ctx.check(self.ctx.lib.ddgi_batch_set_tuning(self.handle, C.byref(t)))
+
+    @property
+    def stats(self) -> L.BatchStats:
+        s = L.BatchStats()
+        self.ctx.check(self.ctx.lib.ddgi_batch_stats(self.handle, C.byref(s)))
+        return s
+
+    def update(self, frames, stream: int = 0) -> None:
+        for i, fp in enumerate(frames):
+            self._frames[i] = fp.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_batch_update(self.handle, self._frames, stream))
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.ddgi_batch_destroy(self.handle)
+            self.handle = None

@@ -212,3 +212,68 @@ def camera(w: Workload, frame: int) -> tuple:
     if w.move_every:
         return (float(frame // w.move_every), 0.0, 0.0)
     return (0.0, 0.0, 0.0)
+
+
+@dataclass
+class GridSpec:
+    dims: tuple
+    rays: int
+    scene: int
+    camera: tuple
+    step: tuple = (1.0, 2.0, 1.0)
+    origin_y: float = 0.0
+    hysteresis: float = 0.97
+
+    @property
+    def probes(self) -> int:
+        return self.dims[0] * self.dims[1] * self.dims[2]
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    num_grids: int
+    num_scenes: int
+    tri_range: tuple
+    dims_choices: tuple
+    rays_choices: tuple
+    box_lo: tuple = (-30, 0, -15)
+    box_hi: tuple = (30, 15, 15)
+    seed: int = 0
+
+
+# Batched form: 64 probe grids of uneven size (each axis from {4, 8, 16, 32}: 64 .. 32,768 probes) with
+# rays/probe from {64, 128, 256, 512}, over 8 resident scenes of 10k .. 1M random triangles (log-uniform).
+BATCHED = BatchWorkload("ddgi_batch_64grids_8scenes", 64, 8, (10_000, 1_000_000), (4, 8, 16, 32),
+                        (64, 128, 256, 512))
+
+
+def batch_layout(bw: BatchWorkload, tri_scale: float = 1.0, max_dim: int | None = None):
+    """(triangle count per scene, GridSpec per grid) of a batched workload, from its seed."""
+    u = uniform(bw.seed, 9000, bw.num_scenes)
+    lo, hi = np.log(bw.tri_range[0]), np.log(bw.tri_range[1])
+    tris = [max(64, int(round(np.exp(lo + (hi - lo) * x) * tri_scale))) for x in u]
+    d = uniform(bw.seed, 9001, 3 * bw.num_grids).reshape(bw.num_grids, 3)
+    r = uniform(bw.seed, 9002, bw.num_grids)
+    sc = uniform(bw.seed, 9003, bw.num_grids)
+    cam = uniform(bw.seed, 9004, 3 * bw.num_grids).reshape(bw.num_grids, 3)
+    lo3, hi3 = np.asarray(bw.box_lo, float), np.asarray(bw.box_hi, float)
+    grids = []
+    for i in range(bw.num_grids):
+        dims = tuple(int(bw.dims_choices[min(int(x * len(bw.dims_choices)), len(bw.dims_choices) - 1)]) for x in d[i])
+        if max_dim:
+            dims = tuple(min(v, max_dim) for v in dims)
+        rays = int(bw.rays_choices[min(int(r[i] * len(bw.rays_choices)), len(bw.rays_choices) - 1)])
+        camera = tuple(float(v) for v in np.round(lo3 + (hi3 - lo3) * cam[i], 3))
+        grids.append(GridSpec(dims, rays, min(int(sc[i] * bw.num_scenes), bw.num_scenes - 1), camera))
+    return tris, grids
+
+
+def build_scene_tris(n: int, seed: int, box_lo=(-30, 0, -15), box_hi=(30, 15, 15), tris_per_mesh: int = 256,
+                     num_materials: int = 1024) -> Scene:
+    """A random-triangle scene of n triangles in a box (the workloads' distributions)."""
+    tris = random_triangles(seed, n, box_lo, box_hi)
+    tri_mesh = np.arange(n) // tris_per_mesh
+    n_mesh = int(tri_mesh.max()) + 1
+    mats = random_materials(seed, min(num_materials, n_mesh))
+    return assemble(tris, tri_mesh, np.arange(n_mesh) % len(mats), mats)

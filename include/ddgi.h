@@ -243,6 +243,46 @@ int  ddgi_atlas_upload(DdgiGrid* grid, const void* host, uint64_t bytes, void* s
  * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
 int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
 
+/* ---- batched form: many grids in one persistent trace launch and one convolution launch ---------------- */
+
+typedef struct DdgiBatch DdgiBatch;
+typedef struct DdgiBatchItem {
+  DdgiGrid*        grid;    /* each grid at most once per batch */
+  const DdgiScene* scene;
+} DdgiBatchItem;
+
+/* Launch shape of a batch (picked by the autotuner, anerend_gb300/autotune.py). No counterpart in the
+ * reference, whose passes run one grid with a fixed launch shape. */
+typedef struct DdgiBatchTuning {
+  int32_t warpProbes;    /* as DdgiTuning.warpProbes, raised per grid to 32/N where needed (default 2) */
+  int32_t rayOrder;      /* as DdgiTuning.rayOrder (default 1) */
+  int32_t shadowMode;    /* as DdgiTuning.shadowMode (default 1) */
+  int32_t convMode;      /* as DdgiTuning.convMode (default 0); tensor-core batches hold at most 64 items */
+  int32_t blocksPerSm;   /* resident 128-thread blocks per SM of the persistent trace (1..8, default 8) */
+  int32_t warpsPerFetch; /* warps of work taken from the shared queue per atomic (1..64, default 4) */
+  int32_t useGraph;      /* capture the launch sequence into a CUDA graph once its shape repeats (default 1) */
+  int32_t reserved;
+} DdgiBatchTuning;
+
+typedef struct DdgiBatchStats {
+  uint64_t rays;           /* primary rays of the last update */
+  uint32_t translations;   /* grids translated by the last update */
+  uint32_t graphLaunches;  /* updates replayed from the captured graph (cumulative) */
+  uint32_t eagerLaunches;  /* updates launched without the graph (cumulative) */
+  uint32_t reserved;
+} DdgiBatchStats;
+
+/* Creates a batch over `n` (grid, scene) items of one context and applies the default tuning to its grids. */
+int  ddgi_batch_create(DdgiContext* ctx, const DdgiBatchItem* items, int n, DdgiBatch** out);
+void ddgi_batch_destroy(DdgiBatch* batch);
+int  ddgi_batch_get_tuning(const DdgiBatch* batch, DdgiBatchTuning* out);
+int  ddgi_batch_set_tuning(DdgiBatch* batch, const DdgiBatchTuning* tuning);
+int  ddgi_batch_stats(const DdgiBatch* batch, DdgiBatchStats* out);
+/* ddgi_update for every item with frames[i] (translate unless baking, trace, convolve), as one persistent
+ * trace launch over all items' rays and one convolution launch, replayed from a CUDA graph once the batch's
+ * shape repeats. Results equal the items' individual ddgi_update calls up to FP32 rounding order. */
+int  ddgi_batch_update(DdgiBatch* batch, const DdgiFrame* frames, void* stream);
+
 /* ---- raw kernels on caller-owned device memory ------------------------------------------------------- */
 
 /* The golden-angle ray set of irradiance_probe_update.rgen:35-46 rotated by mat3(rot) (rgen:87-88),
