@@ -97,6 +97,32 @@ class BatchStats(C.Structure):
                 ("eagerLaunches", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memoryBudget", C.c_uint64), ("maxBatch", C.c_int32), ("inFlight", C.c_int32),
+                ("convMode", C.c_int32), ("reserved", C.c_int32 * 5)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("grid", GridDesc), ("frame", Frame), ("atlasOut", C.c_void_p),
+                ("tag", C.c_uint64)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("submitSeconds", C.c_double),
+                ("admitSeconds", C.c_double), ("doneSeconds", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("failed", C.c_uint64), ("batches", C.c_uint64), ("rays", C.c_uint64), ("peakBytes", C.c_uint64),
+                ("p50LatencyMs", C.c_double), ("p99LatencyMs", C.c_double), ("meanLatencyMs", C.c_double),
+                ("maxLatencyMs", C.c_double), ("elapsedSeconds", C.c_double)]
+
+
+DDGI_REQUEST_QUEUED, DDGI_REQUEST_RUNNING, DDGI_REQUEST_DONE = 0, 1, 2
+DDGI_REQUEST_FAILED, DDGI_REQUEST_REJECTED = -1, -2
+
+
 class GridBuffers(C.Structure):
     _fields_ = [("atlas", C.c_void_p), ("rayRadiance", C.c_void_p), ("rayDirection", C.c_void_p),
                 ("rayHit", C.c_void_p), ("lattice", C.c_void_p),
@@ -119,6 +145,7 @@ SIGNATURES = {
     "ddgi_grid_destroy": (None, [C.c_void_p]),
     "ddgi_grid_buffers": (C.c_int, [C.c_void_p, C.POINTER(GridBuffers)]),
     "ddgi_grid_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ddgi_grid_footprint": (C.c_uint64, [C.POINTER(GridDesc), C.c_int]),
     "ddgi_grid_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ddgi_grid_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "ddgi_translate": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_void_p]),
@@ -134,6 +161,12 @@ SIGNATURES = {
     "ddgi_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
     "ddgi_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "ddgi_batch_update": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p]),
+    "ddgi_server_create": (C.c_int, [C.c_void_p, C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "ddgi_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "ddgi_server_status": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(RequestStatus)]),
+    "ddgi_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+    "ddgi_server_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "ddgi_server_destroy": (None, [C.c_void_p]),
     "ddgi_fibonacci_lattice": (C.c_int, [C.c_int, C.POINTER(C.c_float), C.c_void_p, C.c_void_p]),
     "ddgi_convolve_raw": (C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                     C.c_uint32, C.c_void_p]),

@@ -15,6 +15,18 @@
 namespace ddgi {
 namespace detail {
 
+namespace {
+cudaError_t gridAlloc(DdgiGrid* g, void** p, size_t bytes) {
+  if (g->asyncAlloc) return cudaMallocAsync(p, bytes, g->allocStream);
+  return cudaMalloc(p, bytes);
+}
+void gridFree(DdgiGrid* g, void* p) {
+  if (!p) return;
+  if (g->asyncAlloc) cudaFreeAsync(p, g->allocStream);
+  else cudaFree(p);
+}
+}  // namespace
+
 int fail(DdgiContext* ctx, int code, const char* fmt, ...) {
   if (ctx) {
     char buf[512];
@@ -113,13 +125,17 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
     return fail(ctx, DDGI_EINVAL, "tensor-core convolution needs raysPerProbe %% 64 == 0 (N = %d)", g->g.N);
   if (t.convMode != 0 && !g->rad16) {
     size_t bytes = (size_t)3 * g->g.X * g->g.Y * g->g.Z * g->g.N * 2;
-    CK(cudaMalloc(&g->rad16, bytes), "16-bit radiance buffer");
-    CK(cudaMalloc(&g->tcScratch, tcScratchBytes(g->g.N)), "tensor-core weight scratch");
+    CK(gridAlloc(g, &g->rad16, bytes), "16-bit radiance buffer");
+    CK(gridAlloc(g, &g->tcScratch, tcScratchBytes(g->g.N)), "tensor-core weight scratch");
   }
   std::vector<int> order(g->g.N);
   if (t.rayOrder == 1) order = mortonRayOrder(g->g.N);
   else for (int i = 0; i < g->g.N; ++i) order[i] = i;
-  CK(cudaMemcpy(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice), "ray order upload");
+  if (g->asyncAlloc)  // pageable source: the call returns once the data is staged
+    CK(cudaMemcpyAsync(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, g->allocStream),
+       "ray order upload");
+  else
+    CK(cudaMemcpy(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice), "ray order upload");
   g->tuning = t;
   g->g.warpProbes = t.warpProbes;
   return DDGI_OK;
@@ -250,6 +266,98 @@ int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_
   CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, st), "translate");
   g->cur = 1 - g->cur;
   if (moved) *moved = 1;
+  return DDGI_OK;
+}
+
+
+uint64_t gridFootprint(const DdgiGridDesc* d, int convMode) {
+  GridGPU g = makeGridGPU(*d);
+  uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
+  uint64_t rays = (uint64_t)g.rayW * g.bh * g.Z * g.Y;
+  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + 16 * rays + 16ull * g.N + 4ull * g.N +
+                   4ull * g.N * kOctTexels + 4ull * kOctTexels;
+  if (d->options & DDGI_GRID_WRITE_DIRS) bytes += 16 * rays;
+  if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
+  if (convMode != 0) bytes += 6 * rays + tcScratchBytes(g.N);
+  return bytes;
+}
+
+int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool asyncAlloc, DdgiGrid** out) {
+  *out = nullptr;
+  int rc = validateGridDesc(ctx, desc);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device), "set device");
+  DdgiGrid* g = new (std::nothrow) DdgiGrid();
+  if (!g) return fail(ctx, DDGI_ENOMEM, "host allocation");
+  g->ctx = ctx;
+  g->desc = *desc;
+  g->g = makeGridGPU(*desc);
+  g->asyncAlloc = asyncAlloc;
+  g->allocStream = st;
+  size_t texel = desc->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
+  g->atlasBytes = (uint64_t)g->g.atlasW * g->g.atlasH * texel;
+  g->rayH = g->g.bh * g->g.Z * g->g.Y;
+  size_t rayTexels = (size_t)g->g.rayW * g->rayH;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = gridAlloc(g, &g->atlas[0], g->atlasBytes);
+  if (e == cudaSuccess) e = gridAlloc(g, &g->atlas[1], g->atlasBytes);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->rayRad, 16 * rayTexels);
+  if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = gridAlloc(g, (void**)&g->rayDir, 16 * rayTexels);
+  if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = gridAlloc(g, (void**)&g->rayHit, 4 * rayTexels);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->lattice, 16 * (size_t)g->g.N);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, sizeof(int) * (size_t)g->g.N);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wt, 4 * (size_t)g->g.N * kOctTexels);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wsum, 4 * kOctTexels);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->rayRad, 0, 16 * rayTexels, st);
+  if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], st);
+  if (e == cudaSuccess && !asyncAlloc) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    gridDestroy(g);
+    return cudaFail(ctx, e, "grid allocation");
+  }
+  DdgiTuning t{};
+  t.warpProbes = std::max(1, 32 / g->g.N);
+  t.rayOrder = 1;
+  t.shadowMode = 1;
+  int rc2 = applyTuning(g, t);
+  if (rc2 != DDGI_OK) {
+    gridDestroy(g);
+    return rc2;
+  }
+  *out = g;
+  return DDGI_OK;
+}
+
+void gridDestroy(DdgiGrid* g) {
+  if (!g) return;
+  gridFree(g, g->atlas[0]);
+  gridFree(g, g->atlas[1]);
+  gridFree(g, g->rayRad);
+  gridFree(g, g->rayDir);
+  gridFree(g, g->rayHit);
+  gridFree(g, g->lattice);
+  gridFree(g, g->order);
+  gridFree(g, g->rad16);
+  gridFree(g, g->tcScratch);
+  gridFree(g, g->wt);
+  gridFree(g, g->wsum);
+  cudaFree(g->dTrace);
+  cudaFree(g->dQueue);
+  cudaFree(g->dConv);
+  g->ring.release();
+  delete g;
+}
+
+// Records of the single-grid launches (ddgi_trace / ddgi_convolve), allocated on first use.
+int ensureSoloRecords(DdgiGrid* g) {
+  if (g->dTrace) return DDGI_OK;
+  DdgiContext* ctx = g->ctx;
+  // dTrace is followed by the rotation: one staging copy carries both
+  CK(cudaMalloc(&g->dTrace, sizeof(TraceItem) + sizeof(Mat3)), "trace record");
+  g->dRot = reinterpret_cast<Mat3*>(reinterpret_cast<unsigned char*>(g->dTrace) + sizeof(TraceItem));
+  CK(cudaMalloc(&g->dQueue, sizeof(unsigned long long)), "trace queue");
+  CK(cudaMalloc(&g->dConv, sizeof(ConvItem)), "convolve record");
+  CK(g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem))), "record staging");
   return DDGI_OK;
 }
 
@@ -416,73 +524,14 @@ int ddgi_scene_info(const DdgiScene* s, DdgiSceneInfo* info) {
 // ---- grid -------------------------------------------------------------------------------------------
 int ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out) {
   if (!ctx || !out) return fail(ctx, DDGI_EINVAL, "NULL argument to ddgi_grid_create");
-  *out = nullptr;
-  int rc = validateGridDesc(ctx, desc);
-  if (rc) return rc;
-  CK(cudaSetDevice(ctx->device), "set device");
-  DdgiGrid* g = new (std::nothrow) DdgiGrid();
-  if (!g) return fail(ctx, DDGI_ENOMEM, "host allocation");
-  g->ctx = ctx;
-  g->desc = *desc;
-  g->g = makeGridGPU(*desc);
-  size_t texel = desc->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
-  g->atlasBytes = (uint64_t)g->g.atlasW * g->g.atlasH * texel;
-  g->rayH = g->g.bh * g->g.Z * g->g.Y;
-  size_t rayTexels = (size_t)g->g.rayW * g->rayH;
-  cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&g->atlas[0], g->atlasBytes);
-  if (e == cudaSuccess) e = cudaMalloc(&g->atlas[1], g->atlasBytes);
-  if (e == cudaSuccess) e = cudaMalloc(&g->rayRad, 16 * rayTexels);
-  if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = cudaMalloc(&g->rayDir, 16 * rayTexels);
-  if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = cudaMalloc(&g->rayHit, 4 * rayTexels);
-  if (e == cudaSuccess) e = cudaMalloc(&g->lattice, 16 * (size_t)g->g.N);
-  if (e == cudaSuccess) e = cudaMalloc(&g->order, sizeof(int) * (size_t)g->g.N);
-  // dTrace is followed by the rotation: one staging copy carries both
-  if (e == cudaSuccess) e = cudaMalloc(&g->dTrace, sizeof(TraceItem) + sizeof(Mat3));
-  if (e == cudaSuccess) g->dRot = reinterpret_cast<Mat3*>(reinterpret_cast<unsigned char*>(g->dTrace) + sizeof(TraceItem));
-  if (e == cudaSuccess) e = cudaMalloc(&g->dQueue, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&g->dConv, sizeof(ConvItem));
-  if (e == cudaSuccess) e = g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem)));
-  if (e == cudaSuccess) e = cudaMalloc(&g->wt, 4 * (size_t)g->g.N * kOctTexels);
-  if (e == cudaSuccess) e = cudaMalloc(&g->wsum, 4 * kOctTexels);
-  if (e == cudaSuccess) e = cudaMemset(g->rayRad, 0, 16 * rayTexels);
-  if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], 0);
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) {
-    ddgi_grid_destroy(g);
-    return cudaFail(ctx, e, "grid allocation");
-  }
-  DdgiTuning t{};
-  t.warpProbes = std::max(1, 32 / g->g.N);
-  t.rayOrder = 1;
-  t.shadowMode = 1;
-  int rc2 = applyTuning(g, t);
-  if (rc2 != DDGI_OK) {
-    ddgi_grid_destroy(g);
-    return rc2;
-  }
-  *out = g;
-  return DDGI_OK;
+  return gridCreate(ctx, desc, nullptr, false, out);
 }
 
-void ddgi_grid_destroy(DdgiGrid* g) {
-  if (!g) return;
-  cudaFree(g->atlas[0]);
-  cudaFree(g->atlas[1]);
-  cudaFree(g->rayRad);
-  cudaFree(g->rayDir);
-  cudaFree(g->rayHit);
-  cudaFree(g->lattice);
-  cudaFree(g->order);
-  cudaFree(g->dTrace);
-  cudaFree(g->dQueue);
-  cudaFree(g->dConv);
-  g->ring.release();
-  cudaFree(g->rad16);
-  cudaFree(g->tcScratch);
-  cudaFree(g->wt);
-  cudaFree(g->wsum);
-  delete g;
+void ddgi_grid_destroy(DdgiGrid* g) { gridDestroy(g); }
+
+uint64_t ddgi_grid_footprint(const DdgiGridDesc* desc, int convMode) {
+  if (validateGridDesc(nullptr, desc) != DDGI_OK) return 0;
+  return gridFootprint(desc, convMode);
 }
 
 int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
@@ -557,6 +606,8 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
     gg.pTotal = g->g.X * g->g.Y * g->g.Z;
   }
   // the persistent batched kernels with one item (the same code the batched form runs)
+  rc = ensureSoloRecords(g);
+  if (rc) return rc;
   int slot = 0;
   unsigned char* h = g->ring.acquire(&slot);
   TraceItem& ti = *reinterpret_cast<TraceItem*>(h);
@@ -605,6 +656,8 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
        "tensor-core convolve");
     return DDGI_OK;
   }
+  int rc = ensureSoloRecords(g);
+  if (rc) return rc;
   int slot = 0;
   ConvItem& ci = *reinterpret_cast<ConvItem*>(g->ring.acquire(&slot));
   ci.g = g->g;

@@ -98,7 +98,12 @@ struct DdgiGrid {
   int tracedBegin = 0, tracedEnd = 0;  // the "ProbeLayer" blackboard value, as a range
   bool latticeValid = false;
   bool rad16Written = false;  // the last trace also wrote the 16-bit radiance of its layers
-  // single-item records of the trace and FP32 convolution (the grid runs the batched kernels with one item)
+  // allocation mode: served grids take their memory stream-ordered (cudaMallocAsync / cudaFreeAsync on
+  // allocStream), so creating and freeing them never synchronizes the device
+  bool asyncAlloc = false;
+  cudaStream_t allocStream = nullptr;
+  // single-item records of the trace and FP32 convolution (the grid runs the batched kernels with one item),
+  // allocated on first use
   TraceItem* dTrace = nullptr;
   Mat3* dRot = nullptr;
   unsigned long long* dQueue = nullptr;
@@ -119,6 +124,23 @@ int layerRange(DdgiGrid* grid, int layer, bool advance, int& b, int& e);
 int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st);
 // translation state update of ddgi_translate without the C-ABI argument checks
 int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_t st);
+// Grid construction / destruction; asyncAlloc: stream-ordered memory on `st`, no device synchronization.
+int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool asyncAlloc, DdgiGrid** out);
+void gridDestroy(DdgiGrid* g);
+// Device bytes a grid of this description holds (atlas pair, ray images, lattice and weight tables and, for
+// a tensor-core convolution, the 16-bit radiance and its weight scratch).
+uint64_t gridFootprint(const DdgiGridDesc* d, int convMode);
+// Batched launch of n (grid, scene, frame) items through a reusable launch state (records, staging, graph).
+struct LaunchState;
+LaunchState* launchStateCreate(DdgiContext* ctx);
+void launchStateDestroy(LaunchState* s);
+int launchStateReserve(LaunchState* s, int n);
+int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, DdgiGrid* const* grids,
+                DdgiScene* const* scenes, const DdgiFrame* frames, int n, cudaStream_t st, bool allowGraph,
+                DdgiBatchStats* stats);
+int checkBatchTuning(DdgiContext* ctx, const DdgiBatchTuning& t);
+int tuneGridForBatch(DdgiGrid* g, const DdgiBatchTuning& t);
+DdgiBatchTuning defaultBatchTuning();
 
 }  // namespace detail
 }  // namespace ddgi

@@ -268,3 +268,63 @@ class Batch:
         if self.handle:
             self.ctx.lib.ddgi_batch_destroy(self.handle)
             self.handle = None
+
+
+def grid_desc(dims, step=(1.0, 2.0, 1.0), rays_per_probe: int = 256, origin_y: float = 0.0,
+              hysteresis: float = 0.96, atlas_format: int = L.DDGI_FORMAT_RGBA32F, options: int = 0) -> L.GridDesc:
+    d = L.GridDesc()
+    d.dims[:] = list(dims)
+    d.step[:] = list(step)
+    d.originY = origin_y
+    d.raysPerProbe = rays_per_probe
+    d.atlasFormat = atlas_format
+    d.hysteresis = hysteresis
+    d.options = options
+    return d
+
+
+class Server:
+    """Serving loop (DdgiServer): requests are admitted under a device-memory budget and launched in
+    batches, up to `in_flight` launches overlapping on the device."""
+
+    def __init__(self, ctx: Context, memory_budget: int, max_batch: int = 64, in_flight: int = 2,
+                 conv_mode: int = 0):
+        self.ctx = ctx
+        cfg = L.ServerConfig()
+        cfg.memoryBudget = int(memory_budget)
+        cfg.maxBatch = max_batch
+        cfg.inFlight = in_flight
+        cfg.convMode = conv_mode
+        h = C.c_void_p()
+        ctx.check(ctx.lib.ddgi_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h
+
+    def submit(self, scene: Scene, desc: L.GridDesc, frame: FrameParams, atlas_out: int = 0, tag: int = 0) -> int:
+        r = L.Request()
+        r.scene = scene.handle.value
+        r.grid = desc
+        r.frame = frame.to_c()
+        r.atlasOut = atlas_out
+        r.tag = tag
+        rid = C.c_uint64(0)
+        self.ctx.check(self.ctx.lib.ddgi_server_submit(self.handle, C.byref(r), C.byref(rid)))
+        return rid.value
+
+    def status(self, rid: int) -> L.RequestStatus:
+        s = L.RequestStatus()
+        self.ctx.check(self.ctx.lib.ddgi_server_status(self.handle, rid, C.byref(s)))
+        return s
+
+    def drain(self, timeout: float = 60.0) -> None:
+        self.ctx.check(self.ctx.lib.ddgi_server_drain(self.handle, timeout))
+
+    @property
+    def stats(self) -> L.ServerStats:
+        s = L.ServerStats()
+        self.ctx.check(self.ctx.lib.ddgi_server_stats(self.handle, C.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.ddgi_server_destroy(self.handle)
+            self.handle = None

@@ -277,3 +277,41 @@ def build_scene_tris(n: int, seed: int, box_lo=(-30, 0, -15), box_hi=(30, 15, 15
     n_mesh = int(tri_mesh.max()) + 1
     mats = random_materials(seed, min(num_materials, n_mesh))
     return assemble(tris, tri_mesh, np.arange(n_mesh) % len(mats), mats)
+
+
+@dataclass
+class ServingWorkload:
+    name: str
+    num_scenes: int
+    tri_range: tuple
+    rate: float            # requests per second (Poisson)
+    probe_range: tuple     # log-uniform probes per request
+    rays_choices: tuple
+    budget: int            # device bytes of admitted request grids
+    seed: int = 0
+
+
+# Serving form: 32 resident scenes of 10k .. 1M triangles, Poisson arrivals at 2,000 probe-update requests/s,
+# each a grid of 256 .. 65,536 probes (log-uniform) with 64 .. 512 rays/probe, admitted under a 150 GB budget.
+SERVING = ServingWorkload("ddgi_serving_32scenes_2000rps", 32, (10_000, 1_000_000), 2000.0, (256, 65536),
+                          (64, 128, 256, 512), 150 << 30)
+
+
+def serving_requests(sw: ServingWorkload, count: int, rate: float | None = None):
+    """`count` requests: (arrival time s, scene index, dims, rays, camera, rotation frame)."""
+    rate = rate or sw.rate
+    gaps = -np.log(1.0 - uniform(sw.seed, 9100, count)) / rate
+    t = np.cumsum(gaps)
+    lp = np.log2(sw.probe_range[0]) + (np.log2(sw.probe_range[1]) - np.log2(sw.probe_range[0])) * uniform(sw.seed, 9101, count)
+    sc = uniform(sw.seed, 9102, count)
+    rr = uniform(sw.seed, 9103, count)
+    cam = uniform(sw.seed, 9104, 3 * count).reshape(count, 3)
+    out = []
+    for i in range(count):
+        k = int(round(lp[i]))
+        ax, rem = k // 3, k % 3
+        dims = (1 << (ax + (rem >= 1)), 1 << ax, 1 << (ax + (rem >= 2)))
+        rays = int(sw.rays_choices[min(int(rr[i] * len(sw.rays_choices)), len(sw.rays_choices) - 1)])
+        camera = tuple(float(v) for v in np.round(np.array([-30, 0, -15]) + np.array([60, 15, 30]) * cam[i], 3))
+        out.append((float(t[i]), min(int(sc[i] * sw.num_scenes), sw.num_scenes - 1), dims, rays, camera, i))
+    return out

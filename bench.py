@@ -291,7 +291,7 @@ def run_ours(args, rank, local, world):
     alg_bytes = rays_per_step * (hit_frac * BYTES_PER_HIT + (1 - hit_frac) * BYTES_PER_MISS)
     achieved = alg_bytes / trace_avg_s / 1e9
     traffic = None
-    tp = ROOT / "profiles" / "trace_shade_traffic.json"
+    tp = ROOT / "profiles" / "trace_traffic.json"
     if tp.exists():
         traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
     cpu = None
@@ -318,7 +318,7 @@ def run_ours(args, rank, local, world):
             "wall_s": wall,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 116,
                     "d2h_bytes_per_step": int(grid.buffers.atlasBytes)},
-            "roofline": {"kernel": "k_trace_shade", "bound": "hbm", "achieved": achieved,
+            "roofline": {"kernel": "k_trace_batch", "bound": "hbm", "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "traffic": traffic, "peak_source": peaks["source"],
                          "algorithmic_bytes_per_launch": alg_bytes},

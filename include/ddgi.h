@@ -209,6 +209,8 @@ void ddgi_grid_destroy(DdgiGrid* grid);
 int  ddgi_grid_buffers(const DdgiGrid* grid, DdgiGridBuffers* out);
 /* Clears the atlas to (0,0,0,1) and the translation state to (0,0). */
 int  ddgi_grid_reset(DdgiGrid* grid, void* stream);
+/* Device bytes a grid of this description holds with the given DdgiTuning.convMode (0 for an invalid desc). */
+uint64_t ddgi_grid_footprint(const DdgiGridDesc* desc, int convMode);
 /* Reads / sets the grid's launch shape (results do not depend on it). */
 int  ddgi_grid_get_tuning(const DdgiGrid* grid, DdgiTuning* out);
 int  ddgi_grid_set_tuning(DdgiGrid* grid, const DdgiTuning* tuning);
@@ -282,6 +284,58 @@ int  ddgi_batch_stats(const DdgiBatch* batch, DdgiBatchStats* out);
  * trace launch over all items' rays and one convolution launch, replayed from a CUDA graph once the batch's
  * shape repeats. Results equal the items' individual ddgi_update calls up to FP32 rounding order. */
 int  ddgi_batch_update(DdgiBatch* batch, const DdgiFrame* frames, void* stream);
+
+/* ---- serving: continuous batching of probe-update requests ------------------------------------------------ */
+
+typedef struct DdgiServer DdgiServer;
+
+typedef struct DdgiServerConfig {
+  uint64_t memoryBudget;  /* device bytes of request grids admitted at once (ddgi_grid_footprint) */
+  int32_t  maxBatch;      /* requests per launch (1..64) */
+  int32_t  inFlight;      /* launches running at once, each on its own stream (1..4) */
+  int32_t  convMode;      /* DdgiTuning.convMode of the served grids */
+  int32_t  reserved[5];
+} DdgiServerConfig;
+
+/* One probe update of a grid of its own over a resident scene. The grid starts cleared, is translated,
+ * traced and convolved once, and its atlas is copied to atlasOut (pinned host memory of the grid's
+ * atlasBytes; NULL discards it) before the request completes. */
+typedef struct DdgiRequest {
+  const DdgiScene* scene;
+  DdgiGridDesc     grid;
+  DdgiFrame        frame;
+  void*            atlasOut;
+  uint64_t         tag;
+} DdgiRequest;
+
+#define DDGI_REQUEST_QUEUED    0
+#define DDGI_REQUEST_RUNNING   1
+#define DDGI_REQUEST_DONE      2
+#define DDGI_REQUEST_FAILED   -1
+#define DDGI_REQUEST_REJECTED -2
+
+typedef struct DdgiRequestStatus {
+  int32_t state;          /* DDGI_REQUEST_* */
+  int32_t error;          /* status code of a failed or rejected request */
+  double  submitSeconds, admitSeconds, doneSeconds;  /* server clock */
+} DdgiRequestStatus;
+
+typedef struct DdgiServerStats {
+  uint64_t submitted, completed, rejected, failed, batches, rays, peakBytes;
+  double   p50LatencyMs, p99LatencyMs, meanLatencyMs, maxLatencyMs, elapsedSeconds;
+} DdgiServerStats;
+
+/* Starts the serving loop's worker thread. No counterpart in the reference, which updates one grid per
+ * frame inside its render loop. */
+int  ddgi_server_create(DdgiContext* ctx, const DdgiServerConfig* cfg, DdgiServer** out);
+/* Queues a request (thread-safe, non-blocking). DDGI_EBUSY when it alone exceeds the memory budget. */
+int  ddgi_server_submit(DdgiServer* server, const DdgiRequest* request, uint64_t* id);
+int  ddgi_server_status(DdgiServer* server, uint64_t id, DdgiRequestStatus* out);
+/* Waits until every submitted request has finished; DDGI_ETIMEDOUT after timeoutSeconds. */
+int  ddgi_server_drain(DdgiServer* server, double timeoutSeconds);
+int  ddgi_server_stats(DdgiServer* server, DdgiServerStats* out);
+/* Stops the worker (queued requests fail with DDGI_EBUSY), waits for running launches, frees everything. */
+void ddgi_server_destroy(DdgiServer* server);
 
 /* ---- raw kernels on caller-owned device memory ------------------------------------------------------- */
 

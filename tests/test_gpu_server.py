@@ -1,0 +1,90 @@
+"""Serving loop: continuous batching with overlapping launches. Each request's atlas must be the same when it
+is served alone and when it is served in a mix with others (bit-identical: every ray and every probe runs the
+same code in both cases), admission must respect the memory budget, and oversize requests are refused."""
+import numpy as np
+import pytest
+
+from anerend_gb300 import _lib as L
+from anerend_gb300 import ddgi, scenes
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+REQS = [((4, 2, 4), 64, 0), ((8, 4, 8), 128, 1), ((4, 4, 8), 256, 0), ((16, 2, 8), 64, 1), ((8, 8, 4), 512, 0),
+        ((8, 2, 16), 128, 1), ((4, 2, 4), 256, 1), ((16, 4, 16), 64, 0)]
+
+
+def _scenes(ctx):
+    arrays = [scenes.build_scene_tris(n, 70 + i, (-12, 0, -12), (12, 8, 12)) for i, n in enumerate((15000, 6000))]
+    return [ddgi.Scene(ctx, a) for a in arrays]
+
+
+def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30):
+    srv = ddgi.Server(ctx, budget, max_batch=max_batch, in_flight=in_flight, conv_mode=conv_mode)
+    outs, ids = [], []
+    try:
+        for i, (dims, n, si) in enumerate(REQS):
+            d = ddgi.grid_desc(dims, rays_per_probe=n, hysteresis=0.97)
+            nbytes = 10 * dims[0] * 10 * dims[2] * dims[1] * 16
+            out = torch.empty(nbytes // 4, dtype=torch.float32).pin_memory()
+            fp = ddgi.FrameParams(camera_pos=(0.3 * i, 1.0, -0.2 * i), rotation=scenes.rotation(i, 0))
+            ids.append(srv.submit(scs[si], d, fp, out.data_ptr(), tag=i))
+            outs.append(out)
+        srv.drain(120.0)
+        for rid in ids:
+            assert srv.status(rid).state == L.DDGI_REQUEST_DONE
+        st = srv.stats
+        assert st.completed == len(REQS) and st.failed == 0 and st.rejected == 0
+        assert st.peakBytes <= budget
+        ctx.sync()
+        return [o.numpy().copy() for o in outs], st
+    finally:
+        srv.close()
+
+
+@pytest.mark.parametrize("conv_mode", [0, 1])
+def test_request_alone_equals_in_the_mix(ctx, conv_mode):
+    scs = _scenes(ctx)
+    try:
+        alone, st1 = _serve(ctx, scs, max_batch=1, in_flight=1, conv_mode=conv_mode)
+        mixed, st2 = _serve(ctx, scs, max_batch=64, in_flight=2, conv_mode=conv_mode)
+        assert st1.batches == len(REQS)
+        assert st2.batches < len(REQS)  # requests shared launches
+        for i, (a, b) in enumerate(zip(alone, mixed)):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), i
+        # and equal to a grid updated through ddgi_update
+        dims, n, si = REQS[3]
+        g = ddgi.ProbeGrid(ctx, dims, (1.0, 2.0, 1.0), n, 0.0, 0.97)
+        g.set_tuning(warp_probes=2, conv_mode=conv_mode)
+        g.update(scs[si], ddgi.FrameParams(camera_pos=(0.9, 1.0, -0.6), rotation=scenes.rotation(3, 0)))
+        ctx.sync()
+        assert np.array_equal(g.download_atlas().reshape(-1).view(np.uint32), alone[3].view(np.uint32))
+        g.close()
+    finally:
+        for s in scs:
+            s.close()
+
+
+def test_budget_admission_and_rejection(ctx):
+    scs = _scenes(ctx)
+    try:
+        d = ddgi.grid_desc((8, 4, 8), rays_per_probe=128)
+        need = L.load().ddgi_grid_footprint(d, 0)
+        srv = ddgi.Server(ctx, 2 * need + need // 2, max_batch=64, in_flight=2)  # room for two at a time
+        try:
+            ids = [srv.submit(scs[0], d, ddgi.FrameParams(rotation=scenes.rotation(k, 1))) for k in range(6)]
+            big = ddgi.grid_desc((32, 8, 32), rays_per_probe=512)
+            with pytest.raises(L.DdgiError) as e:
+                srv.submit(scs[0], big, ddgi.FrameParams())
+            assert e.value.code == L.DDGI_EBUSY
+            srv.drain(120.0)
+            st = srv.stats
+            assert st.completed == 6 and st.rejected == 1
+            assert st.peakBytes <= 2 * need + need // 2
+            assert all(srv.status(i).state == L.DDGI_REQUEST_DONE for i in ids)
+        finally:
+            srv.close()
+    finally:
+        for s in scs:
+            s.close()
