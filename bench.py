@@ -203,6 +203,181 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def _time_updates(torch, fn, frames, reps):
+    """Median CUDA-event time (ms) of fn(frame) over reps frames after 2 warm-up calls."""
+    for f in range(2):
+        fn(frames(f))
+    torch.cuda.synchronize()
+    ts = []
+    for f in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        fr = frames(f + 2)
+        e0.record()
+        fn(fr)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def measure_precision(ctx, stream):
+    """Tensor-core and FP32 convolution of the 65,536-probe / 512-ray precision workload (radiance
+    log-uniform in [1e-3, 1e2], seeded, generated on the device)."""
+    import ctypes as C
+
+    import torch
+
+    from anerend_gb300 import _lib as L
+    from anerend_gb300 import ddgi, scenes
+
+    lib = L.load()
+    # precision workload: 64x16x64 probes, 512 rays, radiance log-uniform in [1e-3, 1e2] (seeded, on device)
+    dims, n = (64, 16, 64), 512
+    d = ddgi.grid_desc(dims, rays_per_probe=n, hysteresis=0.97)
+    P = dims[0] * dims[1] * dims[2]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(0)
+    R32 = torch.exp(torch.empty((3, P, n), device="cuda").uniform_(np.log(1e-3), np.log(1e2), generator=gen))
+    dirs = torch.empty(n * 4, dtype=torch.float32, device="cuda")
+    lib.ddgi_fibonacci_lattice(n, (C.c_float * 9)(*scenes.rotation(0, 0).tolist()), dirs.data_ptr(), stream)
+    atlas = torch.rand((10 * dims[2] * dims[1], 10 * dims[0], 4), device="cuda", generator=gen)
+    prec = {"probes": P, "rays_per_probe": n, "algorithmic_bytes": P * (6 * n + 2048)}
+    for name, fmt, dt in (("fp16", L.DDGI_ELEM_F16, torch.float16), ("bf16", L.DDGI_ELEM_BF16, torch.bfloat16)):
+        r16 = R32.to(dt).contiguous()
+
+        def tc(_fr, r16=r16, fmt=fmt):
+            ctx.check(lib.ddgi_convolve_tc_raw(ctx.handle, C.byref(d), r16.data_ptr(), fmt, dirs.data_ptr(),
+                                               atlas.data_ptr(), 0, dims[1], 0, stream))
+
+        ms = _time_updates(torch, tc, lambda f: None, 10)
+        prec[f"tc_{name}_ms"] = ms
+        prec[f"tc_{name}_gbs"] = prec["algorithmic_bytes"] / ms / 1e6
+        del r16
+    bw, bh = 32, 16
+    img = torch.ones((bh * dims[2] * dims[1], bw * dims[0], 4), device="cuda")
+    p = torch.arange(P, device="cuda")
+    j = torch.arange(n, device="cuda")
+    rows = (p // dims[0])[:, None] * bh + (j // bw)[None, :]
+    cols = (p % dims[0])[:, None] * bw + (j % bw)[None, :]
+    for c in range(3):
+        img[rows, cols, c] = R32[c]
+    del R32, rows, cols
+
+    def fp32(_fr):
+        assert lib.ddgi_convolve_raw(C.byref(d), img.data_ptr(), dirs.data_ptr(), atlas.data_ptr(), 0, dims[1], 0,
+                                     stream) == 0
+
+    prec["fp32_cuda_core_ms"] = _time_updates(torch, fp32, lambda f: None, 5)
+    prec["tc_fp16_speedup_vs_fp32"] = prec["fp32_cuda_core_ms"] / prec["tc_fp16_ms"]
+    prec["error_bounds"] = "fp16 <= 1e-3, bf16 <= 1e-2 max relative vs FP64 (tests/test_gpu_tc_conv.py)"
+    del img, atlas
+    torch.cuda.empty_cache()
+    return prec
+
+
+
+def measure_forms(ctx, scene, w, stream, only=None):
+    """The other forms of the path, each bounded to a few seconds: the plain single-grid FP32 form and the
+    tensor-core convolution on the same workload, the tensor-core convolution of the 65,536-probe / 512-ray
+    precision workload, the 64-grid batched workload against its plain form, and a short serving run."""
+    import ctypes as C
+
+    import torch
+
+    from anerend_gb300 import _lib as L
+    from anerend_gb300 import ddgi, scenes
+
+    lib = L.load()
+    out = {}
+    if only == "precision":
+        return {"precision_tc": measure_precision(ctx, stream)}
+    rays = w.probes * w.rays
+    g = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
+
+    def single(fr):
+        g.update(scene, fr, stream)
+
+    def frames1(f):
+        return ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f))
+
+    for name, tun in (("plain_fp32", dict(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0)),
+                      ("tuned_fp32", dict(shadow_mode=1, ray_order=1, warp_probes=2, conv_mode=0)),
+                      ("tuned_tc_bf16", dict(shadow_mode=1, ray_order=1, warp_probes=2, conv_mode=2))):
+        g.set_tuning(**tun)
+        ms = _time_updates(torch, single, frames1, 5)
+        out[f"single_grid_{name}"] = {"ms_per_update": ms, "rays_per_s": rays / ms * 1e3}
+    g.close()
+    out["single_grid_speedup_vs_plain"] = (out["single_grid_plain_fp32"]["ms_per_update"]
+                                           / out["single_grid_tuned_fp32"]["ms_per_update"])
+
+    out["precision_tc"] = measure_precision(ctx, stream)
+
+    # batched workload: 64 grids over 8 scenes, batched tensor-core form vs plain one-grid-at-a-time form
+    bwl = scenes.BATCHED
+    tris, specs = scenes.batch_layout(bwl)
+    scs = [ddgi.Scene(ctx, scenes.build_scene_tris(t, 1000 + i, bwl.box_lo, bwl.box_hi)) for i, t in enumerate(tris)]
+    grids = [ddgi.ProbeGrid(ctx, sp.dims, sp.step, sp.rays, sp.origin_y, sp.hysteresis) for sp in specs]
+    items = [(gg, scs[sp.scene]) for gg, sp in zip(grids, specs)]
+    brays = sum(sp.probes * sp.rays for sp in specs)
+
+    def bframes(f):
+        return [ddgi.FrameParams(camera_pos=sp.camera, rotation=scenes.rotation(i, f)) for i, sp in enumerate(specs)]
+
+    for gg in grids:
+        gg.set_tuning(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0)
+
+    def plain(fr):
+        for (gg, sc), fp in zip(items, fr):
+            gg.update(sc, fp, stream)
+
+    plain_ms = _time_updates(torch, plain, bframes, 3)
+    batch = ddgi.Batch(ctx, items)
+    res_b = {"grids": len(specs), "scenes": len(tris), "triangles": sum(tris), "rays": brays,
+             "plain_fp32_ms": plain_ms, "plain_fp32_rays_per_s": brays / plain_ms * 1e3}
+    for name, conv in (("batched_fp32", 0), ("batched_tc_bf16", 2)):
+        batch.set_tuning(conv_mode=conv, blocks_per_sm=8, warps_per_fetch=4, warp_probes=2, ray_order=1,
+                         shadow_mode=1, use_graph=1)
+        ms = _time_updates(torch, lambda fr: batch.update(fr, stream), bframes, 4)
+        res_b[f"{name}_ms"] = ms
+        res_b[f"{name}_rays_per_s"] = brays / ms * 1e3
+        res_b[f"{name}_probe_updates_per_s"] = sum(sp.probes for sp in specs) / ms * 1e3
+    res_b["speedup_batched_tc_vs_plain"] = plain_ms / res_b["batched_tc_bf16_ms"]
+    res_b["graph_launches"] = int(batch.stats.graphLaunches)
+    out["batched"] = res_b
+    batch.close()
+    for gg in grids:
+        gg.close()
+
+    # serving: Poisson arrivals over the 8 resident scenes above, at the workload's 2,000 req/s and at 200 req/s
+    sw = scenes.SERVING
+    serv = {"scenes": len(scs), "note": "resident scenes of the batched workload (8, 17k..495k triangles)"}
+    for rate, dur in ((2000.0, 1.5), (200.0, 2.0)):
+        reqs = scenes.serving_requests(sw, int(rate * dur), rate)
+        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=2)
+        t0 = time.perf_counter()
+        for (ta, si, dms, rr, cam, k) in reqs:
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            srv.submit(scs[si % len(scs)], ddgi.grid_desc(dms, rays_per_probe=rr, hysteresis=0.97),
+                       ddgi.FrameParams(camera_pos=cam, rotation=scenes.rotation(k, 0)))
+        srv.drain(600.0)
+        wall = time.perf_counter() - t0
+        st = srv.stats
+        offered = sum(int(np.prod(dm)) * rr for (_, _, dm, rr, _, _) in reqs)
+        serv[f"rate_{int(rate)}"] = {"requests": len(reqs), "completed": int(st.completed), "batches": int(st.batches),
+                                     "offered_rays_per_s": offered / max(reqs[-1][0], 1e-9),
+                                     "served_rays_per_s": st.rays / wall, "p50_ms": st.p50LatencyMs,
+                                     "p99_ms": st.p99LatencyMs, "peak_gb": st.peakBytes / 2**30}
+        srv.close()
+    out["serving"] = serv
+    for sc in scs:
+        sc.close()
+    ctx.sync(stream)
+    return out
+
+
 def run_ours(args, rank, local, world):
     import torch
 
@@ -226,6 +401,7 @@ def run_ours(args, rank, local, world):
     probe_grid.close()
 
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
+    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0)  # FP32 throughout
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     rays_per_step = w.probes * w.rays
 
@@ -290,16 +466,23 @@ def run_ours(args, rank, local, world):
     trace_avg_s = sum(trace_ms) / len(trace_ms) / 1e3
     alg_bytes = rays_per_step * (hit_frac * BYTES_PER_HIT + (1 - hit_frac) * BYTES_PER_MISS)
     achieved = alg_bytes / trace_avg_s / 1e9
+    # DRAM bytes of one trace launch, from the ncu capture summarised beside the profile (same workload)
     traffic = None
-    tp = ROOT / "profiles" / "trace_traffic.json"
+    tp = ROOT / "profiles" / "k_trace_batch_single_grid.md"
     if tp.exists():
-        traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
+        import re
+
+        m = re.search(r"^traffic_bytes_per_launch:\s*(\d+)", tp.read_text(), re.M)
+        traffic = int(m.group(1)) if m else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         frames = 4
         v, dt, cores = cpu_sample(w, arrays, frames)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{frames} full probe updates ({frames * rays_per_step} rays), FP64 oracle, {dt:.1f} s"}
+    forms = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        forms = measure_forms(ctx, scene, w, stream)
     if rank == 0:
         srt = sorted(step_ms)
         line = {
@@ -325,6 +508,9 @@ def run_ours(args, rank, local, world):
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clocks,
+            "tuning": {"warpProbes": int(grid.tuning.warpProbes), "rayOrder": int(grid.tuning.rayOrder),
+                       "shadowMode": int(grid.tuning.shadowMode), "convMode": int(grid.tuning.convMode)},
+            "forms": forms,
         }
         print(json.dumps(line))
     grid.close()
@@ -339,6 +525,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the other forms (batched, precision, serving)")
+    ap.add_argument("--form", choices=["precision"], help="run only this form and print its measurements")
     args = ap.parse_args()
     rank, local, world = dist_init()
     if args.impl == "reference":
@@ -349,7 +537,16 @@ def main():
         if rank == 0:
             build.build()
         barrier(world)
-        run_ours(args, rank, local, world)
+        if args.form:
+            import torch
+
+            from anerend_gb300 import ddgi
+
+            torch.cuda.set_device(local)
+            with ddgi.Context(local) as ctx:
+                print(json.dumps(measure_forms(ctx, None, None, torch.cuda.current_stream().cuda_stream, args.form)))
+        else:
+            run_ours(args, rank, local, world)
     if world > 1:
         import torch.distributed as dist
 
