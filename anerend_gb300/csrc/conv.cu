@@ -140,75 +140,142 @@ __global__ void __launch_bounds__(256) k_conv_weights_batch(const ConvItem* __re
   if (threadIdx.x == 0) it.wsum[t] = part[0];
 }
 
-// Each block takes a contiguous range of probe groups (4 probes x 64 texels), so a block mostly stays
-// inside one item; the item's N x 64 weight table is read through L1.
-__global__ void __launch_bounds__(kConvThreads) k_conv_fp32_batch(const ConvItem* __restrict__ items, int numItems,
-                                                                  long long totalGroups) {
-  const int t = threadIdx.x % kOctTexels;
-  const int q = threadIdx.x / kOctTexels;
-  long long per = (totalGroups + gridDim.x - 1) / gridDim.x;
-  long long g0 = (long long)blockIdx.x * per, g1 = min(totalGroups, g0 + per);
-  for (long long grp = g0; grp < g1; ++grp) {
+// Many grids in one launch. The unit of work is a tile of 32 probes of one item (kTileProbes); a block of
+// 128 threads computes the 32 x 64 (probe, texel) block of a tile with a 4-probe x 4-texel register tile per
+// thread, so one shared-memory float4 of weights and four float4s of radiance feed 48 FMAs. The rays are
+// walked in chunks of 16: the next chunk's radiance and weights are fetched into registers while the current
+// chunk is consumed from shared memory. Every (probe, texel) sum runs over j in order with fmaf, as the
+// single-grid kernel does.
+constexpr int kTileProbes = 32;
+constexpr int kTileThreads = 128;
+constexpr int kChunk = 16;  // rays per chunk (the smallest raysPerProbe)
+constexpr int kRStride = kChunk + 1;  // padded probe stride of the radiance chunk (bank spread)
+constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;          // 4 float4 per thread
+constexpr int kWLoads = kChunk * kOctTexels / 4 / kTileThreads;       // 2 float4 per thread
+
+__global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvItem* __restrict__ items, int numItems,
+                                                                  long long totalTiles) {
+  __shared__ float4 sR[kTileProbes * kRStride];
+  __shared__ float4 sW[kChunk * kOctTexels / 4];
+  const int tg = threadIdx.x & 15;  // texels 4tg .. 4tg+3
+  const int pg = threadIdx.x >> 4;  // probes 4pg .. 4pg+3 of the tile
+  for (long long tile = blockIdx.x; tile < totalTiles; tile += gridDim.x) {
     int lo = 0, hi = numItems - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
-      if (items[mid].groupBegin <= grp) lo = mid; else hi = mid - 1;
+      if (items[mid].groupBegin <= tile) lo = mid; else hi = mid - 1;
     }
     const ConvItem& it = items[lo];
     const GridGPU& g = it.g;
     const int probesPerLayer = g.X * g.Z;
-    long long pl = (grp - it.groupBegin) * kConvProbes + q;
-    long long total = (long long)(it.layerEnd - it.layerBegin) * probesPerLayer;
-    if (pl >= total) continue;
-    int layer = it.layerBegin + (int)(pl / probesPerLayer);
-    int p = (int)(pl % probesPerLayer);
-    int px = p % g.X, pz = p / g.X;
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    const float* W = it.wt;
-    for (int j = 0; j < g.N; ++j) {
-      int rx = px * g.bw + (j % g.bw);
-      int ry = (layer * g.Z + pz) * g.bh + (j / g.bw);
-      float4 L = __ldg(&it.rayRad[(size_t)ry * g.rayW + rx]);
-      float w = __ldg(&W[j * kOctTexels + t]);
-      ax = fmaf(w, L.x, ax);
-      ay = fmaf(w, L.y, ay);
-      az = fmaf(w, L.z, az);
+    const long long total = (long long)(it.layerEnd - it.layerBegin) * probesPerLayer;
+    const long long base = (tile - it.groupBegin) * kTileProbes;
+    const int N = g.N;
+    // this thread stages ray (j0 + tg) of probes pg + 8k of the tile (k < kRLoads)
+    const float4* rsrc[kRLoads];
+#pragma unroll
+    for (int k = 0; k < kRLoads; ++k) {
+      long long pl = base + pg + 8 * k;
+      rsrc[k] = nullptr;
+      if (pl < total) {
+        int layer = it.layerBegin + (int)(pl / probesPerLayer);
+        int p = (int)(pl % probesPerLayer);
+        int px = p % g.X, pz = p / g.X;
+        rsrc[k] = it.rayRad + (size_t)((layer * g.Z + pz) * g.bh) * g.rayW + (size_t)px * g.bw;
+      }
     }
-    const float ws = __ldg(&it.wsum[t]);
-    int tx = t % kOct, ty = t / kOct;
-    size_t ai = (size_t)(kProbePix * (layer * g.Z + pz) + 1 + ty) * g.atlasW + (kProbePix * px + 1 + tx);
-    float4 old = loadTexel(it.atlas, g.atlasFmt, ai);
-    float4 out;
-    if (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) {
-      float tw = old.w + ws;
-      float3 tot = f3(ax, ay, az) + xyz(old) * old.w;
-      if (tw > 1e-6f) tot = tot / tw;
-      out = make_float4(tot.x, tot.y, tot.z, tw);
-    } else {
-      float3 res = f3(ax, ay, az);
-      if (ws > 1e-6f) res = res / ws;
-      float h = it.hysteresis, a = 1.0f - h;
-      out = make_float4(res.x * a + old.x * h, res.y * a + old.y * h, res.z * a + old.z * h, ws * a + old.w * h);
+    const float4* W4 = reinterpret_cast<const float4*>(it.wt);
+    float4 rn[kRLoads], wn[kWLoads];
+    auto fetch = [&](int j0) {
+      const int j = j0 + tg;
+      const size_t off = (size_t)(j / g.bw) * g.rayW + (j % g.bw);
+#pragma unroll
+      for (int k = 0; k < kRLoads; ++k) rn[k] = rsrc[k] ? __ldg(rsrc[k] + off) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < kWLoads; ++k) wn[k] = __ldg(W4 + (size_t)j0 * (kOctTexels / 4) + threadIdx.x + k * kTileThreads);
+    };
+    float acc[4][4][3];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = acc[a][b][2] = 0.0f;
+    fetch(0);
+    for (int j0 = 0; j0 < N; j0 += kChunk) {
+      __syncthreads();  // the previous chunk is consumed
+#pragma unroll
+      for (int k = 0; k < kRLoads; ++k) sR[(pg + 8 * k) * kRStride + tg] = rn[k];
+#pragma unroll
+      for (int k = 0; k < kWLoads; ++k) sW[threadIdx.x + k * kTileThreads] = wn[k];
+      __syncthreads();
+      if (j0 + kChunk < N) fetch(j0 + kChunk);
+#pragma unroll 4
+      for (int jj = 0; jj < kChunk; ++jj) {
+        float4 w = sW[jj * (kOctTexels / 4) + tg];
+        float wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          float4 L = sR[(4 * pg + a) * kRStride + jj];
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            acc[a][b][0] = fmaf(wv[b], L.x, acc[a][b][0]);
+            acc[a][b][1] = fmaf(wv[b], L.y, acc[a][b][1]);
+            acc[a][b][2] = fmaf(wv[b], L.z, acc[a][b][2]);
+          }
+        }
+      }
     }
-    storeTexel(it.atlas, g.atlasFmt, ai, out);
+    const bool bake = (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
+    const float h = it.hysteresis, ha = 1.0f - h;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      long long pl = base + 4 * pg + a;
+      if (pl >= total) break;
+      int layer = it.layerBegin + (int)(pl / probesPerLayer);
+      int p = (int)(pl % probesPerLayer);
+      int px = p % g.X, pz = p / g.X;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int t = 4 * tg + b;
+        const float ws = __ldg(&it.wsum[t]);
+        int tx = t % kOct, ty = t / kOct;
+        size_t ai = (size_t)(kProbePix * (layer * g.Z + pz) + 1 + ty) * g.atlasW + (kProbePix * px + 1 + tx);
+        float4 old = loadTexel(it.atlas, g.atlasFmt, ai);
+        float4 out;
+        if (bake) {
+          // probe_conv.comp:307-319
+          float tw = old.w + ws;
+          float3 tot = f3(acc[a][b][0], acc[a][b][1], acc[a][b][2]) + xyz(old) * old.w;
+          if (tw > 1e-6f) tot = tot / tw;
+          out = make_float4(tot.x, tot.y, tot.z, tw);
+        } else {
+          // probe_conv.comp:321-326
+          float3 res = f3(acc[a][b][0], acc[a][b][1], acc[a][b][2]);
+          if (ws > 1e-6f) res = res / ws;
+          out = make_float4(res.x * ha + old.x * h, res.y * ha + old.y * h, res.z * ha + old.z * h,
+                            ws * ha + old.w * h);
+        }
+        storeTexel(it.atlas, g.atlasFmt, ai, out);
+      }
+    }
   }
 }
 
 }  // namespace
 
 long long convGroups(const GridGPU& g, int layerBegin, int layerEnd) {
-  return ((long long)(layerEnd - layerBegin) * g.X * g.Z + kConvProbes - 1) / kConvProbes;
+  return ((long long)(layerEnd - layerBegin) * g.X * g.Z + kTileProbes - 1) / kTileProbes;
 }
 
 cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream) {
   if (numItems <= 0 || totalGroups <= 0) return cudaSuccess;
   k_conv_weights_batch<<<dim3(kOctTexels, numItems), 256, 0, stream>>>(dItems);
-  int dev = 0, sms = 0;
+  int dev = 0, sms = 0, perSm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  long long grid = (long long)sms * 8;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch, kTileThreads, 0);
+  long long grid = (long long)sms * (perSm > 0 ? perSm : 1);
   if (grid > totalGroups) grid = totalGroups;
-  k_conv_fp32_batch<<<(unsigned)grid, kConvThreads, 0, stream>>>(dItems, numItems, totalGroups);
+  k_conv_fp32_batch<<<(unsigned)grid, kTileThreads, 0, stream>>>(dItems, numItems, totalGroups);
   return cudaGetLastError();
 }
 

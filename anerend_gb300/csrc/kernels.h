@@ -52,7 +52,7 @@ struct ConvItem {
   int layerBegin, layerEnd;
   float hysteresis;
   uint32_t flags;
-  long long groupBegin;  // first 4-probe group of this item
+  long long groupBegin;  // first 32-probe tile of this item
 };
 long long convGroups(const GridGPU& g, int layerBegin, int layerEnd);
 cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream);
