@@ -79,7 +79,7 @@ class Frame(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
-                ("convMode", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("convMode", C.c_int32), ("bvhWidth", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class BatchItem(C.Structure):
@@ -88,8 +88,8 @@ class BatchItem(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
-                ("convMode", C.c_int32), ("blocksPerSm", C.c_int32), ("warpsPerFetch", C.c_int32),
-                ("useGraph", C.c_int32), ("reserved", C.c_int32)]
+                ("convMode", C.c_int32), ("blocksPerSm", C.c_int32), ("refillLanes", C.c_int32),
+                ("useGraph", C.c_int32), ("bvhWidth", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -120,6 +120,8 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
     return fail(ctx, DDGI_EINVAL, "warpProbes %d must be a power of two in [%d, 32]", t.warpProbes, minWp);
   if (t.rayOrder != 0 && t.rayOrder != 1) return fail(ctx, DDGI_EINVAL, "rayOrder %d unknown", t.rayOrder);
   if (t.shadowMode != 0 && t.shadowMode != 1) return fail(ctx, DDGI_EINVAL, "shadowMode %d unknown", t.shadowMode);
+  if (t.bvhWidth != 0 && t.bvhWidth != 2 && t.bvhWidth != 8)
+    return fail(ctx, DDGI_EINVAL, "bvhWidth %d must be 2 or 8 (0 = 8)", t.bvhWidth);
   if (t.convMode < 0 || t.convMode > 2) return fail(ctx, DDGI_EINVAL, "convMode %d unknown", t.convMode);
   if (t.convMode != 0 && g->g.N % 64)
     return fail(ctx, DDGI_EINVAL, "tensor-core convolution needs raysPerProbe %% 64 == 0 (N = %d)", g->g.N);
@@ -137,7 +139,9 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
   else
     CK(cudaMemcpy(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice), "ray order upload");
   g->tuning = t;
+  if (g->tuning.bvhWidth == 0) g->tuning.bvhWidth = 8;
   g->g.warpProbes = t.warpProbes;
+  g->g.bvhWide = g->tuning.bvhWidth == 8 ? 1 : 0;
   return DDGI_OK;
 }
 
@@ -206,7 +210,7 @@ int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
   if (sc->shadowValid && sc->shadowLight[0] == lightDir[0] && sc->shadowLight[1] == lightDir[1] &&
       sc->shadowLight[2] == lightDir[2])
     return DDGI_OK;
-  if (sc->view.numTris == 0) return DDGI_OK;
+  if (sc->view.bvh.numTris == 0) return DDGI_OK;
   double n = std::sqrt((double)lightDir[0] * lightDir[0] + (double)lightDir[1] * lightDir[1] +
                        (double)lightDir[2] * lightDir[2]);
   if (!(n > 0)) return fail(ctx, DDGI_EINVAL, "lightDir has zero length");
@@ -235,7 +239,7 @@ int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
   LbvhResult r;
   if (e == cudaSuccess)
     e = lbvhBuild(dInst, (int)sh.size(), sc->meshes, sc->indices, sc->numIndices, sc->vertices, sc->numVertices,
-                  sc->view.numTris, ctx->dErr, st, &r);
+                  sc->view.bvh.numTris, ctx->dErr, st, &r);
   cudaFree(dInst);
   if (e != cudaSuccess) return cudaFail(ctx, e, "shadow BVH build");
   lbvhFree(&sc->shadowBvh);
@@ -245,8 +249,7 @@ int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
     sc->view.shearK[i] = k[i];
     sc->view.shearS[i] = (float)S[i];
   }
-  sc->view.shadowNodes = r.nodes;
-  sc->view.shadowTris = r.tris;
+  sc->view.shadow = BvhRef{r.nodes, r.wnodes, r.tris, r.numTris, r.numNodes, r.numWNodes};
   sc->shadowValid = true;
   return DDGI_OK;
 }
@@ -270,6 +273,9 @@ int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_
 }
 
 
+// Ray slots of a whole-grid trace for any warpProbes: ceil(XZ / wp) * wp <= XZ + 31 probes per layer.
+long long maxRaySlots(const GridGPU& g) { return ((long long)g.X * g.Z + 31) * g.Y * g.N; }
+
 uint64_t gridFootprint(const DdgiGridDesc* d, int convMode) {
   GridGPU g = makeGridGPU(*d);
   uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
@@ -279,6 +285,7 @@ uint64_t gridFootprint(const DdgiGridDesc* d, int convMode) {
   if (d->options & DDGI_GRID_WRITE_DIRS) bytes += 16 * rays;
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
   if (convMode != 0) bytes += 6 * rays + tcScratchBytes(g.N);
+  bytes += kTraceScratchPerRay * (uint64_t)maxRaySlots(g);  // the launch's trace scratch for this grid
   return bytes;
 }
 
@@ -319,6 +326,7 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
   t.warpProbes = std::max(1, 32 / g->g.N);
   t.rayOrder = 1;
   t.shadowMode = 1;
+  t.bvhWidth = 8;
   int rc2 = applyTuning(g, t);
   if (rc2 != DDGI_OK) {
     gridDestroy(g);
@@ -343,6 +351,7 @@ void gridDestroy(DdgiGrid* g) {
   gridFree(g, g->wsum);
   cudaFree(g->dTrace);
   cudaFree(g->dQueue);
+  cudaFree(g->dHits);
   cudaFree(g->dConv);
   g->ring.release();
   delete g;
@@ -355,7 +364,10 @@ int ensureSoloRecords(DdgiGrid* g) {
   // dTrace is followed by the rotation: one staging copy carries both
   CK(cudaMalloc(&g->dTrace, sizeof(TraceItem) + sizeof(Mat3)), "trace record");
   g->dRot = reinterpret_cast<Mat3*>(reinterpret_cast<unsigned char*>(g->dTrace) + sizeof(TraceItem));
-  CK(cudaMalloc(&g->dQueue, sizeof(unsigned long long)), "trace queue");
+  CK(cudaMalloc(&g->dQueue, kTraceCounters * sizeof(unsigned long long)), "trace counters");
+  const long long slots = maxRaySlots(g->g);
+  CK(cudaMalloc(&g->dHits, kTraceScratchPerRay * (size_t)slots), "trace scratch");
+  g->dShadow = g->dHits + slots;
   CK(cudaMalloc(&g->dConv, sizeof(ConvItem)), "convolve record");
   CK(g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem))), "record staging");
   return DDGI_OK;
@@ -478,9 +490,8 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
     ddgi_scene_destroy(sc);
     return cudaFail(ctx, e, "scene upload / BVH build");
   }
-  sc->view.nodes = sc->bvh.nodes;
-  sc->view.tris = sc->bvh.tris;
-  sc->view.numTris = (int)tris;
+  sc->view.bvh = BvhRef{sc->bvh.nodes, sc->bvh.wnodes, sc->bvh.tris, (int)tris, sc->bvh.numNodes, sc->bvh.numWNodes};
+  sc->view.shadow = BvhRef{};
   sc->view.vertices = sc->vertices;
   sc->view.indices = sc->indices;
   sc->view.meshes = sc->meshes;
@@ -491,7 +502,7 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
   sc->info.deviceBytes = sizeof(DdgiPackedVertex) * d->numVertices + 4ull * d->numIndices +
                          sizeof(DdgiMeshInfo) * d->numMeshes + sizeof(InstanceGPU) * inst.size() +
                          sizeof(DdgiMaterialInfo) * d->numMaterials + 48ull * tris +
-                         64ull * (tris > 1 ? tris - 1 : 1);
+                         64ull * (tris > 1 ? tris - 1 : 1) + 208ull * (uint64_t)sc->bvh.numWNodes;
   for (int k = 0; k < 3; ++k) {
     sc->info.boundsMin[k] = sc->bvh.centroidLo[k];
     sc->info.boundsMax[k] = sc->bvh.centroidHi[k];
@@ -595,8 +606,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
     if (rc) return rc;
     view = scene->view;
   } else {
-    view.shadowNodes = nullptr;
-    view.shadowTris = nullptr;
+    view.shadow = BvhRef{};
   }
   GridGPU gg = g->g;
   g->rad16Written = false;
@@ -624,7 +634,8 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   Mat3& rot = *reinterpret_cast<Mat3*>(h + sizeof(TraceItem));
   memcpy(rot.m, frame->rotation, sizeof(rot.m));
   CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
-  CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, ctx->numSms * 8, 4, ctx->dErr, st),
+  CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, g->dHits, g->dShadow,
+                      ctx->numSms * 8, 8, g->tuning.bvhWidth != 2, ctx->dErr, st),
      "trace");
   g->tracedBegin = b;
   g->tracedEnd = e;

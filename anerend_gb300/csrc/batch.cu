@@ -25,7 +25,10 @@ struct LaunchState {
   // device records, one block: cap TraceItem | cap Mat3 | cap ConvItem | cap x 128-byte TcItem
   unsigned char* dRec = nullptr;
   size_t offRots = 0, offConv = 0, offTc = 0, recBytes = 0;
-  unsigned long long* dQueue = nullptr;
+  unsigned long long* dQueue = nullptr;  // kTraceCounters trace counters
+  float4* dHits = nullptr;               // trace scratch: hit records, then shadow list (rayCap each)
+  float4* dShadow = nullptr;
+  long long rayCap = 0;
   StagingRing ring;  // pinned host images of the record block
   std::vector<TcItemHost> tcHost;
   cudaStream_t captureStream = nullptr;  // the caller's stream may be the uncapturable legacy stream
@@ -48,8 +51,11 @@ struct LaunchState {
     captureStream = nullptr;
     cudaFree(dRec);
     cudaFree(dQueue);
+    cudaFree(dHits);
     dRec = nullptr;
     dQueue = nullptr;
+    dHits = dShadow = nullptr;
+    rayCap = 0;
     ring.release();
     cap = 0;
   }
@@ -68,11 +74,25 @@ struct LaunchState {
     offTc = offConv + align(sizeof(ConvItem) * newCap);
     recBytes = offTc + 128 * (size_t)newCap;
     cudaError_t e = cudaMalloc(&dRec, recBytes);
-    if (e == cudaSuccess && !dQueue) e = cudaMalloc(&dQueue, sizeof(unsigned long long));
+    if (e == cudaSuccess && !dQueue) e = cudaMalloc(&dQueue, kTraceCounters * sizeof(unsigned long long));
     if (e == cudaSuccess) e = ring.init(recBytes);
     if (e == cudaSuccess && !captureStream) e = cudaStreamCreateWithFlags(&captureStream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cudaFail(c, e, "launch records");
     cap = newCap;
+    return DDGI_OK;
+  }
+  // Trace scratch for `rays` ray slots; growing drops the captured graph (its kernels hold the pointers).
+  int reserveRays(long long rays) {
+    if (rays <= rayCap) return DDGI_OK;
+    long long newCap = std::max(rays, rayCap + rayCap / 2);
+    dropGraph();
+    cudaFree(dHits);
+    dHits = dShadow = nullptr;
+    rayCap = 0;
+    cudaError_t e = cudaMalloc(&dHits, kTraceScratchPerRay * (size_t)newCap);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "trace scratch");
+    dShadow = dHits + newCap;
+    rayCap = newCap;
     return DDGI_OK;
   }
 };
@@ -98,8 +118,8 @@ int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long t
           int totalTiles, cudaStream_t st) {
   DdgiContext* ctx = S->ctx;
   int blocks = ctx->numSms * t.blocksPerSm;
-  CK(launchTraceBatch(S->dTrace(), S->dRots(), n, maxN, totalWarps, S->dQueue, blocks, t.warpsPerFetch, ctx->dErr,
-                      st),
+  CK(launchTraceBatch(S->dTrace(), S->dRots(), n, maxN, totalWarps, S->dQueue, S->dHits, S->dShadow, blocks,
+                      t.refillLanes, t.bvhWidth != 2, ctx->dErr, st),
      "batched trace");
   if (t.convMode != 0) {
     int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
@@ -155,8 +175,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
       if (rc) return rc;
       view = sc->view;
     } else {
-      view.shadowNodes = nullptr;
-      view.shadowTris = nullptr;
+      view.shadow = BvhRef{};
     }
     GridGPU gg = g->g;
     if (tc) {
@@ -206,13 +225,15 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     g->latticeValid = true;
     g->rad16Written = tc;
   }
+  rc = S->reserveRays(32 * warps);
+  if (rc) return rc;
   CK(S->ring.copy(slot, S->dRec, S->recBytes, st), "launch records");
   if (stats) {
     stats->rays = (uint64_t)rays;
     stats->translations = (uint32_t)moved;
   }
   // the captured sequence depends only on these (per-item values live in the device records)
-  S->shape = {n, maxN, warps, groups, tiles, t.convMode, t.blocksPerSm, t.warpsPerFetch};
+  S->shape = {n, maxN, warps, groups, tiles, t.convMode, t.blocksPerSm, t.refillLanes, t.bvhWidth};
   const bool stable = allowGraph && t.useGraph && S->shape == S->lastShape;
   if (stable && !S->exec) {
     cudaGraph_t graph = nullptr;
@@ -249,10 +270,12 @@ int checkBatchTuning(DdgiContext* ctx, const DdgiBatchTuning& t) {
   if (t.warpProbes < 1 || t.warpProbes > 32 || (t.warpProbes & (t.warpProbes - 1)))
     return fail(ctx, DDGI_EINVAL, "batch warpProbes %d must be a power of two in [1, 32]", t.warpProbes);
   if (t.blocksPerSm < 1 || t.blocksPerSm > 8) return fail(ctx, DDGI_EINVAL, "blocksPerSm must be in [1, 8]");
-  if (t.warpsPerFetch < 1 || t.warpsPerFetch > 64) return fail(ctx, DDGI_EINVAL, "warpsPerFetch must be in [1, 64]");
+  if (t.refillLanes < 1 || t.refillLanes > 32) return fail(ctx, DDGI_EINVAL, "refillLanes must be in [1, 32]");
   if (t.convMode < 0 || t.convMode > 2) return fail(ctx, DDGI_EINVAL, "convMode %d unknown", t.convMode);
   if (t.rayOrder != 0 && t.rayOrder != 1) return fail(ctx, DDGI_EINVAL, "rayOrder %d unknown", t.rayOrder);
   if (t.shadowMode != 0 && t.shadowMode != 1) return fail(ctx, DDGI_EINVAL, "shadowMode %d unknown", t.shadowMode);
+  if (t.bvhWidth != 0 && t.bvhWidth != 2 && t.bvhWidth != 8)
+    return fail(ctx, DDGI_EINVAL, "bvhWidth %d must be 2 or 8 (0 = 8)", t.bvhWidth);
   return DDGI_OK;
 }
 
@@ -263,6 +286,7 @@ int tuneGridForBatch(DdgiGrid* g, const DdgiBatchTuning& t) {
   gt.rayOrder = t.rayOrder;
   gt.shadowMode = t.shadowMode;
   gt.convMode = t.convMode;
+  gt.bvhWidth = t.bvhWidth;
   return applyTuning(g, gt);
 }
 
@@ -273,8 +297,9 @@ DdgiBatchTuning defaultBatchTuning() {
   t.shadowMode = 1;
   t.convMode = 0;
   t.blocksPerSm = 8;
-  t.warpsPerFetch = 4;
+  t.refillLanes = 8;
   t.useGraph = 1;
+  t.bvhWidth = 8;
   return t;
 }
 

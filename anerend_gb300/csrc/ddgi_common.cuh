@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
+#include <math.h>
 #include <stdint.h>
 #include "../../include/ddgi.h"
 
@@ -49,7 +50,11 @@ DDGI_HD float3 clamp3(float3 a, float lo, float hi) {
   return f3(clampf(a.x, lo, hi), clampf(a.y, lo, hi), clampf(a.z, lo, hi));
 }
 DDGI_D float3 normalize3(float3 v) {
+#ifdef __CUDA_ARCH__
   float inv = rsqrtf(dot3(v, v));
+#else
+  float inv = 1.0f / sqrtf(dot3(v, v));  // host builds of the shared headers (CPU tests)
+#endif
   return v * inv;
 }
 DDGI_HD float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
@@ -196,10 +201,20 @@ struct InstanceGPU {
 //   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
 //   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
 //   n3 = (child0, child1, -, -) as ints; child >= 0 internal node, child < 0 leaf ~leafIndex
-struct SceneGPU {
-  const float4* nodes;        // 4 float4 per internal node, root = node 0
-  const float4* tris;         // 3 float4 per leaf (leaf order): v0|globalId, v1|instance, v2|prim
+// One BVH as the traversals see it (traverse.cuh). Triangles: 3 float4 per record, world v0|globalId,
+// v1|instance, v2|primitive. Binary nodes: 4 float4 per internal node (Aila-Laine: both child boxes, then
+// the child ids; a child id c < 0 is triangle record ~c). Wide nodes: kWideNodeF4 float4 each.
+struct BvhRef {
+  const float4* nodes;
+  const float4* wnodes;
+  const float4* tris;
   int numTris;
+  int numNodes;
+  int numWNodes;
+};
+
+struct SceneGPU {
+  BvhRef bvh;                 // world-space triangles of every instance
   const DdgiPackedVertex* vertices;
   const uint32_t* indices;
   const DdgiMeshInfo* meshes;
@@ -207,9 +222,8 @@ struct SceneGPU {
   const DdgiMaterialInfo* materials;
   // Shadow BVH in the sheared ray space of the light direction (Woop et al.'s per-ray shear, fixed for
   // every shadow ray of a frame): a shadow ray from p is the line through shear(p) along +z, so the same
-  // watertight test and traversal run on it with direction (0, 0, 1). Null when not built.
-  const float4* shadowNodes;
-  const float4* shadowTris;
+  // watertight test and traversal run on it with direction (0, 0, 1). shadow.tris is null when not built.
+  BvhRef shadow;
   int shearK[3];      // kx, ky, kz
   float shearS[3];    // Sx, Sy, Sz
 };
@@ -221,6 +235,7 @@ struct GridGPU {
   int atlasW, atlasH, atlasFmt;
   int rayW;
   uint32_t options;
+  int bvhWide;     // 1: traverse the 8-wide BVH, 0: the binary one
   int warpProbes;  // probes per warp (power of two, 32 / warpProbes <= N)
   void* rad16;     // when set, the trace also writes planar 16-bit radiance (row c * pTotal + p, N per row)
   int rad16Fmt;    // 0 FP16, 1 BF16

@@ -22,16 +22,21 @@ struct TraceItem {
   float4* rayRad;
   float4* rayDir;
   int* rayHit;
-  long long warpBegin;    // first queue warp of this item
+  long long warpBegin;    // first warp of this item (its ray slots start at 32 * warpBegin)
 };
 
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);
-// Warps of one grid's trace for frame f (the queue length of its item).
+// Warps of one grid's trace for frame f (32 ray slots each).
 long long traceWarps(const GridGPU& g, const FrameGPU& f);
-// Lattices of every item (rotation per item), then the persistent trace of all items' rays.
+// Device counters of one trace launch: closest-hit queue, shadow-list length, shadow queue, spare.
+constexpr int kTraceCounters = 4;
+// Scratch of one trace launch per ray slot: the hit record and the shadow-list entry (16 B each).
+constexpr size_t kTraceScratchPerRay = 32;
+// Lattices of every item (rotation per item), then the wavefront trace of all items' ray slots:
+// closest-hit traversal, shading, shadow traversal. dHits and dShadow hold 32 * totalWarps float4 each.
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
-                             unsigned long long* dQueue, int blocks, int warpsPerFetch, uint32_t* err,
-                             cudaStream_t stream);
+                             unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
+                             int refillLanes, bool wide, uint32_t* err, cudaStream_t stream);
 
 
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.

@@ -8,11 +8,15 @@
 //                of BVHs, octrees and k-d trees"), equal codes split by index
 //   5. bounds    bottom-up AABBs, the second child to arrive at a node computes it (atomic counters)
 //   6. pack      nodes into the four-float4 traversal layout, triangles into leaf order
+//   7. collapse  the binary tree into the 8-wide tree on the host (wbvh.h); triangle records are laid
+//                out in the wide tree's leaf order and the binary tree's leaf ids are renumbered to match
 #include "ddgi_common.cuh"
 #include "lbvh.h"
+#include "wbvh.h"
 
 #include <cstring>
 #include <utility>
+#include <vector>
 
 namespace ddgi {
 
@@ -434,6 +438,36 @@ cudaError_t lbvhBuild(const InstanceGPU* dInst, int numInst, const DdgiMeshInfo*
     }
   }
   out->numNodes = n > 1 ? n - 1 : 0;
+  {
+    std::vector<float4> hn(4 * (size_t)out->numNodes), ht(3 * (size_t)n);
+    if (out->numNodes)
+      DDGI_TRY(cudaMemcpyAsync(hn.data(), out->nodes, sizeof(float4) * hn.size(), cudaMemcpyDeviceToHost, stream));
+    DDGI_TRY(cudaMemcpyAsync(ht.data(), out->tris, sizeof(float4) * ht.size(), cudaMemcpyDeviceToHost, stream));
+    DDGI_TRY(cudaStreamSynchronize(stream));
+    std::vector<float4> wide;
+    std::vector<int> order;
+    if (!wbvh::collapse(hn.data(), ht.data(), n, wide, order)) {
+      e = cudaErrorUnknown;
+      goto done;
+    }
+    std::vector<int> inv(n);
+    for (int k = 0; k < n; ++k) inv[order[k]] = k;
+    std::vector<float4> ht2(ht.size());
+    for (int k = 0; k < n; ++k)
+      for (int v = 0; v < 3; ++v) ht2[3 * k + v] = ht[3 * (size_t)order[k] + v];
+    for (int i = 0; i < out->numNodes; ++i) {
+      int c0 = wbvh::asIntH(hn[4 * i + 3].x), c1 = wbvh::asIntH(hn[4 * i + 3].y);
+      if (c0 < 0) hn[4 * i + 3].x = wbvh::asFloatH((uint32_t)~inv[~c0]);
+      if (c1 < 0) hn[4 * i + 3].y = wbvh::asFloatH((uint32_t)~inv[~c1]);
+    }
+    out->numWNodes = (int)(wide.size() / kWideNodeF4);
+    DDGI_TRY(cudaMalloc(&out->wnodes, sizeof(float4) * wide.size()));
+    DDGI_TRY(cudaMemcpyAsync(out->wnodes, wide.data(), sizeof(float4) * wide.size(), cudaMemcpyHostToDevice, stream));
+    DDGI_TRY(cudaMemcpyAsync(out->tris, ht2.data(), sizeof(float4) * ht2.size(), cudaMemcpyHostToDevice, stream));
+    if (out->numNodes)
+      DDGI_TRY(cudaMemcpyAsync(out->nodes, hn.data(), sizeof(float4) * hn.size(), cudaMemcpyHostToDevice, stream));
+    DDGI_TRY(cudaStreamSynchronize(stream));
+  }
 done:
 #undef DDGI_TRY
   cudaFree(trisRaw);
@@ -447,8 +481,10 @@ done:
 void lbvhFree(LbvhResult* r) {
   if (r->tris) cudaFree(r->tris);
   if (r->nodes) cudaFree(r->nodes);
+  if (r->wnodes) cudaFree(r->wnodes);
   r->tris = nullptr;
   r->nodes = nullptr;
+  r->wnodes = nullptr;
 }
 
 }  // namespace ddgi

@@ -6,9 +6,11 @@ namespace ddgi {
 
 struct LbvhResult {
   float4* nodes = nullptr;  // 4 float4 per internal node (numNodes of them), root = 0
-  float4* tris = nullptr;   // 3 float4 per leaf, leaf order
+  float4* tris = nullptr;   // 3 float4 per triangle record, in the wide tree's leaf order
+  float4* wnodes = nullptr; // kWideNodeF4 float4 per 8-wide node (numWNodes of them), root = 0
   int numTris = 0;
   int numNodes = 0;
+  int numWNodes = 0;
   float centroidLo[3] = {0, 0, 0}, centroidHi[3] = {0, 0, 0};
 };
 

@@ -106,7 +106,9 @@ struct DdgiGrid {
   // allocated on first use
   TraceItem* dTrace = nullptr;
   Mat3* dRot = nullptr;
-  unsigned long long* dQueue = nullptr;
+  unsigned long long* dQueue = nullptr;  // kTraceCounters trace counters
+  float4* dHits = nullptr;               // trace scratch for every ray slot of the grid (hit records,
+  float4* dShadow = nullptr;             // then the shadow list)
   ConvItem* dConv = nullptr;
   StagingRing ring;
 };
@@ -129,6 +131,7 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
 void gridDestroy(DdgiGrid* g);
 // Device bytes a grid of this description holds (atlas pair, ray images, lattice and weight tables and, for
 // a tensor-core convolution, the 16-bit radiance and its weight scratch).
+long long maxRaySlots(const GridGPU& g);
 uint64_t gridFootprint(const DdgiGridDesc* d, int convMode);
 // Batched launch of n (grid, scene, frame) items through a reusable launch state (records, staging, graph).
 struct LaunchState;

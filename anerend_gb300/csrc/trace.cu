@@ -1,14 +1,15 @@
 // Probe-ray generation, BVH traversal and hit shading: the work of irradiance_probe_update.rgen (ray
 // generation, :48-111), .rchit (hit shading + shadow ray, :134-221) and .rmiss (sky / unshadowed,
-// :17-21) on CUDA cores. The reference traverses with RT cores through traceRayEXT; here a stack-based
-// traversal of the device-built LBVH with a watertight ray/triangle test (Woop, Benthin, Wald 2013,
-// "Watertight Ray/Triangle Intersection", JCGT 2(1)) runs per thread.
+// :17-21) on CUDA cores. The reference traverses with RT cores through traceRayEXT; here each thread
+// runs a stack-based traversal (traverse.cuh) of the 8-wide BVH collapsed from the device-built LBVH, or
+// of the binary LBVH itself, with a watertight ray/triangle test.
 //
-// Thread mapping: a warp holds the same ray index j for 32 neighbouring probes of one layer. All probes
-// share one direction set, so the 32 rays of a warp are parallel and start close to each other, which keeps
-// traversal coherent.
+// Thread mapping: a warp traces 32 / warpProbes directions, consecutive in the grid's ray order, for each
+// of warpProbes neighbouring probes of one layer. One persistent launch covers every grid of a batch;
+// warps take their work from a shared queue.
 #include "ddgi_common.cuh"
 #include "kernels.h"
+#include "traverse.cuh"
 
 #include <climits>
 
@@ -30,155 +31,6 @@ __global__ void k_lattice(int n, Mat3 rot, float4* __restrict__ out) {
   for (int row = 0; row < 3; ++row)
     r[row] = (double)rot.m[row] * v[0] + (double)rot.m[3 + row] * v[1] + (double)rot.m[6 + row] * v[2];
   out[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
-}
-
-// ---------------------------------------------------------------------------------------------------
-// Watertight ray/triangle test.
-struct WRay {
-  float3 o, d, invd;
-  int kx, ky, kz;
-  float Sx, Sy, Sz;
-};
-
-DDGI_D WRay makeRay(float3 o, float3 d) {
-  WRay r;
-  r.o = o;
-  r.d = d;
-  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-  int kx = kz + 1; if (kx == 3) kx = 0;
-  int ky = kx + 1; if (ky == 3) ky = 0;
-  float dz = get(d, kz);
-  if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
-  r.kx = kx; r.ky = ky; r.kz = kz;
-  r.Sx = get(d, kx) / dz;
-  r.Sy = get(d, ky) / dz;
-  r.Sz = 1.0f / dz;
-  // box-test reciprocals; a zero component becomes a tiny same-signed value so (lo - o) * invd is finite
-  float3 dd = f3(d.x != 0.f ? d.x : copysignf(1e-20f, d.x), d.y != 0.f ? d.y : copysignf(1e-20f, d.y),
-                 d.z != 0.f ? d.z : copysignf(1e-20f, d.z));
-  r.invd = f3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
-  return r;
-}
-
-// Returns true for a hit with tmin <= t <= tmax; b1, b2 are the weights of v1, v2. Products and
-// differences of the edge functions are not contracted into FMAs, so a shared edge evaluates to the same
-// value (with opposite sign) from both of its triangles.
-DDGI_D bool intersectTri(const WRay& r, float3 v0, float3 v1, float3 v2, float tmin, float tmax, float& t,
-                         float& b1, float& b2) {
-  float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
-  float Akz = get(A, r.kz), Bkz = get(B, r.kz), Ckz = get(C, r.kz);
-  float Ax = __fsub_rn(get(A, r.kx), __fmul_rn(r.Sx, Akz));
-  float Ay = __fsub_rn(get(A, r.ky), __fmul_rn(r.Sy, Akz));
-  float Bx = __fsub_rn(get(B, r.kx), __fmul_rn(r.Sx, Bkz));
-  float By = __fsub_rn(get(B, r.ky), __fmul_rn(r.Sy, Bkz));
-  float Cx = __fsub_rn(get(C, r.kx), __fmul_rn(r.Sx, Ckz));
-  float Cy = __fsub_rn(get(C, r.ky), __fmul_rn(r.Sy, Ckz));
-  float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-  float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-  float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-  if (U == 0.0f || V == 0.0f || W == 0.0f) {  // exact fallback of the paper
-    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
-    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
-    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
-  }
-  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-  float det = U + V + W;
-  if (det == 0.0f) return false;
-  float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
-  float T = U * Az + V * Bz + W * Cz;
-  float tt = __fdiv_rn(T, det);
-  if (!(tt >= tmin && tt <= tmax)) return false;
-  float inv = __fdiv_rn(1.0f, det);
-  t = tt;
-  b1 = V * inv;
-  b2 = W * inv;
-  return true;
-}
-
-// Slab test with a conservative far distance (Ize 2013, "Robust BVH Ray Traversal", 1 + 2*gamma(3)).
-DDGI_D bool slab(const WRay& r, float lx, float hx, float ly, float hy, float lz, float hz, float tmin,
-                 float tmax, float& tnear) {
-  float t0x = (lx - r.o.x) * r.invd.x, t1x = (hx - r.o.x) * r.invd.x;
-  float t0y = (ly - r.o.y) * r.invd.y, t1y = (hy - r.o.y) * r.invd.y;
-  float t0z = (lz - r.o.z) * r.invd.z, t1z = (hz - r.o.z) * r.invd.z;
-  float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
-  tnear = tn;
-  return tn <= tf * 1.0000004f;
-}
-
-struct HitInfo {
-  int leaf;
-  int gid;
-  float t, b1, b2;
-};
-
-// Closest hit (kAnyHit = false): smallest t, ties to the lowest global triangle id.
-// Any hit (kAnyHit = true): returns at the first triangle with t in range.
-template <bool kAnyHit>
-DDGI_D bool traverse(const SceneGPU& s, const WRay& r, float tmin, float tmax, HitInfo& hit,
-                     uint32_t* __restrict__ err) {
-  hit.leaf = -1;
-  hit.gid = INT_MAX;
-  hit.t = tmax;
-  if (s.numTris <= 0) return false;
-  auto testLeaf = [&](int leaf) -> bool {
-    float4 a = __ldg(&s.tris[3 * leaf]), b = __ldg(&s.tris[3 * leaf + 1]), c = __ldg(&s.tris[3 * leaf + 2]);
-    float t, b1, b2;
-    if (intersectTri(r, xyz(a), xyz(b), xyz(c), tmin, hit.t, t, b1, b2)) {
-      int g = __float_as_int(a.w);
-      if (kAnyHit) {
-        hit.leaf = leaf; hit.gid = g; hit.t = t; hit.b1 = b1; hit.b2 = b2;
-        return true;
-      }
-      if (t < hit.t || (t == hit.t && g < hit.gid)) {
-        hit.leaf = leaf; hit.gid = g; hit.t = t; hit.b1 = b1; hit.b2 = b2;
-      }
-    }
-    return false;
-  };
-  if (s.numTris == 1) {
-    testLeaf(0);
-    return hit.leaf >= 0;
-  }
-  int stack[kStackSize];
-  int sp = 0;
-  int node = 0;
-  while (true) {
-    const float4* nd = s.nodes + 4 * node;
-    float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-    float tn0, tn1;
-    bool h0 = slab(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tmin, hit.t, tn0);
-    bool h1 = slab(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tmin, hit.t, tn1);
-    int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-    if (h0 && c0 < 0) {
-      if (testLeaf(~c0) && kAnyHit) return true;
-      h0 = false;
-    }
-    if (h1 && c1 < 0) {
-      if (testLeaf(~c1) && kAnyHit) return true;
-      h1 = false;
-    }
-    if (h0 && h1) {
-      int nearC = c0, farC = c1;
-      if (tn1 < tn0) { nearC = c1; farC = c0; }
-      if (sp >= kStackSize) {  // cannot happen for trees of depth <= 64; flag and stop this ray
-        atomicOr(err, DDGI_DEVERR_STACK_OVERFLOW);
-        break;
-      }
-      stack[sp++] = farC;
-      node = nearC;
-    } else if (h0) {
-      node = c0;
-    } else if (h1) {
-      node = c1;
-    } else {
-      if (sp == 0) break;
-      node = stack[--sp];
-    }
-  }
-  return hit.leaf >= 0;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -273,149 +125,304 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Warp shape: a warp traces D = 32 / warpProbes directions for each of warpProbes consecutive probes of a
-// layer; consecutive direction slots k map to lattice rays j = order[k]. With the octahedral Morton order
-// the D directions of a warp are neighbours on the sphere, so the warp's rays share traversal paths near
-// their common origin.
+// Wavefront trace of one launch (every item of a batch, or one grid): three kernels in stream order.
+//   k_trace_closest  persistent closest-hit traversal; writes one hit record per ray slot
+//   k_shade          one thread per ray slot: hit reconstruction, shading, probe lookup, outputs; appends
+//                    a shadow ray (origin + slot id) to a list for each hit
+//   k_trace_shadow   persistent any-hit traversal over the list; overwrites the radiance of shadowed rays
+// Splitting keeps each kernel small (registers, instruction cache) and lets the traversal kernels refill
+// idle lanes with new rays instead of waiting for a warp's longest ray.
+//
+// Ray slots: item i owns slots [32 warpBegin_i, 32 (warpBegin_i + traceWarps_i)); slot 32 w + l of an item
+// is lane l of its warp w. Warp w traces D = 32 / warpProbes directions, consecutive in the grid's ray
+// order, for each of warpProbes neighbouring probes of one layer; with the octahedral Morton order the D
+// directions are neighbours on the sphere, so rays fetched together share traversal paths.
 #ifndef DDGI_TRACE_MIN_BLOCKS
 #define DDGI_TRACE_MIN_BLOCKS 8
 #endif
-// One warp of probe rays (warp index `warp` of the grid's trace, lanes past the grid's rays idle).
-DDGI_D void traceWarp(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const float4* __restrict__ lattice,
-                      const int* __restrict__ order, const void* __restrict__ atlasPrev,
-                      float4* __restrict__ rayRad, float4* __restrict__ rayDir, int* __restrict__ rayHit,
-                      uint32_t* __restrict__ err, long long warp, int lane) {
-  const int D = 32 / g.warpProbes;                // directions per warp
+
+struct RaySlot {
+  int px, pz, layer, j;
+  bool valid;
+};
+
+DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restrict__ order, long long warp,
+                       int lane) {
+  RaySlot r;
+  r.valid = false;
+  const int D = 32 / g.warpProbes;
   const int dirChunks = g.N / D;
   const int probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
-  int dc = (int)(warp % dirChunks);
-  long long rest = warp / dirChunks;
-  int pg = (int)(rest % probeGroups);
-  int layer = f.layerBegin + (int)(rest / probeGroups);
-  if (layer >= f.layerEnd) return;
-  int p = pg * g.warpProbes + lane / D;
-  if (p >= g.X * g.Z) return;
-  int j = __ldg(&order[dc * D + lane % D]);
-  int px = p % g.X, pz = p / g.X;
+  const int dc = (int)(warp % dirChunks);
+  const long long rest = warp / dirChunks;
+  const int pg = (int)(rest % probeGroups);
+  r.layer = f.layerBegin + (int)(rest / probeGroups);
+  if (r.layer >= f.layerEnd) return r;
+  const int p = pg * g.warpProbes + lane / D;
+  if (p >= g.X * g.Z) return r;
+  r.j = __ldg(&order[dc * D + lane % D]);
+  r.px = p % g.X;
+  r.pz = p / g.X;
+  r.valid = true;
+  return r;
+}
 
-  // ray generation (rgen:51-88)
+DDGI_D int findItem(const TraceItem* __restrict__ items, int numItems, long long warp) {
+  int lo = 0, hi = numItems - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (items[mid].warpBegin <= warp) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ray generation (rgen:51-88)
+DDGI_D float3 probeOrigin(const GridGPU& g, const FrameGPU& f, const RaySlot& rs) {
   float3 stepv, offv;
   probeFrame(g, f, stepv, offv);
-  float3 origin = f3((float)px, (float)layer, (float)pz) * stepv + offv;
-  float4 d4 = __ldg(&lattice[j]);
-  float3 dir = xyz(d4);
+  return f3((float)rs.px, (float)rs.layer, (float)rs.pz) * stepv + offv;
+}
 
-  WRay ray = makeRay(origin, dir);
-  HitInfo hit;
-  float3 L;
-  int hitCode = -1;
-  if (!traverse<false>(s, ray, kTMin, kTMax, hit, err)) {
-    L = toLinear(f.skyColor * f.skyIntensity);  // rmiss:20
-  } else {
-    // hit reconstruction (rchit:137-152)
-    int inst = __float_as_int(__ldg(&s.tris[3 * hit.leaf + 1].w));
-    int prim = __float_as_int(__ldg(&s.tris[3 * hit.leaf + 2].w));
-    const InstanceGPU& in = s.instances[inst];
-    const DdgiMeshInfo& mesh = s.meshes[in.mesh];
-    uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
-    const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
-    const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
-    const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
-    const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
-    float b1 = hit.b1, b2 = hit.b2, b0 = 1.0f - b1 - b2;
-    float4 a0 = __ldg((const float4*)v0.d0), a1 = __ldg((const float4*)v1.d0), a2 = __ldg((const float4*)v2.d0);
-    float4 c0 = __ldg((const float4*)v0.d1), c1 = __ldg((const float4*)v1.d1), c2 = __ldg((const float4*)v2.d1);
-    float4 e0 = __ldg((const float4*)v0.d2), e1 = __ldg((const float4*)v1.d2), e2 = __ldg((const float4*)v2.d2);
-    float3 posObj = xyz(a0) * b0 + xyz(a1) * b1 + xyz(a2) * b2;
-    const float* m = in.o2w;
-    float3 pos = f3(m[0] * posObj.x + m[1] * posObj.y + m[2] * posObj.z + m[3],
-                    m[4] * posObj.x + m[5] * posObj.y + m[6] * posObj.z + m[7],
-                    m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
+DDGI_D size_t rayIndex(const GridGPU& g, const RaySlot& rs) {
+  const int rx = rs.px * g.bw + (rs.j % g.bw);
+  const int ry = (rs.layer * g.Z + rs.pz) * g.bh + (rs.j / g.bw);
+  return (size_t)ry * g.rayW + rx;
+}
 
-    // shadow ray toward the sun (rchit:155-176), any hit in [0.1, 50]
-    bool shadowed;
-    HitInfo shit;
-    if (s.shadowNodes) {
-      // the light's sheared space: the ray is the +z line through shear(pos)
-      float pk[3] = {pos.x, pos.y, pos.z};
-      float pz = pk[s.shearK[2]];
-      float3 o = f3(pk[s.shearK[0]] - s.shearS[0] * pz, pk[s.shearK[1]] - s.shearS[1] * pz, s.shearS[2] * pz);
-      SceneGPU ls = s;
-      ls.nodes = s.shadowNodes;
-      ls.tris = s.shadowTris;
-      shadowed = traverse<true>(ls, makeRay(o, f3(0.f, 0.f, 1.f)), kTMin, kTMax, shit, err);
-    } else {
-      float3 shadowDir = normalize3(-f.lightDir);
-      shadowed = traverse<true>(s, makeRay(pos, shadowDir), kTMin, kTMax, shit, err);
-    }
-
-    // surface (rchit:179-187, getSurfaceDataFromMat bindless.glsl:181-237 without textures)
-    const DdgiMaterialInfo& mat = s.materials[in.material];
-    float3 nObj = f3(c0.z, c0.w, e0.x) * b0 + f3(c1.z, c1.w, e1.x) * b1 + f3(c2.z, c2.w, e2.x) * b2;
-    nObj = normalize3(nObj);
-    const float* wi = in.w2oLin;  // normal * WorldToObject (row vector times the inverse 3x3)
-    float3 normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6],
-                                  nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
-                                  nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
-    float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
-    float3 color = toLinear(vcol);
-    float4 bcf = __ldg((const float4*)mat.baseColFac);
-    if (bcf.x + bcf.y + bcf.z > 0.1f) color = xyz(bcf);
-    float4 mr = __ldg((const float4*)mat.metRough);
-    float4 em = __ldg((const float4*)mat.emissive);
-    float metallic = mr.x, roughness = mr.y;
-
-    L = f3(0.f, 0.f, 0.f);
-    if (!shadowed)
-      L = calcLightDirectional(normal, color, metallic, roughness, pos, origin, f.lightDir, f.sunIntensity);
-    if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG)
-      L += calcIndirectDiffuse(g, f, atlasPrev, normal, color, metallic, roughness, pos, origin);
-    L += xyz(em) * em.w;
-    hitCode = hit.gid * 2 + (shadowed ? 1 : 0);
-  }
-
-  // stores (rgen:108-109)
-  int rx = px * g.bw + (j % g.bw);
-  int ry = (layer * g.Z + pz) * g.bh + (j / g.bw);
-  size_t idx = (size_t)ry * g.rayW + rx;
-  rayRad[idx] = make_float4(L.x, L.y, L.z, 1.0f);
-  if (rayDir) rayDir[idx] = make_float4(dir.x, dir.y, dir.z, 1.0f);
-  if (rayHit) rayHit[idx] = hitCode;
-  if (g.rad16) {  // operand of the tensor-core convolution
-    size_t base = ((size_t)(layer * g.Z + pz) * g.X + px) * g.N + j;
-    size_t plane = (size_t)g.pTotal * g.N;
-    uint16_t* o = (uint16_t*)g.rad16;
-    float c[3] = {L.x, L.y, L.z};
+// operand of the tensor-core convolution: planar 16-bit radiance, row c * pTotal + probe
+DDGI_D void storeRad16(const GridGPU& g, const RaySlot& rs, float3 L) {
+  const size_t base = ((size_t)(rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N + rs.j;
+  const size_t plane = (size_t)g.pTotal * g.N;
+  uint16_t* o = (uint16_t*)g.rad16;
+  const float c[3] = {L.x, L.y, L.z};
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-      o[base + k * plane] = g.rad16Fmt == 0 ? __half_as_ushort(__float2half_rn(c[k]))
-                                            : __bfloat16_as_ushort(__float2bfloat16_rn(c[k]));
+  for (int k = 0; k < 3; ++k)
+    o[base + k * plane] = g.rad16Fmt == 0 ? __half_as_ushort(__float2half_rn(c[k]))
+                                          : __bfloat16_as_ushort(__float2bfloat16_rn(c[k]));
+}
+
+constexpr int kNoRay = -2;  // hit record of a slot without a ray (past the grid's probes or layers)
+
+// Traversal state of one lane: the binary or the 8-wide stack machine.
+template <bool kWide> struct TravOf;
+template <> struct TravOf<false> { using T = BinTrav; };
+template <> struct TravOf<true> { using T = WideTrav; };
+
+template <bool kWide, bool kAnyHit>
+DDGI_D bool travInit(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& s, HitInfo& hit) {
+  if constexpr (kWide) return wideInit<kAnyHit>(b, r, kTMax, s, hit);
+  else return binInit<kAnyHit>(b, r, kTMin, kTMax, s, hit);
+}
+template <bool kWide, bool kAnyHit>
+DDGI_D bool travStep(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& s, HitInfo& hit, uint32_t* err) {
+  if constexpr (kWide) return wideStep<kAnyHit>(b, r, kTMin, s, hit, err);
+  else return binStep<kAnyHit>(b, r, kTMin, s, hit, err);
+}
+
+// Closest hits of every ray slot (rgen:90-106). Each lane owns one ray; once at least refillLanes lanes of
+// a warp are idle the warp takes that many new slots from the queue (counters[0]) with one atomic.
+template <bool kWide>
+__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+    k_trace_closest(const TraceItem* __restrict__ items, int numItems, long long totalRays,
+                    unsigned long long* __restrict__ counters, int refillLanes, float4* __restrict__ hits,
+                    uint32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  long long id = -1;
+  bool drained = false;
+  BvhRef bvh;
+  WRay ray;
+  HitInfo hit;
+  typename TravOf<kWide>::T st;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, id < 0);
+    if (drained && idle == 0xffffffffu) break;
+    if (!drained && __popc(idle) >= refillLanes) {
+      const int need = __popc(idle);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&counters[0], (unsigned long long)need);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((long long)base + need >= totalRays) drained = true;
+      const long long cand = (long long)base + __popc(idle & below);
+      if (id < 0 && cand < totalRays) {
+        const long long warp = cand >> 5;
+        const TraceItem& T = items[findItem(items, numItems, warp)];
+        const RaySlot rs = raySlot(T.g, T.f, T.order, warp - T.warpBegin, (int)(cand & 31));
+        if (!rs.valid) {
+          hits[cand] = make_float4(__int_as_float(kNoRay), 0.f, 0.f, 0.f);
+        } else {
+          ray = makeRay(probeOrigin(T.g, T.f, rs), xyz(__ldg(&T.lattice[rs.j])));
+          bvh = T.s.bvh;
+          if (travInit<kWide, false>(bvh, ray, st, hit))
+            hits[cand] = make_float4(__int_as_float(hit.leaf), hit.t, hit.b1, hit.b2);
+          else
+            id = cand;
+        }
+      }
+    }
+    if (id >= 0 && travStep<kWide, false>(bvh, ray, st, hit, err)) {
+      hits[id] = make_float4(__int_as_float(hit.leaf), hit.t, hit.b1, hit.b2);
+      id = -1;
+    }
   }
 }
 
-// Persistent trace over many grids: warps take `warpsPerFetch` warps of work at a time from one queue that
-// spans every item's rays (item i owns warps [warpBegin_i, warpBegin_i + numWarps_i)).
-__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
-    k_trace_batch(const TraceItem* __restrict__ items, int numItems, long long totalWarps,
-                  unsigned long long* __restrict__ queue, int warpsPerFetch, uint32_t* __restrict__ err) {
+// Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
+// computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
+// shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
+__global__ void __launch_bounds__(256) k_shade(const TraceItem* __restrict__ items, int numItems, long long totalRays,
+                                               float4* __restrict__ hits, float4* __restrict__ shadowList,
+                                               unsigned long long* __restrict__ counters) {
   const int lane = threadIdx.x & 31;
-  while (true) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(queue, (unsigned long long)warpsPerFetch);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if ((long long)base >= totalWarps) break;
-    for (int k = 0; k < warpsPerFetch; ++k) {
-      long long w = (long long)base + k;
-      if (w >= totalWarps) break;
-      int lo = 0, hi = numItems - 1;
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (items[mid].warpBegin <= w) lo = mid; else hi = mid - 1;
+  const unsigned below = (1u << lane) - 1u;
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < totalRays;
+       id += (long long)gridDim.x * blockDim.x) {
+    const float4 hr = hits[id];
+    const int leaf = __float_as_int(hr.x);
+    bool cast = false;
+    float3 so = f3(0.f, 0.f, 0.f);
+    if (leaf != kNoRay) {
+      const long long warp = id >> 5;
+      const TraceItem& T = items[findItem(items, numItems, warp)];
+      const SceneGPU& s = T.s;
+      const GridGPU& g = T.g;
+      const FrameGPU& f = T.f;
+      const RaySlot rs = raySlot(g, f, T.order, warp - T.warpBegin, (int)(id & 31));
+      const float3 origin = probeOrigin(g, f, rs);
+      const float3 dir = xyz(__ldg(&T.lattice[rs.j]));
+      float3 L;
+      int hitCode = -1;
+      if (leaf < 0) {
+        L = toLinear(f.skyColor * f.skyIntensity);  // rmiss:20
+      } else {
+        // hit reconstruction (rchit:137-152)
+        const float4 r0 = __ldg(&s.bvh.tris[3 * leaf]);
+        const int inst = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 1].w));
+        const int prim = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 2].w));
+        const InstanceGPU& in = s.instances[inst];
+        const DdgiMeshInfo& mesh = s.meshes[in.mesh];
+        const uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
+        const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
+        const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
+        const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
+        const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
+        const float b1 = hr.z, b2 = hr.w, b0 = 1.0f - b1 - b2;
+        const float4 a0 = __ldg((const float4*)v0.d0), a1 = __ldg((const float4*)v1.d0), a2 = __ldg((const float4*)v2.d0);
+        const float4 c0 = __ldg((const float4*)v0.d1), c1 = __ldg((const float4*)v1.d1), c2 = __ldg((const float4*)v2.d1);
+        const float4 e0 = __ldg((const float4*)v0.d2), e1 = __ldg((const float4*)v1.d2), e2 = __ldg((const float4*)v2.d2);
+        const float3 posObj = xyz(a0) * b0 + xyz(a1) * b1 + xyz(a2) * b2;
+        const float* m = in.o2w;
+        const float3 pos = f3(m[0] * posObj.x + m[1] * posObj.y + m[2] * posObj.z + m[3],
+                              m[4] * posObj.x + m[5] * posObj.y + m[6] * posObj.z + m[7],
+                              m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
+        // shadow ray origin toward the sun (rchit:155-176): the light's sheared space when built
+        if (s.shadow.tris != nullptr) {
+          const float pk[3] = {pos.x, pos.y, pos.z};
+          const float pz = pk[s.shearK[2]];
+          so = f3(pk[s.shearK[0]] - s.shearS[0] * pz, pk[s.shearK[1]] - s.shearS[1] * pz, s.shearS[2] * pz);
+        } else {
+          so = pos;
+        }
+        cast = true;
+        // surface (rchit:179-187, getSurfaceDataFromMat bindless.glsl:181-237 without textures)
+        const DdgiMaterialInfo& mat = s.materials[in.material];
+        float3 nObj = f3(c0.z, c0.w, e0.x) * b0 + f3(c1.z, c1.w, e1.x) * b1 + f3(c2.z, c2.w, e2.x) * b2;
+        nObj = normalize3(nObj);
+        const float* wi = in.w2oLin;  // normal * WorldToObject (row vector times the inverse 3x3)
+        const float3 normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6],
+                                            nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
+                                            nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
+        const float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
+        float3 color = toLinear(vcol);
+        const float4 bcf = __ldg((const float4*)mat.baseColFac);
+        if (bcf.x + bcf.y + bcf.z > 0.1f) color = xyz(bcf);
+        const float4 mr = __ldg((const float4*)mat.metRough);
+        const float4 em = __ldg((const float4*)mat.emissive);
+        const float metallic = mr.x, roughness = mr.y;
+        // lit: L = calcLight; shadowed: L = 0; then += indirect, += emissive (rchit:195-214)
+        L = calcLightDirectional(normal, color, metallic, roughness, pos, origin, f.lightDir, f.sunIntensity);
+        float3 Ls = f3(0.f, 0.f, 0.f);
+        if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG) {
+          const float3 ind = calcIndirectDiffuse(g, f, T.atlasPrev, normal, color, metallic, roughness, pos, origin);
+          L += ind;
+          Ls += ind;
+        }
+        L += xyz(em) * em.w;
+        Ls += xyz(em) * em.w;
+        hits[id] = make_float4(Ls.x, Ls.y, Ls.z, 0.f);
+        hitCode = __float_as_int(r0.w) * 2;
       }
-      const TraceItem& it = items[lo];
-      traceWarp(it.s, it.g, it.f, it.lattice, it.order, it.atlasPrev, it.rayRad, it.rayDir, it.rayHit, err,
-                w - it.warpBegin, lane);
-      __syncwarp();
+      // stores (rgen:108-109)
+      const size_t idx = rayIndex(g, rs);
+      T.rayRad[idx] = make_float4(L.x, L.y, L.z, 1.0f);
+      if (T.rayDir) T.rayDir[idx] = make_float4(dir.x, dir.y, dir.z, 1.0f);
+      if (T.rayHit) T.rayHit[idx] = hitCode;
+      if (g.rad16) storeRad16(g, rs, L);
+    }
+    // append the shadow rays of this warp's slots with one atomic
+    const unsigned act = __activemask();
+    const unsigned want = __ballot_sync(act, cast);
+    if (want) {
+      const int leader = __ffs(act) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&counters[1], (unsigned long long)__popc(want));
+      base = __shfl_sync(act, base, leader);
+      if (cast) shadowList[base + __popc(want & below)] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)id));
+    }
+  }
+}
+
+// Shadow rays (rchit:155-176): any hit in [0.1, 50] toward the sun; a shadowed ray's radiance becomes the
+// shadowed value the shading pass parked in its hit record, and its hit code gets the shadow bit.
+template <bool kWide>
+__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+    k_trace_shadow(const TraceItem* __restrict__ items, int numItems, const float4* __restrict__ shadowList,
+                   unsigned long long* __restrict__ counters, int refillLanes, const float4* __restrict__ hits,
+                   uint32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const long long total = (long long)counters[1];
+  long long id = -1;
+  int item = 0;
+  bool drained = total == 0;
+  BvhRef bvh;
+  WRay ray;
+  HitInfo hit;
+  typename TravOf<kWide>::T st;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, id < 0);
+    if (drained && idle == 0xffffffffu) break;
+    bool finished = false;
+    if (!drained && __popc(idle) >= refillLanes) {
+      const int need = __popc(idle);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&counters[2], (unsigned long long)need);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((long long)base + need >= total) drained = true;
+      const long long k = (long long)base + __popc(idle & below);
+      if (id < 0 && k < total) {
+        const float4 rec = shadowList[k];
+        id = (long long)__float_as_uint(rec.w);
+        item = findItem(items, numItems, id >> 5);
+        const TraceItem& T = items[item];
+        const bool lightSpace = T.s.shadow.tris != nullptr;
+        bvh = lightSpace ? T.s.shadow : T.s.bvh;
+        ray = makeRay(xyz(rec), lightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
+        finished = travInit<kWide, true>(bvh, ray, st, hit);
+      }
+    }
+    if (id >= 0 && !finished) finished = travStep<kWide, true>(bvh, ray, st, hit, err);
+    if (id >= 0 && finished) {
+      if (hit.leaf >= 0) {
+        const TraceItem& T = items[item];
+        const RaySlot rs = raySlot(T.g, T.f, T.order, (id >> 5) - T.warpBegin, (int)(id & 31));
+        const float3 Ls = xyz(hits[id]);
+        const size_t idx = rayIndex(T.g, rs);
+        T.rayRad[idx] = make_float4(Ls.x, Ls.y, Ls.z, 1.0f);
+        if (T.rayHit) T.rayHit[idx] |= 1;
+        if (T.g.rad16) storeRad16(T.g, rs, Ls);
+      }
+      id = -1;
     }
   }
 }
@@ -455,14 +462,30 @@ long long traceWarps(const GridGPU& g, const FrameGPU& f) {
 }
 
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
-                             unsigned long long* dQueue, int blocks, int warpsPerFetch, uint32_t* err,
-                             cudaStream_t stream) {
-  cudaError_t e = cudaMemsetAsync(dQueue, 0, sizeof(unsigned long long), stream);
+                             unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
+                             int refillLanes, bool wide, uint32_t* err, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(dCounters, 0, kTraceCounters * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   dim3 lg((maxN + 127) / 128, numItems);
   k_lattice_batch<<<lg, 128, 0, stream>>>(dItems, dRots);
-  if (totalWarps > 0)
-    k_trace_batch<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, totalWarps, dQueue, warpsPerFetch, err);
+  if (totalWarps <= 0) return cudaGetLastError();
+  const long long rays = totalWarps * 32;
+  if (rays > 0xffffffffll) return cudaErrorInvalidValue;  // shadow records carry 32-bit slot ids
+  const int refill = refillLanes < 1 ? 1 : (refillLanes > 32 ? 32 : refillLanes);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long shadeBlocks = (rays + 255) / 256;
+  if (shadeBlocks > (long long)sms * 16) shadeBlocks = (long long)sms * 16;
+  if (wide) {
+    k_trace_closest<true><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits, err);
+    k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
+    k_trace_shadow<true><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
+  } else {
+    k_trace_closest<false><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits, err);
+    k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
+    k_trace_shadow<false><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
+  }
   return cudaGetLastError();
 }
 

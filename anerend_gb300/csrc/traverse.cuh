@@ -1,0 +1,337 @@
+// Ray traversal shared by the device kernels and host builds of this header (CPU tests):
+//   - the watertight ray/triangle test (Woop, Benthin, Wald 2013, "Watertight Ray/Triangle Intersection")
+//   - the conservative slab test (Ize 2013, "Robust BVH Ray Traversal")
+//   - traversal of the binary LBVH (Aila-Laine node layout) and of the 8-wide BVH collapsed from it
+// Closest hit: smallest t, ties to the lowest global triangle id. Any hit: the first triangle in range.
+// Both traversals visit every triangle whose box the conservative slab test accepts, so they return the
+// same closest hit whatever the tree shape. Replaces the RT-core traceRayEXT calls of the reference
+// (irradiance_probe_update.rgen:96-106, .rchit:55-66).
+#pragma once
+
+#include <limits.h>
+#include <string.h>
+#include "ddgi_common.cuh"
+
+namespace ddgi {
+
+#ifdef __CUDA_ARCH__
+DDGI_D float mulRn(float a, float b) { return __fmul_rn(a, b); }
+DDGI_D float subRn(float a, float b) { return __fsub_rn(a, b); }
+DDGI_D float divRn(float a, float b) { return __fdiv_rn(a, b); }
+template <class T> DDGI_D T ldRo(const T* p) { return __ldg(p); }
+DDGI_D int asInt(float f) { return __float_as_int(f); }
+DDGI_D uint32_t asUint(float f) { return __float_as_uint(f); }
+DDGI_D int lowestBit(uint32_t m) { return __ffs(m) - 1; }
+DDGI_D int popc(uint32_t m) { return __popc(m); }
+DDGI_D void flagError(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
+#else
+// host builds must compile with -ffp-contract=off so products and differences round separately
+inline float mulRn(float a, float b) { return a * b; }
+inline float subRn(float a, float b) { return a - b; }
+inline float divRn(float a, float b) { return a / b; }
+template <class T> inline T ldRo(const T* p) { return *p; }
+inline int asInt(float f) { int i; memcpy(&i, &f, 4); return i; }
+inline uint32_t asUint(float f) { uint32_t i; memcpy(&i, &f, 4); return i; }
+inline int lowestBit(uint32_t m) { return __builtin_ctz(m); }
+inline int popc(uint32_t m) { return __builtin_popcount(m); }
+inline void flagError(uint32_t* err, uint32_t bits) { if (err) *err |= bits; }
+#endif
+
+struct WRay {
+  float3 o, d, invd;
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+DDGI_HD WRay makeRay(float3 o, float3 d) {
+  WRay r;
+  r.o = o;
+  r.d = d;
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1; if (kx == 3) kx = 0;
+  int ky = kx + 1; if (ky == 3) ky = 0;
+  float dz = get(d, kz);
+  if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
+  r.kx = kx; r.ky = ky; r.kz = kz;
+  r.Sx = get(d, kx) / dz;
+  r.Sy = get(d, ky) / dz;
+  r.Sz = 1.0f / dz;
+  // box-test reciprocals; a zero component becomes a tiny same-signed value so (lo - o) * invd is finite
+  float3 dd = f3(d.x != 0.f ? d.x : copysignf(1e-20f, d.x), d.y != 0.f ? d.y : copysignf(1e-20f, d.y),
+                 d.z != 0.f ? d.z : copysignf(1e-20f, d.z));
+  r.invd = f3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
+  return r;
+}
+
+// Returns true for a hit with tmin <= t <= tmax; b1, b2 are the weights of v1, v2. Products and
+// differences of the edge functions are not contracted into FMAs, so a shared edge evaluates to the same
+// value (with opposite sign) from both of its triangles.
+DDGI_HD bool intersectTri(const WRay& r, float3 v0, float3 v1, float3 v2, float tmin, float tmax, float& t,
+                          float& b1, float& b2) {
+  float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+  float Akz = get(A, r.kz), Bkz = get(B, r.kz), Ckz = get(C, r.kz);
+  float Ax = subRn(get(A, r.kx), mulRn(r.Sx, Akz));
+  float Ay = subRn(get(A, r.ky), mulRn(r.Sy, Akz));
+  float Bx = subRn(get(B, r.kx), mulRn(r.Sx, Bkz));
+  float By = subRn(get(B, r.ky), mulRn(r.Sy, Bkz));
+  float Cx = subRn(get(C, r.kx), mulRn(r.Sx, Ckz));
+  float Cy = subRn(get(C, r.ky), mulRn(r.Sy, Ckz));
+  float U = subRn(mulRn(Cx, By), mulRn(Cy, Bx));
+  float V = subRn(mulRn(Ax, Cy), mulRn(Ay, Cx));
+  float W = subRn(mulRn(Bx, Ay), mulRn(By, Ax));
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {  // exact fallback of the paper
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  float det = U + V + W;
+  if (det == 0.0f) return false;
+  float Az = mulRn(r.Sz, Akz), Bz = mulRn(r.Sz, Bkz), Cz = mulRn(r.Sz, Ckz);
+  float T = U * Az + V * Bz + W * Cz;
+  float tt = divRn(T, det);
+  if (!(tt >= tmin && tt <= tmax)) return false;
+  float inv = divRn(1.0f, det);
+  t = tt;
+  b1 = V * inv;
+  b2 = W * inv;
+  return true;
+}
+
+// Slab test with a conservative far distance (Ize 2013: 1 + 2*gamma(3)).
+DDGI_HD bool slab(const WRay& r, float lx, float hx, float ly, float hy, float lz, float hz, float tmin,
+                  float tmax, float& tnear) {
+  float t0x = (lx - r.o.x) * r.invd.x, t1x = (hx - r.o.x) * r.invd.x;
+  float t0y = (ly - r.o.y) * r.invd.y, t1y = (hy - r.o.y) * r.invd.y;
+  float t0z = (lz - r.o.z) * r.invd.z, t1z = (hz - r.o.z) * r.invd.z;
+  float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+  tnear = tn;
+  return tn <= tf * 1.0000004f;
+}
+
+struct HitInfo {
+  int leaf;  // triangle record index
+  int gid;   // global triangle id
+  float t, b1, b2;
+};
+
+// Test one triangle record; returns true when an any-hit query can stop.
+template <bool kAnyHit>
+DDGI_HD bool testTri(const BvhRef& b, const WRay& r, int rec, float tmin, HitInfo& hit) {
+  float4 a = ldRo(&b.tris[3 * rec]), c1 = ldRo(&b.tris[3 * rec + 1]), c2 = ldRo(&b.tris[3 * rec + 2]);
+  float t, b1, b2;
+  if (intersectTri(r, xyz(a), xyz(c1), xyz(c2), tmin, hit.t, t, b1, b2)) {
+    int g = asInt(a.w);
+    if (kAnyHit) {
+      hit.leaf = rec; hit.gid = g; hit.t = t; hit.b1 = b1; hit.b2 = b2;
+      return true;
+    }
+    if (t < hit.t || (t == hit.t && g < hit.gid)) {
+      hit.leaf = rec; hit.gid = g; hit.t = t; hit.b1 = b1; hit.b2 = b2;
+    }
+  }
+  return false;
+}
+
+// ---- binary BVH ------------------------------------------------------------------------------------
+// Resumable traversal: init, then step until it returns true. One step visits one node (its two child
+// boxes, and the triangles of its leaf children). The persistent kernels interleave steps with refills
+// of idle lanes; traverse() runs the steps to the end.
+struct BinTrav {
+  int node, sp;
+  int stack[kStackSize];
+};
+
+// Returns true when there is nothing to traverse (no triangles, or a single triangle, tested here).
+template <bool kAnyHit>
+DDGI_HD bool binInit(const BvhRef& b, const WRay& r, float tmin, float tmax, BinTrav& s, HitInfo& hit) {
+  hit.leaf = -1;
+  hit.gid = INT_MAX;
+  hit.t = tmax;
+  s.node = 0;
+  s.sp = 0;
+  if (b.numTris <= 0) return true;
+  if (b.numTris == 1) {
+    testTri<kAnyHit>(b, r, 0, tmin, hit);
+    return true;
+  }
+  return false;
+}
+
+template <bool kAnyHit>
+DDGI_HD bool binStep(const BvhRef& b, const WRay& r, float tmin, BinTrav& s, HitInfo& hit, uint32_t* err) {
+  if ((unsigned)s.node >= (unsigned)b.numNodes) {
+    flagError(err, DDGI_DEVERR_BOUNDS);
+    return true;
+  }
+  const float4* nd = b.nodes + 4 * s.node;
+  float4 n0 = ldRo(nd), n1 = ldRo(nd + 1), n2 = ldRo(nd + 2), n3 = ldRo(nd + 3);
+  float tn0, tn1;
+  bool h0 = slab(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tmin, hit.t, tn0);
+  bool h1 = slab(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tmin, hit.t, tn1);
+  int c0 = asInt(n3.x), c1 = asInt(n3.y);
+  if (h0 && c0 < 0) {
+    if (testTri<kAnyHit>(b, r, ~c0, tmin, hit) && kAnyHit) return true;
+    h0 = false;
+  }
+  if (h1 && c1 < 0) {
+    if (testTri<kAnyHit>(b, r, ~c1, tmin, hit) && kAnyHit) return true;
+    h1 = false;
+  }
+  if (h0 && h1) {
+    int nearC = c0, farC = c1;
+    if (tn1 < tn0) { nearC = c1; farC = c0; }
+    if (s.sp >= kStackSize) {  // cannot happen for trees of depth <= 64; flag and stop this ray
+      flagError(err, DDGI_DEVERR_STACK_OVERFLOW);
+      return true;
+    }
+    s.stack[s.sp++] = farC;
+    s.node = nearC;
+  } else if (h0) {
+    s.node = c0;
+  } else if (h1) {
+    s.node = c1;
+  } else {
+    if (s.sp == 0) return true;
+    s.node = s.stack[--s.sp];
+  }
+  return false;
+}
+
+template <bool kAnyHit>
+DDGI_HD bool traverse(const BvhRef& b, const WRay& r, float tmin, float tmax, HitInfo& hit, uint32_t* err) {
+  BinTrav s;
+  if (!binInit<kAnyHit>(b, r, tmin, tmax, s, hit))
+    while (!binStep<kAnyHit>(b, r, tmin, s, hit, err)) {
+    }
+  return hit.leaf >= 0;
+}
+
+// ---- 8-wide BVH -------------------------------------------------------------------------------------
+// Node = 13 float4 (208 B):
+//   [0]      uint4 {childBase, triBase, meta of slots 0-3, meta of slots 4-7} (meta: one byte per slot)
+//   [1],[2]  lo.x of slots 0-7      [3],[4]   hi.x      [5],[6]  lo.y   [7],[8]  hi.y
+//   [9],[10] lo.z                    [11],[12] hi.z
+// meta byte: 0 = empty slot; (7 << 5) | k = internal child, wide node childBase + k (k = rank of the slot
+// among the node's internal slots); (c << 5) | o with c in 1..kWideLeafMax = leaf of c triangle records
+// starting at triBase + o. Slot s holds the child that lies most toward the corner with sign bits s (bit a
+// set = +axis a), so visiting keys s ^ octant(ray) in increasing order is roughly front to back.
+constexpr int kWideNodeF4 = 13;
+constexpr int kWideLeafMax = 1;
+constexpr int kWideStack = 64;
+
+struct WideTrav {
+  int node, sp;
+  uint32_t oct;
+  uint2 stack[kWideStack];  // {childBase, (internal-slot mask << 8) | remaining keys}
+};
+
+template <bool kAnyHit>
+DDGI_HD bool wideInit(const BvhRef& b, const WRay& r, float tmax, WideTrav& s, HitInfo& hit) {
+  hit.leaf = -1;
+  hit.gid = INT_MAX;
+  hit.t = tmax;
+  s.node = 0;
+  s.sp = 0;
+  s.oct = (r.invd.x < 0.f ? 1u : 0u) | (r.invd.y < 0.f ? 2u : 0u) | (r.invd.z < 0.f ? 4u : 0u);
+  return b.numTris <= 0;
+}
+
+template <bool kAnyHit>
+DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, HitInfo& hit, uint32_t* err) {
+  if ((unsigned)s.node >= (unsigned)b.numWNodes) {
+    flagError(err, DDGI_DEVERR_BOUNDS);
+    return true;
+  }
+  const uint32_t oct = s.oct;
+  // near / far plane rows of each axis for this ray's direction signs
+  const int nxo = (oct & 1) ? 3 : 1, fxo = 4 - nxo;
+  const int nyo = (oct & 2) ? 7 : 5, fyo = 12 - nyo;
+  const int nzo = (oct & 4) ? 11 : 9, fzo = 20 - nzo;
+  const float4* nd = b.wnodes + kWideNodeF4 * s.node;
+  const uint4 hd = ldRo(reinterpret_cast<const uint4*>(nd));
+  uint32_t ihits = 0, imask = 0, lhits = 0;
+  // two halves of four slots each: six float4 of planes per half keep the register footprint small
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float4 nx = ldRo(nd + nxo + h), fx = ldRo(nd + fxo + h);
+    const float4 ny = ldRo(nd + nyo + h), fy = ldRo(nd + fyo + h);
+    const float4 nz = ldRo(nd + nzo + h), fz = ldRo(nd + fzo + h);
+    const uint32_t mh = h ? hd.w : hd.z;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = 4 * h + q;
+      const uint32_t m = (mh >> (8 * q)) & 0xffu;
+      const float pnx = q == 0 ? nx.x : q == 1 ? nx.y : q == 2 ? nx.z : nx.w;
+      const float pfx = q == 0 ? fx.x : q == 1 ? fx.y : q == 2 ? fx.z : fx.w;
+      const float pny = q == 0 ? ny.x : q == 1 ? ny.y : q == 2 ? ny.z : ny.w;
+      const float pfy = q == 0 ? fy.x : q == 1 ? fy.y : q == 2 ? fy.z : fy.w;
+      const float pnz = q == 0 ? nz.x : q == 1 ? nz.y : q == 2 ? nz.z : nz.w;
+      const float pfz = q == 0 ? fz.x : q == 1 ? fz.y : q == 2 ? fz.z : fz.w;
+      // near/far distances per axis: (plane - o) * invd, each rounded as in the slab test above
+      const float tn = fmaxf(fmaxf((pnx - r.o.x) * r.invd.x, (pny - r.o.y) * r.invd.y),
+                             fmaxf((pnz - r.o.z) * r.invd.z, tmin));
+      const float tf = fminf(fminf((pfx - r.o.x) * r.invd.x, (pfy - r.o.y) * r.invd.y),
+                             fminf((pfz - r.o.z) * r.invd.z, hit.t));
+      const bool internal = (m >> 5) == 7u;
+      imask |= (internal ? 1u : 0u) << c;
+      if (m != 0u && tn <= tf * 1.0000004f) {
+        if (internal) ihits |= 1u << (c ^ oct);
+        else lhits |= 1u << c;
+      }
+    }
+  }
+  const uint32_t triBase = hd.y;
+  while (lhits) {
+    const int c = lowestBit(lhits);
+    lhits &= lhits - 1u;
+    const uint32_t m = ((c < 4 ? hd.z : hd.w) >> (8 * (c & 3))) & 0xffu;
+    const int first = (int)(triBase + (m & 31u)), cnt = (int)(m >> 5);
+    if (first + cnt > b.numTris) {
+      flagError(err, DDGI_DEVERR_BOUNDS);
+      return true;
+    }
+    for (int k = 0; k < cnt; ++k)
+      if (testTri<kAnyHit>(b, r, first + k, tmin, hit) && kAnyHit) return true;
+  }
+  if (ihits) {
+    // descend into the nearest-keyed internal child, keep the rest of this node's hits on the stack
+    const int key = lowestBit(ihits);
+    ihits &= ihits - 1u;
+    const uint32_t slot = (uint32_t)key ^ oct;
+    const int next = (int)(hd.x + (uint32_t)popc(imask & ((1u << slot) - 1u)));
+    if (ihits) {
+      if (s.sp >= kWideStack) {
+        flagError(err, DDGI_DEVERR_STACK_OVERFLOW);
+        return true;
+      }
+      s.stack[s.sp++] = make_uint2(hd.x, (imask << 8) | ihits);
+    }
+    s.node = next;
+    return false;
+  }
+  if (s.sp == 0) return true;
+  uint2& top = s.stack[s.sp - 1];
+  uint32_t keys = top.y & 0xffu;
+  const uint32_t tim = top.y >> 8;
+  const int key = lowestBit(keys);
+  keys &= keys - 1u;
+  const uint32_t slot = (uint32_t)key ^ oct;
+  s.node = (int)(top.x + (uint32_t)popc(tim & ((1u << slot) - 1u)));
+  if (keys) top.y = (tim << 8) | keys;
+  else --s.sp;
+  return false;
+}
+
+template <bool kAnyHit>
+DDGI_HD bool traverseWide(const BvhRef& b, const WRay& r, float tmin, float tmax, HitInfo& hit, uint32_t* err) {
+  WideTrav s;
+  if (!wideInit<kAnyHit>(b, r, tmax, s, hit))
+    while (!wideStep<kAnyHit>(b, r, tmin, s, hit, err)) {
+    }
+  return hit.leaf >= 0;
+}
+
+}  // namespace ddgi

@@ -1,0 +1,234 @@
+// Collapse of the binary LBVH into the 8-wide BVH that traverseWide reads (node layout in traverse.cuh).
+// Host code, run once per built BVH; the binary tree comes from the device build.
+//
+// Each wide node starts from one binary subtree and repeatedly opens the open child (subtree of more
+// than kWideLeafMax triangles) with the largest surface area until it has 8 children or none is left to
+// open. Children of at most kWideLeafMax triangles become leaves; their triangle records are laid out
+// contiguously per wide node (triBase + offset); larger children become wide nodes, numbered in
+// breadth-first order so the internal children of a node are consecutive (childBase + rank). Children are
+// placed in slots by a greedy octant assignment (slot s = the child lying most toward the corner with
+// sign bits s). The method follows the greedy variant of Ylitie, Karras, Laine 2017 ("Efficient
+// incoherent ray traversal on GPUs through compressed wide BVHs"), with uncompressed FP32 child boxes.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "traverse.cuh"
+
+namespace ddgi {
+namespace wbvh {
+
+struct Box {
+  float lo[3], hi[3];
+};
+
+inline float area(const Box& b) {
+  float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+inline Box merge(const Box& a, const Box& b) {
+  Box r;
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = std::min(a.lo[k], b.lo[k]);
+    r.hi[k] = std::max(a.hi[k], b.hi[k]);
+  }
+  return r;
+}
+
+inline int asIntH(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+inline float asFloatH(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+
+struct Cand {
+  int ref;    // binary child id: >= 0 internal node, < 0 triangle record ~ref
+  Box box;
+  int count;  // triangles below
+};
+
+// nodes2: numTris - 1 binary nodes (4 float4 each, root 0; none when numTris == 1); tris: numTris records.
+// Output: wide nodes (kWideNodeF4 float4 each, root 0) and `order` (new record index -> old record index).
+// Returns false only for numTris <= 0.
+inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std::vector<float4>& out,
+                     std::vector<int>& order) {
+  out.clear();
+  order.clear();
+  if (numTris <= 0) return false;
+  const int numNodes2 = numTris - 1;
+  auto childOf = [&](int node, int k) { return asIntH(k == 0 ? nodes2[4 * node + 3].x : nodes2[4 * node + 3].y); };
+  auto childBox = [&](int node, int k) {
+    const float4 a = nodes2[4 * node + k], z = nodes2[4 * node + 2];
+    Box b;
+    b.lo[0] = a.x; b.hi[0] = a.y; b.lo[1] = a.z; b.hi[1] = a.w;
+    b.lo[2] = k == 0 ? z.x : z.z;
+    b.hi[2] = k == 0 ? z.y : z.w;
+    return b;
+  };
+  auto triBox = [&](int rec) {
+    Box b;
+    const float4 v[3] = {tris[3 * rec], tris[3 * rec + 1], tris[3 * rec + 2]};
+    for (int k = 0; k < 3; ++k) {
+      float c0 = k == 0 ? v[0].x : (k == 1 ? v[0].y : v[0].z);
+      float c1 = k == 0 ? v[1].x : (k == 1 ? v[1].y : v[1].z);
+      float c2 = k == 0 ? v[2].x : (k == 1 ? v[2].y : v[2].z);
+      b.lo[k] = std::min(c0, std::min(c1, c2));
+      b.hi[k] = std::max(c0, std::max(c1, c2));
+    }
+    return b;
+  };
+
+  // triangle counts of the binary subtrees (iterative post-order)
+  std::vector<int> count(numNodes2 > 0 ? numNodes2 : 1, 0);
+  if (numNodes2 > 0) {
+    std::vector<std::pair<int, int>> st;  // (node, state)
+    st.push_back({0, 0});
+    while (!st.empty()) {
+      auto& top = st.back();
+      const int n = top.first;
+      if (top.second == 0) {
+        top.second = 1;
+        for (int k = 0; k < 2; ++k) {
+          int c = childOf(n, k);
+          if (c >= 0) st.push_back({c, 0});
+        }
+      } else {
+        int s = 0;
+        for (int k = 0; k < 2; ++k) {
+          int c = childOf(n, k);
+          s += c >= 0 ? count[c] : 1;
+        }
+        count[n] = s;
+        st.pop_back();
+      }
+    }
+  }
+  auto cand = [&](int parent, int k) {
+    Cand c;
+    c.ref = childOf(parent, k);
+    c.box = childBox(parent, k);
+    c.count = c.ref >= 0 ? count[c.ref] : 1;
+    return c;
+  };
+  auto gather = [&](const Cand& c, std::vector<int>& recs) {  // triangle records below a candidate
+    std::vector<int> st{c.ref};
+    while (!st.empty()) {
+      int r = st.back();
+      st.pop_back();
+      if (r < 0) { recs.push_back(~r); continue; }
+      st.push_back(childOf(r, 1));
+      st.push_back(childOf(r, 0));
+    }
+  };
+
+  struct Job {
+    std::vector<Cand> kids;  // the children of the wide node before opening
+    int index;
+  };
+  std::vector<Job> queue;
+  {
+    Job root;
+    root.index = 0;
+    if (numNodes2 == 0) {
+      root.kids.push_back(Cand{~0, triBox(0), 1});
+    } else {
+      root.kids.push_back(cand(0, 0));
+      root.kids.push_back(cand(0, 1));
+    }
+    queue.push_back(root);
+  }
+  out.resize(kWideNodeF4);
+  int numWide = 1;
+  for (size_t qi = 0; qi < queue.size(); ++qi) {
+    std::vector<Cand> kids = std::move(queue[qi].kids);
+    const int index = queue[qi].index;
+    // open the largest open child while slots remain
+    while ((int)kids.size() < 8) {
+      int best = -1;
+      float bestA = -1.0f;
+      for (int i = 0; i < (int)kids.size(); ++i) {
+        if (kids[i].ref >= 0 && kids[i].count > kWideLeafMax && area(kids[i].box) > bestA) {
+          best = i;
+          bestA = area(kids[i].box);
+        }
+      }
+      if (best < 0) break;
+      const int r = kids[best].ref;
+      kids[best] = cand(r, 0);
+      kids.push_back(cand(r, 1));
+    }
+    // octant slots: greedy on the score dot(centre_i - centre_node, corner_s)
+    const int nk = (int)kids.size();
+    Box nb = kids[0].box;
+    for (int i = 1; i < nk; ++i) nb = merge(nb, kids[i].box);
+    float nc[3];
+    for (int a = 0; a < 3; ++a) nc[a] = 0.5f * (nb.lo[a] + nb.hi[a]);
+    int slotOf[8], kidOf[8];
+    for (int s = 0; s < 8; ++s) kidOf[s] = -1;
+    for (int i = 0; i < nk; ++i) slotOf[i] = -1;
+    for (int step = 0; step < nk; ++step) {
+      float bestS = -3.0e38f;
+      int bi = -1, bs = -1;
+      for (int i = 0; i < nk; ++i) {
+        if (slotOf[i] >= 0) continue;
+        float d[3];
+        for (int a = 0; a < 3; ++a) d[a] = 0.5f * (kids[i].box.lo[a] + kids[i].box.hi[a]) - nc[a];
+        for (int s = 0; s < 8; ++s) {
+          if (kidOf[s] >= 0) continue;
+          float sc = ((s & 1) ? d[0] : -d[0]) + ((s & 2) ? d[1] : -d[1]) + ((s & 4) ? d[2] : -d[2]);
+          if (sc > bestS) { bestS = sc; bi = i; bs = s; }
+        }
+      }
+      slotOf[bi] = bs;
+      kidOf[bs] = bi;
+    }
+    // leaves: records laid out per node in slot order; internal children: consecutive wide nodes
+    const uint32_t triBase = (uint32_t)order.size();
+    const int childBase = numWide;
+    uint8_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int rank = 0;
+    for (int s = 0; s < 8; ++s) {
+      const int i = kidOf[s];
+      if (i < 0) continue;
+      if (kids[i].count <= kWideLeafMax) {
+        const uint32_t off = (uint32_t)order.size() - triBase;
+        std::vector<int> recs;
+        gather(kids[i], recs);
+        for (int rec : recs) order.push_back(rec);
+        meta[s] = (uint8_t)(((uint32_t)recs.size() << 5) | off);
+      } else {
+        meta[s] = (uint8_t)((7u << 5) | (uint32_t)rank);
+        Job j;
+        j.index = childBase + rank;
+        j.kids.push_back(cand(kids[i].ref, 0));
+        j.kids.push_back(cand(kids[i].ref, 1));
+        queue.push_back(std::move(j));
+        ++rank;
+      }
+    }
+    numWide += rank;
+    out.resize((size_t)numWide * kWideNodeF4);
+    float4* nd = out.data() + (size_t)index * kWideNodeF4;
+    uint32_t m0 = 0, m1 = 0;
+    for (int s = 0; s < 4; ++s) m0 |= (uint32_t)meta[s] << (8 * s);
+    for (int s = 0; s < 4; ++s) m1 |= (uint32_t)meta[4 + s] << (8 * s);
+    nd[0] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
+    float pl[6][8];
+    for (int s = 0; s < 8; ++s) {
+      const int i = kidOf[s];
+      for (int a = 0; a < 3; ++a) {
+        pl[2 * a][s] = i >= 0 ? kids[i].box.lo[a] : 0.0f;
+        pl[2 * a + 1][s] = i >= 0 ? kids[i].box.hi[a] : 0.0f;
+      }
+    }
+    for (int p = 0; p < 6; ++p) {
+      nd[1 + 2 * p] = make_float4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
+      nd[2 + 2 * p] = make_float4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
+    }
+  }
+  return (int)order.size() == numTris;
+}
+
+}  // namespace wbvh
+}  // namespace ddgi

@@ -136,7 +136,8 @@ class ProbeGrid:
         return t
 
     def set_tuning(self, warp_probes: int | None = None, ray_order: int | None = None,
-                   shadow_mode: int | None = None, conv_mode: int | None = None) -> None:
+                   shadow_mode: int | None = None, conv_mode: int | None = None,
+                   bvh_width: int | None = None) -> None:
         t = self.tuning
         if warp_probes is not None:
             t.warpProbes = warp_probes
@@ -146,6 +147,8 @@ class ProbeGrid:
             t.shadowMode = shadow_mode
         if conv_mode is not None:
             t.convMode = conv_mode
+        if bvh_width is not None:
+            t.bvhWidth = bvh_width
         self.ctx.check(self.ctx.lib.ddgi_grid_set_tuning(self.handle, C.byref(t)))
 
     def reset(self, stream: int = 0) -> None:
@@ -247,8 +250,8 @@ class Batch:
     def set_tuning(self, **kw) -> None:
         t = self.tuning
         names = {"warp_probes": "warpProbes", "ray_order": "rayOrder", "shadow_mode": "shadowMode",
-                 "conv_mode": "convMode", "blocks_per_sm": "blocksPerSm", "warps_per_fetch": "warpsPerFetch",
-                 "use_graph": "useGraph"}
+                 "conv_mode": "convMode", "blocks_per_sm": "blocksPerSm", "refill_lanes": "refillLanes",
+                 "use_graph": "useGraph", "bvh_width": "bvhWidth"}
         for k, v in kw.items():
             setattr(t, names.get(k, k), int(v))
         self.ctx.check(self.ctx.lib.ddgi_batch_set_tuning(self.handle, C.byref(t)))

@@ -277,7 +277,7 @@ def measure_precision(ctx, stream):
 
 
 
-def measure_forms(ctx, scene, w, stream, only=None):
+def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
     """The other forms of the path, each bounded to a few seconds: the plain single-grid FP32 form and the
     tensor-core convolution on the same workload, the tensor-core convolution of the 65,536-probe / 512-ray
     precision workload, the 64-grid batched workload against its plain form, and a short serving run."""
@@ -301,9 +301,11 @@ def measure_forms(ctx, scene, w, stream, only=None):
     def frames1(f):
         return ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f))
 
-    for name, tun in (("plain_fp32", dict(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0)),
-                      ("tuned_fp32", dict(shadow_mode=1, ray_order=1, warp_probes=2, conv_mode=0)),
-                      ("tuned_tc_bf16", dict(shadow_mode=1, ray_order=1, warp_probes=2, conv_mode=2))):
+    tuned = dict(shadow_mode=1, ray_order=1, warp_probes=2, bvh_width=bvh_width)
+    for name, tun in (("plain_fp32", dict(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0, bvh_width=2)),
+                      ("tuned_fp32", dict(tuned, conv_mode=0)),
+                      ("tuned_tc_fp16", dict(tuned, conv_mode=1)),
+                      ("tuned_tc_bf16", dict(tuned, conv_mode=2))):
         g.set_tuning(**tun)
         ms = _time_updates(torch, single, frames1, 5)
         out[f"single_grid_{name}"] = {"ms_per_update": ms, "rays_per_s": rays / ms * 1e3}
@@ -325,7 +327,7 @@ def measure_forms(ctx, scene, w, stream, only=None):
         return [ddgi.FrameParams(camera_pos=sp.camera, rotation=scenes.rotation(i, f)) for i, sp in enumerate(specs)]
 
     for gg in grids:
-        gg.set_tuning(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0)
+        gg.set_tuning(shadow_mode=0, ray_order=0, warp_probes=32, conv_mode=0, bvh_width=2)
 
     def plain(fr):
         for (gg, sc), fp in zip(items, fr):
@@ -335,9 +337,9 @@ def measure_forms(ctx, scene, w, stream, only=None):
     batch = ddgi.Batch(ctx, items)
     res_b = {"grids": len(specs), "scenes": len(tris), "triangles": sum(tris), "rays": brays,
              "plain_fp32_ms": plain_ms, "plain_fp32_rays_per_s": brays / plain_ms * 1e3}
-    for name, conv in (("batched_fp32", 0), ("batched_tc_bf16", 2)):
-        batch.set_tuning(conv_mode=conv, blocks_per_sm=8, warps_per_fetch=4, warp_probes=2, ray_order=1,
-                         shadow_mode=1, use_graph=1)
+    for name, conv in (("batched_fp32", 0), ("batched_tc_fp16", 1), ("batched_tc_bf16", 2)):
+        batch.set_tuning(conv_mode=conv, blocks_per_sm=8, refill_lanes=8, warp_probes=2, ray_order=1,
+                         shadow_mode=1, use_graph=1, bvh_width=bvh_width)
         ms = _time_updates(torch, lambda fr: batch.update(fr, stream), bframes, 4)
         res_b[f"{name}_ms"] = ms
         res_b[f"{name}_rays_per_s"] = brays / ms * 1e3
@@ -401,7 +403,7 @@ def run_ours(args, rank, local, world):
     probe_grid.close()
 
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
-    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0)  # FP32 throughout
+    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0, bvh_width=args.bvh_width)  # FP32
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     rays_per_step = w.probes * w.rays
 
@@ -433,7 +435,7 @@ def run_ours(args, rank, local, world):
         e[2].record()
         grid.convolve(fp, stream)
         e[3].record()
-        launches += 4 + (1 if moved else 0)  # lattice, trace, weights, convolve (+ translate)
+        launches += 6 + (1 if moved else 0)  # lattice, closest hit, shade, shadow, weights, convolve (+ translate)
         f += 1
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
@@ -482,7 +484,7 @@ def run_ours(args, rank, local, world):
                "sample": f"{frames} full probe updates ({frames * rays_per_step} rays), FP64 oracle, {dt:.1f} s"}
     forms = None
     if rank == 0 and world == 1 and not args.no_extras:
-        forms = measure_forms(ctx, scene, w, stream)
+        forms = measure_forms(ctx, scene, w, stream, bvh_width=args.bvh_width)
     if rank == 0:
         srt = sorted(step_ms)
         line = {
@@ -509,7 +511,8 @@ def run_ours(args, rank, local, world):
             "gpu_launches": launches,
             "clocks": clocks,
             "tuning": {"warpProbes": int(grid.tuning.warpProbes), "rayOrder": int(grid.tuning.rayOrder),
-                       "shadowMode": int(grid.tuning.shadowMode), "convMode": int(grid.tuning.convMode)},
+                       "shadowMode": int(grid.tuning.shadowMode), "convMode": int(grid.tuning.convMode),
+                       "bvhWidth": int(grid.tuning.bvhWidth)},
             "forms": forms,
         }
         print(json.dumps(line))
@@ -527,6 +530,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the other forms (batched, precision, serving)")
     ap.add_argument("--form", choices=["precision"], help="run only this form and print its measurements")
+    ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal tree (8-wide or binary)")
     args = ap.parse_args()
     rank, local, world = dist_init()
     if args.impl == "reference":

@@ -157,7 +157,9 @@ typedef struct DdgiTuning {
   int32_t convMode;     /* 0: FP32 convolution on CUDA cores (default); 1: tcgen05 tensor cores with FP16
                            radiance and weights; 2: tensor cores with BF16. Tensor-core modes need N % 64 == 0;
                            accumulation and the hysteresis blend stay FP32 */
-  int32_t reserved[4];
+  int32_t bvhWidth;     /* traversal tree: 8 = 8-wide BVH collapsed from the LBVH (default; 0 means 8);
+                           2 = the binary LBVH. Both give the same hits */
+  int32_t reserved[3];
 } DdgiTuning;
 
 /* Device views of the grid's buffers (owned by the grid). */
@@ -261,9 +263,10 @@ typedef struct DdgiBatchTuning {
   int32_t shadowMode;    /* as DdgiTuning.shadowMode (default 1) */
   int32_t convMode;      /* as DdgiTuning.convMode (default 0); tensor-core batches hold at most 64 items */
   int32_t blocksPerSm;   /* resident 128-thread blocks per SM of the persistent trace (1..8, default 8) */
-  int32_t warpsPerFetch; /* warps of work taken from the shared queue per atomic (1..64, default 4) */
+  int32_t refillLanes;   /* a warp of the persistent traversals takes new rays from the queue once this many of
+                            its 32 lanes are idle (1..32, default 8) */
   int32_t useGraph;      /* capture the launch sequence into a CUDA graph once its shape repeats (default 1) */
-  int32_t reserved;
+  int32_t bvhWidth;      /* as DdgiTuning.bvhWidth (default 8) */
 } DdgiBatchTuning;
 
 typedef struct DdgiBatchStats {

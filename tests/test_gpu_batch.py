@@ -72,7 +72,7 @@ def test_batch_round_robin_layers_and_tuning_changes(ctx):
             for (g, s), fp in zip(solo, fr):
                 g.update(s, fp)
             if f == 2:  # a tuning change drops the captured graph; results must not change
-                batch.set_tuning(blocks_per_sm=4, warps_per_fetch=16)
+                batch.set_tuning(blocks_per_sm=4, refill_lanes=16)
             batch.update(fr)
             ctx.sync()
             for (g1, _), (g2, _) in zip(solo, batched):

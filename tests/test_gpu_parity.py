@@ -156,6 +156,7 @@ def g_rows(og):
     dict(shadow_mode=1, ray_order=1, warp_probes=2),   # light-space shadow BVH, Morton direction order
     dict(shadow_mode=0, ray_order=0, warp_probes=32),  # scene-BVH shadow rays, 32 parallel rays per warp
     dict(shadow_mode=1, ray_order=0, warp_probes=1),
+    dict(shadow_mode=1, ray_order=1, warp_probes=2, bvh_width=2),  # the binary LBVH instead of the 8-wide tree
 ])
 def test_cpu_reference_workload_8_frames(ctx, tuning):
     w = scenes.CPU_REFERENCE
@@ -370,3 +371,39 @@ def test_single_grid_workload_translation_and_rays(ctx):
         osc.close()
         grid.close()
         scene.close()
+
+
+@pytest.mark.parametrize("shadow_mode", [0, 1])
+def test_bvh_widths_give_identical_rays(ctx, shadow_mode):
+    """The 8-wide BVH and the binary LBVH it is collapsed from return the same closest hit and shadow bit
+    for every ray, so the traced radiance is bit-identical (one layer of the 262,144-triangle workload)."""
+    w = scenes.SINGLE_GRID
+    scene = ddgi.Scene(ctx, scenes.build_scene(w))
+    grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=L.DDGI_GRID_RECORD_HITS)
+    try:
+        out = {}
+        for width in (8, 2):
+            grid.set_tuning(shadow_mode=shadow_mode, bvh_width=width)
+            assert grid.tuning.bvhWidth == width
+            fp = ddgi.FrameParams(camera_pos=scenes.camera(w, 0), rotation=scenes.rotation(w.seed, 0), layer=5)
+            grid.trace(scene, fp)
+            ctx.sync()
+            rad, hits, _ = grid.download_rays(hits=True)
+            out[width] = (rad.copy(), hits.copy())
+        rows = slice(5 * w.dims[2] * 16, 6 * w.dims[2] * 16)
+        assert np.array_equal(out[8][1][rows], out[2][1][rows])
+        assert np.array_equal(out[8][0][rows].view(np.uint32), out[2][0][rows].view(np.uint32))
+        assert (out[8][1][rows] >= 0).mean() > 0.5
+    finally:
+        grid.close()
+        scene.close()
+
+
+def test_bvh_width_is_validated(ctx):
+    grid = ddgi.ProbeGrid(ctx, (4, 2, 4), (1.0, 1.0, 1.0), 64, 0.0, 0.97)
+    try:
+        assert grid.tuning.bvhWidth == 8
+        with pytest.raises(L.DdgiError):
+            grid.set_tuning(bvh_width=4)
+    finally:
+        grid.close()
