@@ -79,7 +79,8 @@ class Frame(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("warpProbes", C.c_int32), ("rayOrder", C.c_int32), ("shadowMode", C.c_int32),
-                ("convMode", C.c_int32), ("bvhWidth", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("convMode", C.c_int32), ("bvhWidth", C.c_int32), ("refillLanes", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class BatchItem(C.Structure):

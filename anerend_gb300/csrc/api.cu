@@ -122,6 +122,7 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
   if (t.shadowMode != 0 && t.shadowMode != 1) return fail(ctx, DDGI_EINVAL, "shadowMode %d unknown", t.shadowMode);
   if (t.bvhWidth != 0 && t.bvhWidth != 2 && t.bvhWidth != 8)
     return fail(ctx, DDGI_EINVAL, "bvhWidth %d must be 2 or 8 (0 = 8)", t.bvhWidth);
+  if (t.refillLanes < 0 || t.refillLanes > 32) return fail(ctx, DDGI_EINVAL, "refillLanes %d not in [1, 32]", t.refillLanes);
   if (t.convMode < 0 || t.convMode > 2) return fail(ctx, DDGI_EINVAL, "convMode %d unknown", t.convMode);
   if (t.convMode != 0 && g->g.N % 64)
     return fail(ctx, DDGI_EINVAL, "tensor-core convolution needs raysPerProbe %% 64 == 0 (N = %d)", g->g.N);
@@ -140,6 +141,7 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
     CK(cudaMemcpy(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice), "ray order upload");
   g->tuning = t;
   if (g->tuning.bvhWidth == 0) g->tuning.bvhWidth = 8;
+  if (g->tuning.refillLanes == 0) g->tuning.refillLanes = 8;
   g->g.warpProbes = t.warpProbes;
   g->g.bvhWide = g->tuning.bvhWidth == 8 ? 1 : 0;
   return DDGI_OK;
@@ -635,7 +637,8 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   memcpy(rot.m, frame->rotation, sizeof(rot.m));
   CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
   CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, g->dHits, g->dShadow,
-                      ctx->numSms * 8, 8, g->tuning.bvhWidth != 2, ctx->dErr, st),
+                      ctx->numSms * 8, g->tuning.refillLanes, g->tuning.bvhWidth != 2, g->tuning.shadowMode == 1,
+                      ctx->dErr, st),
      "trace");
   g->tracedBegin = b;
   g->tracedEnd = e;

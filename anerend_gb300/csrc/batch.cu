@@ -119,7 +119,7 @@ int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long t
   DdgiContext* ctx = S->ctx;
   int blocks = ctx->numSms * t.blocksPerSm;
   CK(launchTraceBatch(S->dTrace(), S->dRots(), n, maxN, totalWarps, S->dQueue, S->dHits, S->dShadow, blocks,
-                      t.refillLanes, t.bvhWidth != 2, ctx->dErr, st),
+                      t.refillLanes, t.bvhWidth != 2, t.shadowMode == 1, ctx->dErr, st),
      "batched trace");
   if (t.convMode != 0) {
     int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
@@ -287,6 +287,7 @@ int tuneGridForBatch(DdgiGrid* g, const DdgiBatchTuning& t) {
   gt.shadowMode = t.shadowMode;
   gt.convMode = t.convMode;
   gt.bvhWidth = t.bvhWidth;
+  gt.refillLanes = t.refillLanes;
   return applyTuning(g, gt);
 }
 

@@ -36,7 +36,7 @@ constexpr size_t kTraceScratchPerRay = 32;
 // closest-hit traversal, shading, shadow traversal. dHits and dShadow hold 32 * totalWarps float4 each.
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
-                             int refillLanes, bool wide, uint32_t* err, cudaStream_t stream);
+                             int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream);
 
 
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.

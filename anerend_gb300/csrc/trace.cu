@@ -213,9 +213,9 @@ DDGI_D bool travInit(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& 
   if constexpr (kWide) return wideInit<kAnyHit>(b, r, kTMax, s, hit);
   else return binInit<kAnyHit>(b, r, kTMin, kTMax, s, hit);
 }
-template <bool kWide, bool kAnyHit>
+template <bool kWide, bool kAnyHit, bool kPlusZ = false>
 DDGI_D bool travStep(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& s, HitInfo& hit, uint32_t* err) {
-  if constexpr (kWide) return wideStep<kAnyHit>(b, r, kTMin, s, hit, err);
+  if constexpr (kWide) return wideStep<kAnyHit, kPlusZ>(b, r, kTMin, s, hit, err);
   else return binStep<kAnyHit>(b, r, kTMin, s, hit, err);
 }
 
@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(256) k_shade(const TraceItem* __restrict__ ite
 
 // Shadow rays (rchit:155-176): any hit in [0.1, 50] toward the sun; a shadowed ray's radiance becomes the
 // shadowed value the shading pass parked in its hit record, and its hit code gets the shadow bit.
-template <bool kWide>
+// kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
+template <bool kWide, bool kLightSpace>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
     k_trace_shadow(const TraceItem* __restrict__ items, int numItems, const float4* __restrict__ shadowList,
                    unsigned long long* __restrict__ counters, int refillLanes, const float4* __restrict__ hits,
@@ -405,13 +406,12 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
         id = (long long)__float_as_uint(rec.w);
         item = findItem(items, numItems, id >> 5);
         const TraceItem& T = items[item];
-        const bool lightSpace = T.s.shadow.tris != nullptr;
-        bvh = lightSpace ? T.s.shadow : T.s.bvh;
-        ray = makeRay(xyz(rec), lightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
+        bvh = kLightSpace ? T.s.shadow : T.s.bvh;
+        ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
       }
     }
-    if (id >= 0 && !finished) finished = travStep<kWide, true>(bvh, ray, st, hit, err);
+    if (id >= 0 && !finished) finished = travStep<kWide, true, kLightSpace>(bvh, ray, st, hit, err);
     if (id >= 0 && finished) {
       if (hit.leaf >= 0) {
         const TraceItem& T = items[item];
@@ -463,7 +463,7 @@ long long traceWarps(const GridGPU& g, const FrameGPU& f) {
 
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
-                             int refillLanes, bool wide, uint32_t* err, cudaStream_t stream) {
+                             int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream) {
   cudaError_t e = cudaMemsetAsync(dCounters, 0, kTraceCounters * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   dim3 lg((maxN + 127) / 128, numItems);
@@ -477,15 +477,14 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long shadeBlocks = (rays + 255) / 256;
   if (shadeBlocks > (long long)sms * 16) shadeBlocks = (long long)sms * 16;
-  if (wide) {
+  if (wide)
     k_trace_closest<true><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits, err);
-    k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
-    k_trace_shadow<true><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
-  } else {
+  else
     k_trace_closest<false><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits, err);
-    k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
-    k_trace_shadow<false><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
-  }
+  k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
+  auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true> : k_trace_shadow<true, false>)
+                     : (lightSpace ? k_trace_shadow<false, true> : k_trace_shadow<false, false>);
+  shadow<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
   return cudaGetLastError();
 }
 

@@ -23,7 +23,19 @@ DDGI_D int asInt(float f) { return __float_as_int(f); }
 DDGI_D uint32_t asUint(float f) { return __float_as_uint(f); }
 DDGI_D int lowestBit(uint32_t m) { return __ffs(m) - 1; }
 DDGI_D int popc(uint32_t m) { return __popc(m); }
+DDGI_D uint32_t bytePerm(uint32_t x, uint32_t y, uint32_t sel) { return __byte_perm(x, y, sel); }
+DDGI_D float asFloatHd(uint32_t u) { return __uint_as_float(u); }
 DDGI_D void flagError(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
+DDGI_D float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+DDGI_D float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 #else
 // host builds must compile with -ffp-contract=off so products and differences round separately
 inline float mulRn(float a, float b) { return a * b; }
@@ -34,11 +46,25 @@ inline int asInt(float f) { int i; memcpy(&i, &f, 4); return i; }
 inline uint32_t asUint(float f) { uint32_t i; memcpy(&i, &f, 4); return i; }
 inline int lowestBit(uint32_t m) { return __builtin_ctz(m); }
 inline int popc(uint32_t m) { return __builtin_popcount(m); }
+inline float asFloatHd(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+inline uint32_t bytePerm(uint32_t x, uint32_t y, uint32_t sel) {
+  uint64_t v = ((uint64_t)y << 32) | x;
+  uint32_t r = 0;
+  for (int k = 0; k < 4; ++k) r |= (uint32_t)((v >> (8 * ((sel >> (4 * k)) & 7))) & 0xff) << (8 * k);
+  return r;
+}
 inline void flagError(uint32_t* err, uint32_t bits) { if (err) *err |= bits; }
+inline float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+inline float min3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
 #endif
 
 struct WRay {
-  float3 o, d, invd;
+  float3 o, invd;
+  // box distances as one FMA per plane: t = fma(plane, invd, add) with add = -o * invd widened by an
+  // absolute margin (nAdd for near planes, fAdd for far planes), see wideStep
+  float3 nAdd, fAdd;
+  float3 invd15;  // invd * 2^15 and |invd| * 2^-21 (quantized wide nodes)
+  float3 invdM;
   int kx, ky, kz;
   float Sx, Sy, Sz;
 };
@@ -46,7 +72,6 @@ struct WRay {
 DDGI_HD WRay makeRay(float3 o, float3 d) {
   WRay r;
   r.o = o;
-  r.d = d;
   float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
   int kx = kz + 1; if (kx == 3) kx = 0;
@@ -61,6 +86,15 @@ DDGI_HD WRay makeRay(float3 o, float3 d) {
   float3 dd = f3(d.x != 0.f ? d.x : copysignf(1e-20f, d.x), d.y != 0.f ? d.y : copysignf(1e-20f, d.y),
                  d.z != 0.f ? d.z : copysignf(1e-20f, d.z));
   r.invd = f3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
+  // margin 2^-21 |o * invd| (8 units of rounding) covers the rounding of o * invd and of the additions,
+  // leaving one rounding of the FMA, within the conservative far-distance factor of the slab test
+  const float wx = o.x * r.invd.x, wy = o.y * r.invd.y, wz = o.z * r.invd.z;
+  const float ex = fabsf(wx) * 4.76837158203125e-7f, ey = fabsf(wy) * 4.76837158203125e-7f,
+              ez = fabsf(wz) * 4.76837158203125e-7f;
+  r.nAdd = f3(-wx - ex, -wy - ey, -wz - ez);
+  r.fAdd = f3(-wx + ex, -wy + ey, -wz + ez);
+  r.invd15 = r.invd * 32768.0f;
+  r.invdM = f3(fabsf(r.invd.x), fabsf(r.invd.y), fabsf(r.invd.z)) * 4.76837158203125e-7f;
   return r;
 }
 
@@ -99,14 +133,18 @@ DDGI_HD bool intersectTri(const WRay& r, float3 v0, float3 v1, float3 v2, float 
   return true;
 }
 
-// Slab test with a conservative far distance (Ize 2013: 1 + 2*gamma(3)).
+// Slab test with a conservative far distance (Ize 2013: 1 + 2*gamma(3)). Plane distances are
+// fma(plane, invd, nAdd) for the near plane of each axis and fma(plane, invd, fAdd) for the far one; the
+// margins in nAdd / fAdd keep the test conservative also for an axis-parallel ray whose origin lies exactly
+// on a box face (where (plane - o) * invd would give a signed zero far distance).
 DDGI_HD bool slab(const WRay& r, float lx, float hx, float ly, float hy, float lz, float hz, float tmin,
                   float tmax, float& tnear) {
-  float t0x = (lx - r.o.x) * r.invd.x, t1x = (hx - r.o.x) * r.invd.x;
-  float t0y = (ly - r.o.y) * r.invd.y, t1y = (hy - r.o.y) * r.invd.y;
-  float t0z = (lz - r.o.z) * r.invd.z, t1z = (hz - r.o.z) * r.invd.z;
-  float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-  float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+  const bool sx = r.invd.x < 0.f, sy = r.invd.y < 0.f, sz = r.invd.z < 0.f;
+  const float tnx = fmaf(sx ? hx : lx, r.invd.x, r.nAdd.x), tfx = fmaf(sx ? lx : hx, r.invd.x, r.fAdd.x);
+  const float tny = fmaf(sy ? hy : ly, r.invd.y, r.nAdd.y), tfy = fmaf(sy ? ly : hy, r.invd.y, r.fAdd.y);
+  const float tnz = fmaf(sz ? hz : lz, r.invd.z, r.nAdd.z), tfz = fmaf(sz ? lz : hz, r.invd.z, r.fAdd.z);
+  const float tn = max3f(tnx, tny, fmaxf(tnz, tmin));
+  const float tf = min3f(tfx, tfy, fminf(tfz, tmax));
   tnear = tn;
   return tn <= tf * 1.0000004f;
 }
@@ -218,7 +256,21 @@ DDGI_HD bool traverse(const BvhRef& b, const WRay& r, float tmin, float tmax, Hi
 // among the node's internal slots); (c << 5) | o with c in 1..kWideLeafMax = leaf of c triangle records
 // starting at triBase + o. Slot s holds the child that lies most toward the corner with sign bits s (bit a
 // set = +axis a), so visiting keys s ^ octant(ray) in increasing order is roughly front to back.
+#ifndef DDGI_WIDE_QUANT
+#define DDGI_WIDE_QUANT 0
+#endif
+#if DDGI_WIDE_QUANT
+// Quantized node = 5 float4 (80 B):
+//   [0]  float origin p.x, p.y, p.z; uint biased exponents e_x | e_y << 8 | e_z << 16 (scale s_a = 2^(e_a-127))
+//   [1]  uint4 {childBase, triBase, meta of slots 0-3, meta of slots 4-7}
+//   [2]  q lo.x of slots 0-7 (one byte each) | q lo.y   [3] q lo.z | q hi.x   [4] q hi.y | q hi.z
+// Slot boxes are [p + q_lo s, p + q_hi s] in exact arithmetic and contain the child (host rounding is
+// outward). The traversal reads a byte q as v = 1 + q 2^-15 (one byte permute builds the float) and gets
+// the plane distance as fma(v, 2^15 s invd, (p - 2^15 s - o) invd -/+ margin).
+constexpr int kWideNodeF4 = 5;
+#else
 constexpr int kWideNodeF4 = 13;
+#endif
 constexpr int kWideLeafMax = 1;
 constexpr int kWideStack = 64;
 
@@ -239,7 +291,10 @@ DDGI_HD bool wideInit(const BvhRef& b, const WRay& r, float tmax, WideTrav& s, H
   return b.numTris <= 0;
 }
 
-template <bool kAnyHit>
+// kPlusZ: every ray has direction exactly (0, 0, 1) (shadow rays in the light's sheared space); the box
+// test is then exact: the origin's x, y inside the box's and the z range [lo.z - o.z, hi.z - o.z] meeting
+// [tmin, t]. Otherwise near/far distances per axis are fma(plane, invd, nAdd / fAdd).
+template <bool kAnyHit, bool kPlusZ = false>
 DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, HitInfo& hit, uint32_t* err) {
   if ((unsigned)s.node >= (unsigned)b.numWNodes) {
     flagError(err, DDGI_DEVERR_BOUNDS);
@@ -251,6 +306,73 @@ DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, H
   const int nyo = (oct & 2) ? 7 : 5, fyo = 12 - nyo;
   const int nzo = (oct & 4) ? 11 : 9, fzo = 20 - nzo;
   const float4* nd = b.wnodes + kWideNodeF4 * s.node;
+#if DDGI_WIDE_QUANT
+  const float4 h0 = ldRo(nd);
+  const uint4 hd = ldRo(reinterpret_cast<const uint4*>(nd + 1));
+  const uint4 w0 = ldRo(reinterpret_cast<const uint4*>(nd + 2)), w1 = ldRo(reinterpret_cast<const uint4*>(nd + 3)),
+              w2 = ldRo(reinterpret_cast<const uint4*>(nd + 4));
+  // byte words: lo.x 0-1, lo.y 2-3, lo.z 4-5, hi.x 6-7, hi.y 8-9, hi.z 10-11
+  const uint32_t qw[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+  const uint32_t eb = asUint(h0.w);
+  const float p[3] = {h0.x, h0.y, h0.z};
+  const float o[3] = {r.o.x, r.o.y, r.o.z};
+  const float iv[3] = {r.invd.x, r.invd.y, r.invd.z};
+  const float iv15[3] = {r.invd15.x, r.invd15.y, r.invd15.z};
+  const float ivm[3] = {r.invdM.x, r.invdM.y, r.invdM.z};
+  float A[3], Bn[3], Bf[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const uint32_t e = (eb >> (8 * a)) & 0xffu;
+    const float sc = asFloatHd(e << 23);
+    const float c = fmaf(-32768.0f, sc, p[a]);  // p - 2^15 s
+    A[a] = sc * iv15[a];
+    const float B = (c - o[a]) * iv[a];
+    const float E = (fabsf(c) + fabsf(o[a])) * ivm[a];
+    Bn[a] = B - E;
+    Bf[a] = B + E;
+  }
+  float Rv[2] = {0.f, 0.f};
+  if (kPlusZ) {  // the origin in each axis' quantized units as 1 + R 2^-15, for the exact x / y containment
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const uint32_t e = (eb >> (8 * a)) & 0xffu;
+      Rv[a] = fmaf(o[a] - p[a], asFloatHd((254u - e) << 23) * 3.0517578125e-05f, 1.0f);
+    }
+  }
+  // near / far word pairs for the ray's direction signs
+  const int nxw = (oct & 1) ? 6 : 0, fxw = 6 - nxw;
+  const int nyw = (oct & 2) ? 8 : 2, fyw = 10 - nyw;
+  const int nzw = (oct & 4) ? 10 : 4, fzw = 14 - nzw;
+  uint32_t ihits = 0, imask = 0, lhits = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int h = c >> 2, k = c & 3;
+    const uint32_t sel = 0x7604u | ((uint32_t)k << 4);
+    const uint32_t m = ((c < 4 ? hd.z : hd.w) >> (8 * k)) & 0xffu;
+    const float vnx = asFloatHd(bytePerm(qw[nxw + h], 0x3F800000u, sel));
+    const float vfx = asFloatHd(bytePerm(qw[fxw + h], 0x3F800000u, sel));
+    const float vny = asFloatHd(bytePerm(qw[nyw + h], 0x3F800000u, sel));
+    const float vfy = asFloatHd(bytePerm(qw[fyw + h], 0x3F800000u, sel));
+    const float vnz = asFloatHd(bytePerm(qw[nzw + h], 0x3F800000u, sel));
+    const float vfz = asFloatHd(bytePerm(qw[fzw + h], 0x3F800000u, sel));
+    bool in;
+    if (kPlusZ) {  // oct == 0: near words are the lo words
+      in = vnx <= Rv[0] + 4.76837158203125e-7f && vfx >= Rv[0] - 4.76837158203125e-7f &&
+           vny <= Rv[1] + 4.76837158203125e-7f && vfy >= Rv[1] - 4.76837158203125e-7f &&
+           fmaxf(fmaf(vnz, A[2], Bn[2]), tmin) <= fminf(fmaf(vfz, A[2], Bf[2]), hit.t) * 1.0000004f;
+    } else {
+      const float tn = max3f(fmaf(vnx, A[0], Bn[0]), fmaf(vny, A[1], Bn[1]), fmaxf(fmaf(vnz, A[2], Bn[2]), tmin));
+      const float tf = min3f(fmaf(vfx, A[0], Bf[0]), fmaf(vfy, A[1], Bf[1]), fminf(fmaf(vfz, A[2], Bf[2]), hit.t));
+      in = tn <= tf * 1.0000004f;
+    }
+    const bool internal = (m >> 5) == 7u;
+    imask |= (internal ? 1u : 0u) << c;
+    if (m != 0u && in) {
+      if (internal) ihits |= 1u << (c ^ oct);
+      else lhits |= 1u << c;
+    }
+  }
+#else
   const uint4 hd = ldRo(reinterpret_cast<const uint4*>(nd));
   uint32_t ihits = 0, imask = 0, lhits = 0;
   // two halves of four slots each: six float4 of planes per half keep the register footprint small
@@ -270,19 +392,26 @@ DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, H
       const float pfy = q == 0 ? fy.x : q == 1 ? fy.y : q == 2 ? fy.z : fy.w;
       const float pnz = q == 0 ? nz.x : q == 1 ? nz.y : q == 2 ? nz.z : nz.w;
       const float pfz = q == 0 ? fz.x : q == 1 ? fz.y : q == 2 ? fz.z : fz.w;
-      // near/far distances per axis: (plane - o) * invd, each rounded as in the slab test above
-      const float tn = fmaxf(fmaxf((pnx - r.o.x) * r.invd.x, (pny - r.o.y) * r.invd.y),
-                             fmaxf((pnz - r.o.z) * r.invd.z, tmin));
-      const float tf = fminf(fminf((pfx - r.o.x) * r.invd.x, (pfy - r.o.y) * r.invd.y),
-                             fminf((pfz - r.o.z) * r.invd.z, hit.t));
+      bool in;
+      if (kPlusZ) {  // oct == 0: near planes are the lo planes
+        in = pnx <= r.o.x && r.o.x <= pfx && pny <= r.o.y && r.o.y <= pfy &&
+             fmaxf(pnz - r.o.z, tmin) <= fminf(pfz - r.o.z, hit.t) * 1.0000004f;
+      } else {
+        const float tn = max3f(fmaf(pnx, r.invd.x, r.nAdd.x), fmaf(pny, r.invd.y, r.nAdd.y),
+                               fmaxf(fmaf(pnz, r.invd.z, r.nAdd.z), tmin));
+        const float tf = min3f(fmaf(pfx, r.invd.x, r.fAdd.x), fmaf(pfy, r.invd.y, r.fAdd.y),
+                               fminf(fmaf(pfz, r.invd.z, r.fAdd.z), hit.t));
+        in = tn <= tf * 1.0000004f;
+      }
       const bool internal = (m >> 5) == 7u;
       imask |= (internal ? 1u : 0u) << c;
-      if (m != 0u && tn <= tf * 1.0000004f) {
+      if (m != 0u && in) {
         if (internal) ihits |= 1u << (c ^ oct);
         else lhits |= 1u << c;
       }
     }
   }
+#endif
   const uint32_t triBase = hd.y;
   while (lhits) {
     const int c = lowestBit(lhits);
@@ -325,11 +454,11 @@ DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, H
   return false;
 }
 
-template <bool kAnyHit>
+template <bool kAnyHit, bool kPlusZ = false>
 DDGI_HD bool traverseWide(const BvhRef& b, const WRay& r, float tmin, float tmax, HitInfo& hit, uint32_t* err) {
   WideTrav s;
   if (!wideInit<kAnyHit>(b, r, tmax, s, hit))
-    while (!wideStep<kAnyHit>(b, r, tmin, s, hit, err)) {
+    while (!wideStep<kAnyHit, kPlusZ>(b, r, tmin, s, hit, err)) {
     }
   return hit.leaf >= 0;
 }

@@ -12,6 +12,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -213,6 +214,42 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
     uint32_t m0 = 0, m1 = 0;
     for (int s = 0; s < 4; ++s) m0 |= (uint32_t)meta[s] << (8 * s);
     for (int s = 0; s < 4; ++s) m1 |= (uint32_t)meta[4 + s] << (8 * s);
+#if DDGI_WIDE_QUANT
+    // origin = node box min; per axis the smallest power-of-two scale with extent <= 255 s; child planes
+    // rounded outward (exact double arithmetic on float inputs)
+    uint32_t eb = 0;
+    float pf[3];
+    double sc[3];
+    for (int a = 0; a < 3; ++a) {
+      pf[a] = nb.lo[a];
+      const double ext = (double)nb.hi[a] - (double)pf[a];
+      int e = -100;
+      if (ext > 0) e = (int)std::ceil(std::log2(ext / 255.0));
+      e = std::max(-126, std::min(126, e));
+      while (std::ldexp(255.0, e) < ext) ++e;
+      sc[a] = std::ldexp(1.0, e);
+      eb |= (uint32_t)(e + 127) << (8 * a);
+    }
+    uint8_t qlo[3][8], qhi[3][8];
+    for (int sl = 0; sl < 8; ++sl) {
+      const int i = kidOf[sl];
+      for (int a = 0; a < 3; ++a) {
+        if (i < 0) { qlo[a][sl] = 0; qhi[a][sl] = 0; continue; }
+        double lo = std::floor(((double)kids[i].box.lo[a] - (double)pf[a]) / sc[a]);
+        double hi = std::ceil(((double)kids[i].box.hi[a] - (double)pf[a]) / sc[a]);
+        qlo[a][sl] = (uint8_t)std::max(0.0, std::min(255.0, lo));
+        qhi[a][sl] = (uint8_t)std::max(0.0, std::min(255.0, hi));
+      }
+    }
+    auto word = [&](const uint8_t* q, int h) {
+      return (uint32_t)q[4 * h] | (uint32_t)q[4 * h + 1] << 8 | (uint32_t)q[4 * h + 2] << 16 | (uint32_t)q[4 * h + 3] << 24;
+    };
+    nd[0] = make_float4(pf[0], pf[1], pf[2], asFloatH(eb));
+    nd[1] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
+    nd[2] = make_float4(asFloatH(word(qlo[0], 0)), asFloatH(word(qlo[0], 1)), asFloatH(word(qlo[1], 0)), asFloatH(word(qlo[1], 1)));
+    nd[3] = make_float4(asFloatH(word(qlo[2], 0)), asFloatH(word(qlo[2], 1)), asFloatH(word(qhi[0], 0)), asFloatH(word(qhi[0], 1)));
+    nd[4] = make_float4(asFloatH(word(qhi[1], 0)), asFloatH(word(qhi[1], 1)), asFloatH(word(qhi[2], 0)), asFloatH(word(qhi[2], 1)));
+#else
     nd[0] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
     float pl[6][8];
     for (int s = 0; s < 8; ++s) {
@@ -226,8 +263,37 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
       nd[1 + 2 * p] = make_float4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
       nd[2 + 2 * p] = make_float4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
     }
+#endif
   }
   return (int)order.size() == numTris;
+}
+
+// Header words and the exact box of slot `sl` of a wide node (host checks).
+inline void nodeHeader(const float4* nd, uint32_t& childBase, uint32_t& triBase, uint32_t meta[2]) {
+  const float4 h = nd[DDGI_WIDE_QUANT ? 1 : 0];
+  childBase = (uint32_t)asIntH(h.x);
+  triBase = (uint32_t)asIntH(h.y);
+  meta[0] = (uint32_t)asIntH(h.z);
+  meta[1] = (uint32_t)asIntH(h.w);
+}
+inline void slotBox(const float4* nd, int sl, double lo[3], double hi[3]) {
+#if DDGI_WIDE_QUANT
+  const uint32_t eb = (uint32_t)asIntH(nd[0].w);
+  const float p[3] = {nd[0].x, nd[0].y, nd[0].z};
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(nd + 2);
+  auto q = [&](int word0) { return (double)((w[word0 + sl / 4] >> (8 * (sl % 4))) & 0xffu); };
+  for (int a = 0; a < 3; ++a) {
+    const double s = std::ldexp(1.0, (int)((eb >> (8 * a)) & 0xffu) - 127);
+    lo[a] = (double)p[a] + q(2 * a) * s;
+    hi[a] = (double)p[a] + q(6 + 2 * a) * s;
+  }
+#else
+  const float* f = reinterpret_cast<const float*>(nd);
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = f[4 * (1 + 4 * a) + sl];
+    hi[a] = f[4 * (3 + 4 * a) + sl];
+  }
+#endif
 }
 
 }  // namespace wbvh

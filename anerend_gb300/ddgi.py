@@ -137,7 +137,7 @@ class ProbeGrid:
 
     def set_tuning(self, warp_probes: int | None = None, ray_order: int | None = None,
                    shadow_mode: int | None = None, conv_mode: int | None = None,
-                   bvh_width: int | None = None) -> None:
+                   bvh_width: int | None = None, refill_lanes: int | None = None) -> None:
         t = self.tuning
         if warp_probes is not None:
             t.warpProbes = warp_probes
@@ -149,6 +149,8 @@ class ProbeGrid:
             t.convMode = conv_mode
         if bvh_width is not None:
             t.bvhWidth = bvh_width
+        if refill_lanes is not None:
+            t.refillLanes = refill_lanes
         self.ctx.check(self.ctx.lib.ddgi_grid_set_tuning(self.handle, C.byref(t)))
 
     def reset(self, stream: int = 0) -> None:

@@ -337,9 +337,16 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
     batch = ddgi.Batch(ctx, items)
     res_b = {"grids": len(specs), "scenes": len(tris), "triangles": sum(tris), "rays": brays,
              "plain_fp32_ms": plain_ms, "plain_fp32_rays_per_s": brays / plain_ms * 1e3}
+    # launch shape from the autotuner (timed on the BF16 tensor-core form; the trace dominates, so the shape
+    # carries over to the other convolution modes)
+    from anerend_gb300 import autotune
+
+    batch.set_tuning(conv_mode=2, use_graph=1)
+    tuned = autotune.tune_batch(batch, bframes, autotune.batch_signature(specs, tris), stream, reps=2, warmup=2,
+                                use_cache=False)
+    res_b["autotuned"] = {"tuning": tuned["tuning"], "trials": len(tuned["trials"]), "best_ms": tuned["ms"]}
     for name, conv in (("batched_fp32", 0), ("batched_tc_fp16", 1), ("batched_tc_bf16", 2)):
-        batch.set_tuning(conv_mode=conv, blocks_per_sm=8, refill_lanes=8, warp_probes=2, ray_order=1,
-                         shadow_mode=1, use_graph=1, bvh_width=bvh_width)
+        batch.set_tuning(conv_mode=conv, use_graph=1, **tuned["tuning"])
         ms = _time_updates(torch, lambda fr: batch.update(fr, stream), bframes, 4)
         res_b[f"{name}_ms"] = ms
         res_b[f"{name}_rays_per_s"] = brays / ms * 1e3
@@ -403,7 +410,8 @@ def run_ours(args, rank, local, world):
     probe_grid.close()
 
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
-    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0, bvh_width=args.bvh_width)  # FP32
+    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0, bvh_width=args.bvh_width,
+                    refill_lanes=args.refill_lanes)  # FP32 throughout
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     rays_per_step = w.probes * w.rays
 
@@ -512,7 +520,7 @@ def run_ours(args, rank, local, world):
             "clocks": clocks,
             "tuning": {"warpProbes": int(grid.tuning.warpProbes), "rayOrder": int(grid.tuning.rayOrder),
                        "shadowMode": int(grid.tuning.shadowMode), "convMode": int(grid.tuning.convMode),
-                       "bvhWidth": int(grid.tuning.bvhWidth)},
+                       "bvhWidth": int(grid.tuning.bvhWidth), "refillLanes": int(grid.tuning.refillLanes)},
             "forms": forms,
         }
         print(json.dumps(line))
@@ -531,6 +539,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the other forms (batched, precision, serving)")
     ap.add_argument("--form", choices=["precision"], help="run only this form and print its measurements")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal tree (8-wide or binary)")
+    ap.add_argument("--refill-lanes", type=int, default=8, help="idle lanes before a traversal warp refills (1..32)")
     args = ap.parse_args()
     rank, local, world = dist_init()
     if args.impl == "reference":

@@ -159,7 +159,9 @@ typedef struct DdgiTuning {
                            accumulation and the hysteresis blend stay FP32 */
   int32_t bvhWidth;     /* traversal tree: 8 = 8-wide BVH collapsed from the LBVH (default; 0 means 8);
                            2 = the binary LBVH. Both give the same hits */
-  int32_t reserved[3];
+  int32_t refillLanes;  /* a warp of the persistent traversals takes new rays once this many of its lanes are
+                           idle (1..32; default 8; 0 means 8) */
+  int32_t reserved[2];
 } DdgiTuning;
 
 /* Device views of the grid's buffers (owned by the grid). */

@@ -80,6 +80,10 @@ struct Bvh2Builder {
   }
 };
 
+struct Box64 {
+  double lo[3], hi[3];
+};
+
 bool sameHit(const HitInfo& a, const HitInfo& b) {
   if ((a.leaf >= 0) != (b.leaf >= 0)) return false;
   if (a.leaf < 0) return true;
@@ -149,10 +153,10 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
     nodes2[4 * n + 3].x = asF(c0);
     nodes2[4 * n + 3].y = asF(c1);
   }
-  // structure: every slot's box contains every record below it; internal indices in range
+  // structure: every slot's box contains every record below it; indices in range; each record once
   {
-    std::vector<std::pair<int, wbvh::Box>> st;
-    wbvh::Box all{{-3e38f, -3e38f, -3e38f}, {3e38f, 3e38f, 3e38f}};
+    std::vector<std::pair<int, Box64>> st;
+    Box64 all{{-3e38, -3e38, -3e38}, {3e38, 3e38, 3e38}};
     st.push_back({0, all});
     int visited = 0;
     std::vector<int> seen(numTris, 0);
@@ -162,17 +166,21 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
       if (n < 0 || n >= numWide) { stats[5]++; continue; }
       ++visited;
       const float4* nd = wide.data() + (size_t)n * kWideNodeF4;
-      uint32_t childBase = wbvh::asIntH(nd[0].x), triBase = wbvh::asIntH(nd[0].y);
-      uint32_t mm[2] = {(uint32_t)wbvh::asIntH(nd[0].z), (uint32_t)wbvh::asIntH(nd[0].w)};
+      uint32_t childBase, triBase, mm[2];
+      wbvh::nodeHeader(nd, childBase, triBase, mm);
       int rank = 0;
       for (int s = 0; s < 8; ++s) {
         uint32_t m = (mm[s / 4] >> (8 * (s % 4))) & 0xff;
         if (!m) continue;
-        const float* f = reinterpret_cast<const float*>(nd);
-        auto plane = [&](int p) { return f[4 * (1 + 2 * p) + s]; };
-        wbvh::Box b{{plane(0), plane(2), plane(4)}, {plane(1), plane(3), plane(5)}};
-        for (int a = 0; a < 3; ++a)
-          if (b.lo[a] < pb.lo[a] || b.hi[a] > pb.hi[a]) stats[5]++;
+        double blo[3], bhi[3];
+        wbvh::slotBox(nd, s, blo, bhi);
+        Box64 b{{blo[0], blo[1], blo[2]}, {bhi[0], bhi[1], bhi[2]}};
+        // every triangle below a slot must lie in the slot's box: carry the intersection of the boxes
+        // on the path (a quantized child node may reach one step past its parent's slot box)
+        for (int a = 0; a < 3; ++a) {
+          b.lo[a] = std::max(b.lo[a], pb.lo[a]);
+          b.hi[a] = std::min(b.hi[a], pb.hi[a]);
+        }
         if ((m >> 5) == 7) {
           if ((int)(m & 31) != rank) stats[5]++;
           st.push_back({(int)(childBase + rank), b});
@@ -217,6 +225,10 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
       float z = rng.uni() * 2 - 1, ph = rng.uni() * 6.2831853f, s = std::sqrt(std::max(0.0f, 1 - z * z));
       d = f3(s * std::cos(ph), s * std::sin(ph), z);
     }
+    if (q % 13 == 6 && numTris > 0) {  // origin straight below a vertex: +z rays through vertices and edges
+      const Tri& t = tris[rng.next() % numTris];
+      o = f3(t.v[q % 3][0], t.v[q % 3][1], t.v[q % 3][2] - 3.0f);
+    }
     WRay r = makeRay(o, d);
     HitInfo bf;
     bf.leaf = -1; bf.gid = INT_MAX; bf.t = 50.0f;
@@ -229,6 +241,18 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
     if (!sameHit(bf, hw)) stats[3]++;
     if (any != (bf.leaf >= 0) || (any && !(ha.t >= 0.1f && ha.t <= 50.0f))) stats[4]++;
     if (bf.leaf >= 0) stats[6]++;
+    // the same origin along exactly +z through the specialised box test (light-space shadow rays)
+    if (q % 3 == 0) {
+      WRay rz = makeRay(o, f3(0.f, 0.f, 1.f));
+      HitInfo bz;
+      bz.leaf = -1; bz.gid = INT_MAX; bz.t = 50.0f;
+      for (int k = 0; k < numTris; ++k) testTri<false>(bref, rz, k, 0.1f, bz);
+      HitInfo hz, az;
+      traverseWide<false, true>(bref, rz, 0.1f, 50.0f, hz, &err);
+      bool anyz = traverseWide<true, true>(bref, rz, 0.1f, 50.0f, az, &err);
+      if (!sameHit(bz, hz)) stats[3]++;
+      if (anyz != (bz.leaf >= 0)) stats[4]++;
+    }
   }
   stats[7] = err;
   return (int)(stats[2] + stats[3] + stats[4] + stats[5] + (err ? 1 : 0));

@@ -1,5 +1,5 @@
-"""CPU checks of the 8-wide BVH collapse and of the binary and wide traversals (host build of the same
-header the trace kernel uses): closest hits equal a brute-force loop over all triangles bit for bit,
+"""CPU checks of the 8-wide BVH collapse (FP32 and quantized node layouts) and of the binary and wide
+traversals (host build of the same header the trace kernel uses): closest hits equal a brute-force loop over all triangles bit for bit,
 including exact-duplicate triangles (t ties broken by the lowest global id), zero-area triangles,
 axis-aligned rays with signed zero components and rays aimed at vertices and edges."""
 import ctypes
@@ -26,14 +26,14 @@ def _cuda_include():
     return None
 
 
-@pytest.fixture(scope="module")
-def lib(tmp_path_factory):
+@pytest.fixture(scope="module", params=[0, 1], ids=["fp32-nodes", "quantized-nodes"])
+def lib(request, tmp_path_factory):
     inc = _cuda_include()
     if inc is None or shutil.which("g++") is None:
         pytest.skip("g++ or the CUDA headers are missing")
     out = tmp_path_factory.mktemp("wbvh") / "libwbvh_check.so"
-    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", f"-I{inc}",
-           f"-I{ROOT / 'anerend_gb300' / 'csrc'}", str(SRC), "-o", str(out)]
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", f"-DDDGI_WIDE_QUANT={request.param}",
+           f"-I{inc}", f"-I{ROOT / 'anerend_gb300' / 'csrc'}", str(SRC), "-o", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     lib = ctypes.CDLL(str(out))
