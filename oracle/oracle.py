@@ -184,13 +184,15 @@ def lattice(n: int, rot: np.ndarray) -> np.ndarray:
 
 
 def convolve(desc, ray_rad: np.ndarray, dirs: np.ndarray, atlas: np.ndarray, layer_begin: int, layer_end: int,
-             flags: int, threads: int = 0) -> None:
-    """probe_conv.comp on FP64 arrays; `atlas` is updated in place."""
+             flags: int, threads: int = 0, hysteresis: float | None = None) -> None:
+    """probe_conv.comp on FP64 arrays; `atlas` is updated in place. hysteresis defaults to the grid
+    description's (a float32 value)."""
     ray_rad = np.ascontiguousarray(ray_rad, np.float64)
     dirs = np.ascontiguousarray(dirs, np.float64)
     assert atlas.dtype == np.float64 and atlas.flags.c_contiguous
-    load().oracle_convolve(C.addressof(desc), _p(ray_rad), _p(dirs), _p(atlas), layer_begin, layer_end, flags,
-                           float(desc.hysteresis), threads)
+    h = float(desc.hysteresis) if hysteresis is None else float(hysteresis)
+    load().oracle_convolve(C.addressof(desc), _p(ray_rad), _p(dirs), _p(atlas), layer_begin, layer_end, flags, h,
+                           threads)
 
 
 def translate(desc, atlas: np.ndarray, dx: int, dz: int) -> np.ndarray:

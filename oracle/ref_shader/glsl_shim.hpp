@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 namespace glsl {
 
@@ -41,6 +42,8 @@ struct vec<T, 2> {
   vec(T a, T b) : x(a), y(b) {}
   template <class U>
   vec(const vec<U, 2>& o) : x(T(o.x)), y(T(o.y)) {}
+  template <class U, int M, int... I, class = std::enable_if_t<!std::is_same<U, T>::value>>
+  explicit vec(const Swz<vec<U, 2>, U, M, I...>& s) : vec(vec<U, 2>(s)) {}
   template <class U>
   explicit vec(const vec<U, 3>& o) : x(T(o.x)), y(T(o.y)) {}
   template <class U>
@@ -73,6 +76,8 @@ struct vec<T, 3> {
   vec(T a, const vec<T, 2>& b) : x(a), y(b.x), z(b.y) {}
   template <class U>
   vec(const vec<U, 3>& o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
+  template <class U, int M, int... I, class = std::enable_if_t<!std::is_same<U, T>::value>>
+  explicit vec(const Swz<vec<U, 3>, U, M, I...>& s) : vec(vec<U, 3>(s)) {}
   template <class U>
   explicit vec(const vec<U, 4>& o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
   vec(const vec& o) { std::memcpy(e, o.e, sizeof(e)); }
