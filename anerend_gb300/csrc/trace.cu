@@ -52,10 +52,14 @@ DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int
   float fx = ox - fx0, fy = oy - fy0;
   int x0 = sx + (int)fx0, y0 = sy + (int)fy0;
   int x1 = x0 + 1, y1 = y0 + 1;
-  x0 = ((x0 % g.atlasW) + g.atlasW) % g.atlasW;
-  x1 = ((x1 % g.atlasW) + g.atlasW) % g.atlasW;
-  y0 = ((y0 % g.atlasH) + g.atlasH) % g.atlasH;
-  y1 = ((y1 % g.atlasH) + g.atlasH) % g.atlasH;
+  // REPEAT wrap. The indices are never negative (ix, iy, iz >= 0; the octahedral offset is >= -1 and sx,
+  // sy >= 1) and stay below W + 10 and H + 10 Z + 10 <= 3 H, so conditional subtractions equal the modulo.
+  if (x0 >= g.atlasW) x0 -= g.atlasW;
+  if (x1 >= g.atlasW) x1 -= g.atlasW;
+  if (y0 >= g.atlasH) y0 -= g.atlasH;
+  if (y0 >= g.atlasH) y0 -= g.atlasH;
+  if (y1 >= g.atlasH) y1 -= g.atlasH;
+  if (y1 >= g.atlasH) y1 -= g.atlasH;
   float4 t00 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x0);
   float4 t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
   float4 t01 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x0);
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
 // Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
 // computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
 // shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
-__global__ void __launch_bounds__(256) k_shade(const TraceItem* __restrict__ items, int numItems, long long totalRays,
+__global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ items, int numItems, long long totalRays,
                                                float4* __restrict__ hits, float4* __restrict__ shadowList,
                                                unsigned long long* __restrict__ counters) {
   const int lane = threadIdx.x & 31;
@@ -332,10 +336,16 @@ __global__ void __launch_bounds__(256) k_shade(const TraceItem* __restrict__ ite
         const float3 normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6],
                                             nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
                                             nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
-        const float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
-        float3 color = toLinear(vcol);
+        // the base colour factor wins when its sum exceeds 0.1; otherwise the interpolated vertex colour in
+        // linear space (rchit:183-184, bindless.glsl:199-203)
         const float4 bcf = __ldg((const float4*)mat.baseColFac);
-        if (bcf.x + bcf.y + bcf.z > 0.1f) color = xyz(bcf);
+        float3 color;
+        if (bcf.x + bcf.y + bcf.z > 0.1f) {
+          color = xyz(bcf);
+        } else {
+          const float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
+          color = toLinear(vcol);
+        }
         const float4 mr = __ldg((const float4*)mat.metRough);
         const float4 em = __ldg((const float4*)mat.emissive);
         const float metallic = mr.x, roughness = mr.y;

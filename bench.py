@@ -7,7 +7,8 @@ rotated golden-angle lattice, trace + shade of all 2,097,152 rays, and the convo
   value      probe rays/s, device-timed (CUDA events on the launching stream), inputs resident in HBM
   e2e        the same metric through the C ABI from the host: ddgi_update + ddgi_atlas_download into pinned
              host memory, wall clock per step (host frame parameters in, atlas out)
-  roofline   of the dominant kernel (trace + shade): algorithmic bytes / its event-timed duration vs the
+  roofline   of the dominant work, the trace (closest-hit traversal, shading, shadow traversal: three
+             kernels in stream order): algorithmic bytes / its event-timed duration vs the
              measured HBM copy bandwidth
   cpu_baseline  the FP64 oracle on all host cores over a bounded sample (rank 0, N = 1 only)
 
@@ -478,7 +479,7 @@ def run_ours(args, rank, local, world):
     achieved = alg_bytes / trace_avg_s / 1e9
     # DRAM bytes of one trace launch, from the ncu capture summarised beside the profile (same workload)
     traffic = None
-    tp = ROOT / "profiles" / "k_trace_batch_single_grid.md"
+    tp = ROOT / "profiles" / "trace_wavefront_single_grid.md"
     if tp.exists():
         import re
 
@@ -511,7 +512,8 @@ def run_ours(args, rank, local, world):
             "wall_s": wall,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 116,
                     "d2h_bytes_per_step": int(grid.buffers.atlasBytes)},
-            "roofline": {"kernel": "k_trace_batch", "bound": "hbm", "achieved": achieved,
+            "roofline": {"kernel": "trace (k_trace_closest + k_shade + k_trace_shadow)", "bound": "hbm",
+                         "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "traffic": traffic, "peak_source": peaks["source"],
                          "algorithmic_bytes_per_launch": alg_bytes},
