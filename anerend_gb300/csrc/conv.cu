@@ -2,9 +2,10 @@
 //
 // Every probe of a dispatch uses the same N ray directions, so the cosine weights are one table
 // W[t][j] = max(0, dot(d_j, omega_t)) (0 where <= 1e-6, probe_conv.comp:296-299) shared by all probes, and
-// the weight sum s_t = sum_j W[t][j] is shared too. The kernel stages W^T (N x 64) in shared memory once per
-// CTA, then walks groups of four probes: their ray radiance is staged in shared memory and each thread
-// accumulates one (probe, texel) pair, normalises by s_t and blends with the old atlas texel.
+// the weight sum s_t = sum_j W[t][j] is shared too. A weights kernel writes W^T (N x 64) and s; the
+// convolution kernel then works on tiles of 32 probes with a 4-probe x 4-texel register tile per thread,
+// streaming the rays through shared memory in chunks of 16 (k_conv_fp32_batch). One launch covers many
+// grids (a record per grid) or one grid passed by value (the raw entry points).
 #include "ddgi_common.cuh"
 #include "kernels.h"
 
@@ -12,8 +13,6 @@ namespace ddgi {
 
 namespace {
 
-constexpr int kConvProbes = 4;                       // probes per group
-constexpr int kConvThreads = kConvProbes * kOctTexels;  // 256
 
 __global__ void __launch_bounds__(256) k_conv_weights(int n, const float4* __restrict__ dirs, float* __restrict__ wt,
                                                       float* __restrict__ wsum) {
@@ -35,86 +34,6 @@ __global__ void __launch_bounds__(256) k_conv_weights(int n, const float4* __res
     __syncthreads();
   }
   if (threadIdx.x == 0) wsum[t] = part[0];
-}
-
-// kSmemW: the N x 64 weight table is staged in shared memory (N <= 512); otherwise it is read from global
-// memory, where it stays L1/L2-resident (256 KB at N = 1024).
-template <bool kSmemW>
-__global__ void __launch_bounds__(kConvThreads) k_conv_fp32(GridGPU g, const float4* __restrict__ rayRad,
-                                                            const float* __restrict__ wt,
-                                                            const float* __restrict__ wsum,
-                                                            void* __restrict__ atlas, int layerBegin,
-                                                            int layerEnd, float hysteresis, uint32_t flags) {
-  extern __shared__ float4 smem4[];
-  const int N = g.N;
-  const float* sW = wt;
-  float4* sR = smem4;  // kConvProbes * N
-  if (kSmemW) {
-    float* w = reinterpret_cast<float*>(smem4);  // N * 64
-    for (int i = threadIdx.x; i < N * kOctTexels; i += blockDim.x) w[i] = wt[i];
-    sW = w;
-    sR = smem4 + (N * kOctTexels) / 4;
-  }
-  const int t = threadIdx.x % kOctTexels;
-  const int q = threadIdx.x / kOctTexels;
-  const float ws = wsum[t];
-  const int probesPerLayer = g.X * g.Z;
-  const long long total = (long long)(layerEnd - layerBegin) * probesPerLayer;
-  const long long groups = (total + kConvProbes - 1) / kConvProbes;
-  const bool bake = (flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
-  for (long long grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    __syncthreads();  // sW ready / previous group's sR consumed
-    // stage the radiance of the group's probes
-    for (int i = threadIdx.x; i < kConvProbes * N; i += blockDim.x) {
-      int qq = i / N, j = i % N;
-      long long pl = grp * kConvProbes + qq;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (pl < total) {
-        int layer = layerBegin + (int)(pl / probesPerLayer);
-        int p = (int)(pl % probesPerLayer);
-        int px = p % g.X, pz = p / g.X;
-        int rx = px * g.bw + (j % g.bw);
-        int ry = (layer * g.Z + pz) * g.bh + (j / g.bw);
-        v = rayRad[(size_t)ry * g.rayW + rx];
-      }
-      sR[qq * N + j] = v;
-    }
-    __syncthreads();
-    long long pl = grp * kConvProbes + q;
-    if (pl >= total) continue;
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    const float4* r = sR + q * N;
-#pragma unroll 8
-    for (int j = 0; j < N; ++j) {
-      float w = sW[j * kOctTexels + t];
-      float4 L = r[j];
-      ax = fmaf(w, L.x, ax);
-      ay = fmaf(w, L.y, ay);
-      az = fmaf(w, L.z, az);
-    }
-    int layer = layerBegin + (int)(pl / probesPerLayer);
-    int p = (int)(pl % probesPerLayer);
-    int px = p % g.X, pz = p / g.X;
-    int tx = t % kOct, ty = t / kOct;
-    size_t ai = (size_t)(kProbePix * (layer * g.Z + pz) + 1 + ty) * g.atlasW + (kProbePix * px + 1 + tx);
-    float4 old = loadTexel(atlas, g.atlasFmt, ai);
-    float4 out;
-    if (bake) {
-      // probe_conv.comp:307-319: weighted accumulation with the stored weight in .w
-      float tw = old.w + ws;
-      float3 tot = f3(ax, ay, az) + xyz(old) * old.w;
-      if (tw > 1e-6f) tot = tot / tw;
-      out = make_float4(tot.x, tot.y, tot.z, tw);
-    } else {
-      // probe_conv.comp:321-326
-      float3 res = f3(ax, ay, az);
-      if (ws > 1e-6f) res = res / ws;
-      float a = 1.0f - hysteresis;
-      out = make_float4(res.x * a + old.x * hysteresis, res.y * a + old.y * hysteresis,
-                        res.z * a + old.z * hysteresis, ws * a + old.w * hysteresis);
-    }
-    storeTexel(atlas, g.atlasFmt, ai, out);
-  }
 }
 
 // ---- many grids in one launch -------------------------------------------------------------------
@@ -153,19 +72,22 @@ constexpr int kRStride = kChunk + 1;  // padded probe stride of the radiance chu
 constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;          // 4 float4 per thread
 constexpr int kWLoads = kChunk * kOctTexels / 4 / kTileThreads;       // 2 float4 per thread
 
+// kSingle: one item, passed by value in `single` (the raw entry points, which own no device records).
+template <bool kSingle>
 __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvItem* __restrict__ items, int numItems,
-                                                                  long long totalTiles) {
+                                                                     long long totalTiles,
+                                                                     const __grid_constant__ ConvItem single) {
   __shared__ float4 sR[kTileProbes * kRStride];
   __shared__ float4 sW[kChunk * kOctTexels / 4];
   const int tg = threadIdx.x & 15;  // texels 4tg .. 4tg+3
   const int pg = threadIdx.x >> 4;  // probes 4pg .. 4pg+3 of the tile
   for (long long tile = blockIdx.x; tile < totalTiles; tile += gridDim.x) {
-    int lo = 0, hi = numItems - 1;
+    int lo = 0, hi = kSingle ? 0 : numItems - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
       if (items[mid].groupBegin <= tile) lo = mid; else hi = mid - 1;
     }
-    const ConvItem& it = items[lo];
+    const ConvItem& it = kSingle ? single : items[lo];
     const GridGPU& g = it.g;
     const int probesPerLayer = g.X * g.Z;
     const long long total = (long long)(it.layerEnd - it.layerBegin) * probesPerLayer;
@@ -272,10 +194,10 @@ cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long 
   int dev = 0, sms = 0, perSm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch, kTileThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch<false>, kTileThreads, 0);
   long long grid = (long long)sms * (perSm > 0 ? perSm : 1);
   if (grid > totalGroups) grid = totalGroups;
-  k_conv_fp32_batch<<<(unsigned)grid, kTileThreads, 0, stream>>>(dItems, numItems, totalGroups);
+  k_conv_fp32_batch<false><<<(unsigned)grid, kTileThreads, 0, stream>>>(dItems, numItems, totalGroups, ConvItem{});
   return cudaGetLastError();
 }
 
@@ -288,22 +210,25 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream) {
   if (layerEnd <= layerBegin) return cudaSuccess;
-  const bool smemW = g.N <= 512;
-  size_t smem = sizeof(float4) * (size_t)kConvProbes * g.N;
-  if (smemW) smem += sizeof(float) * (size_t)g.N * kOctTexels;
-  auto kern = smemW ? k_conv_fp32<true> : k_conv_fp32<false>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0;
+  ConvItem it{};
+  it.g = g;
+  it.rayRad = rayRad;
+  it.wt = const_cast<float*>(wt);
+  it.wsum = const_cast<float*>(wsum);
+  it.atlas = atlas;
+  it.layerBegin = layerBegin;
+  it.layerEnd = layerEnd;
+  it.hysteresis = hysteresis;
+  it.flags = flags;
+  it.groupBegin = 0;
+  const long long tiles = convGroups(g, layerBegin, layerEnd);
+  int dev = 0, sms = 0, perSm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  long long groups = ((long long)(layerEnd - layerBegin) * g.X * g.Z + kConvProbes - 1) / kConvProbes;
-  int perSm = smem <= 100 * 1024 ? 2 : 1;
-  long long grid = (long long)sms * perSm;
-  if (grid > groups) grid = groups;
-  if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, kConvThreads, smem, stream>>>(g, rayRad, wt, wsum, atlas, layerBegin, layerEnd, hysteresis,
-                                                      flags);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch<true>, kTileThreads, 0);
+  long long grid = (long long)sms * (perSm > 0 ? perSm : 1);
+  if (grid > tiles) grid = tiles;
+  k_conv_fp32_batch<true><<<(unsigned)grid, kTileThreads, 0, stream>>>(nullptr, 1, tiles, it);
   return cudaGetLastError();
 }
 
