@@ -6,9 +6,10 @@
 // One CTA per SM walks tiles of 128 probes. Per tile and 64-ray K-chunk a TMA producer warp loads the three
 // 128 x 64 radiance tiles and the 64 x 64 weight tile (SWIZZLE_128B); one thread of the MMA warp issues
 // 4 K-steps x 3 channels of tcgen05.mma (M = 128 probes, N = 64 texels, K = 16) into FP32 accumulators in
-// TMEM (3 x 64 columns, double-buffered = 384 of 512 columns). Four epilogue warps read the accumulators with
-// tcgen05.ld (thread = probe), normalise by the texel's weight sum and apply the hysteresis blend (or the
-// bake accumulation) in FP32 against the old atlas texel.
+// TMEM (3 x 64 columns, double-buffered = 384 of 512 columns). Eight epilogue warps read the accumulators with
+// tcgen05.ld (thread = probe), stage them in shared memory and walk the atlas coalesced (lanes = 4 probes x
+// 8 texels of a row), normalising by the texel's weight sum and applying the hysteresis blend (or the bake
+// accumulation) in FP32 against the old atlas texel.
 //
 // Every mbarrier wait is bounded: on timeout the kernel raises DDGI_DEVERR_TIMEOUT, stops issuing work,
 // waits (bounded) for its own TMA loads and MMAs in flight, frees its TMEM and returns.
@@ -28,12 +29,17 @@ namespace {
 
 constexpr int kTileP = 128;                  // probes per tile (MMA M)
 constexpr int kChunkK = 64;                  // rays per K-chunk (128 bytes of 16-bit values)
-constexpr int kStages = 4;  // 4 x 56 KB = 224 KB of operand staging
+constexpr int kStages = 3;  // 3 x 56 KB of operand staging
 constexpr int kATileBytes = kTileP * kChunkK * 2;   // 16 KB per channel
 constexpr int kWTileBytes = kOctTexels * kChunkK * 2;  // 8 KB
 constexpr int kStageBytes = 3 * kATileBytes + kWTileBytes;  // 56 KB
 constexpr int kTmemCols = 512;
-constexpr int kThreadsTc = 192;              // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kEpiWarps = 8;                 // two per TMEM lane quarter, each on half of the texel blocks
+constexpr int kThreadsTc = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+// epilogue staging: per epilogue warp, 3 channels x 32 probes x 16 texels of one texel block (row stride 17)
+constexpr int kStageRow = 17;
+constexpr int kStageWarpFloats = 3 * 32 * kStageRow;
+constexpr size_t kSmemTc = (size_t)kStages * kStageBytes + kEpiWarps * kStageWarpFloats * sizeof(float) + 1024;
 constexpr uint32_t kSpinLimit = 1u << 22;
 
 DDGI_D uint32_t smemU32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) { mbarInit(&fullBar[s], 1); mbarInit(&emptyBar[s], 1); }
-    for (int b = 0; b < 2; ++b) { mbarInit(&accFull[b], 1); mbarInit(&accEmpty[b], 128); }
+    for (int b = 0; b < 2; ++b) { mbarInit(&accFull[b], 1); mbarInit(&accEmpty[b], 32 * kEpiWarps); }
     mbarInit(&drainBar, 1);
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -274,63 +280,94 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
     }
   } else {
-    // ---- epilogue: warps 2..5, thread = probe row of the tile ----
+    // ---- epilogue: warps 2..9 ----
+    // A warp may read TMEM lanes 32q..32q+31 with q = warp % 4 (its probe rows); the two warps of a quarter
+    // split the four blocks of 16 texels between them. Per block (two texel rows)
+    // it reads its rows' accumulators (thread = probe), stages them in shared memory and then walks the
+    // atlas coalesced: per step its lanes cover 4 probes x the 8 texels of one row (4 runs of 128 bytes).
+    // The old texels do not depend on the MMA, so their loads are issued before the accumulator wait.
     const int quarter = warp & 3;  // TMEM lane quarter this warp may access
-    const int row = quarter * 32 + lane;
+    const int half = (warp - 2) >> 2;  // which two texel blocks
+    float* stage = reinterpret_cast<float*>(smem + (size_t)kStages * kStageBytes) + (warp - 2) * kStageWarpFloats;
+    const int tx = lane & 7, pp = lane >> 3;
     int local = 0;
     for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
       const TcItem& it = tcItem(items, tcItemOf(items, numItems, t));
       const bool bake = (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
       const float h = it.hysteresis, a = 1.0f - h;
-      int b = local & 1;
-      uint32_t accPhase = (local >> 1) & 1;
-      if (!mbarWait(&accFull[b], accPhase)) { fail(); break; }
-      tcFenceAfter();
-      const int probe = it.pBegin + (t - it.tileBegin) * kTileP + row;
-      const bool live = probe < it.pEnd;
-      int px = 0, pzAll = 0;
-      if (live) {
-        px = probe % it.X;
-        pzAll = probe / it.X;  // layer * Z + z
+      const int b = local & 1;
+      const uint32_t accPhase = (local >> 1) & 1;
+      // atlas offsets of the 8 probes this lane visits (probe 4g + pp of the warp's 32), texel (tx, 0)
+      const int warpProbe0 = it.pBegin + (t - it.tileBegin) * kTileP + quarter * 32;
+      size_t base[8];
+      uint32_t liveMask = 0;
+#pragma unroll
+      for (int g = 0; g < 8; ++g) {
+        const int probe = warpProbe0 + 4 * g + pp;
+        const bool live = probe < it.pEnd;
+        const int px = live ? probe % it.X : 0, pzAll = live ? probe / it.X : 0;  // pzAll = layer * Z + z
+        base[g] = (size_t)(kProbePix * pzAll + 1) * it.atlasW + (kProbePix * px + 1 + tx);
+        liveMask |= (live ? 1u : 0u) << g;
       }
       const uint32_t laneAddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 3 * kOctTexels);
+      bool ok = true;
 #pragma unroll 1
-      for (int blk = 0; blk < kOctTexels / 16; ++blk) {
+      for (int blk = 2 * half; blk < 2 * half + 2; ++blk) {
+        // step k: probe group k >> 1, texel row ty = 2 blk + (k & 1)
+        float4 olds[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int g = k >> 1, ty = 2 * blk + (k & 1);
+          olds[k] = (liveMask >> g) & 1u ? loadTexel(it.atlas, it.atlasFmt, base[g] + (size_t)ty * it.atlasW)
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if (blk == 2 * half) {
+          // warp-uniform outcome: the tcgen05.ld below is warp-collective
+          if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase))) {
+            if (lane == 0) fail();
+            ok = false;
+            break;
+          }
+          tcFenceAfter();
+        }
         float cr[16], cg[16], cb[16];
         tmemLoad16(laneAddr + 0 * kOctTexels + blk * 16, cr);
         tmemLoad16(laneAddr + 1 * kOctTexels + blk * 16, cg);
         tmemLoad16(laneAddr + 2 * kOctTexels + blk * 16, cb);
-        if (!live) continue;
-        // the 16 old texels (two texel rows) are loaded before any store, so the loads overlap instead of
-        // each waiting behind the previous texel's store to the same buffer
-        float4 olds[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          int tex = blk * 16 + i;
-          size_t ai = (size_t)(kProbePix * pzAll + 1 + tex / kOct) * it.atlasW + (kProbePix * px + 1 + tex % kOct);
-          olds[i] = loadTexel(it.atlas, it.atlasFmt, ai);
+        for (int i = 0; i < 16; ++i) {  // thread = probe row `lane`: conflict-free (stride 17)
+          stage[0 * 32 * kStageRow + lane * kStageRow + i] = cr[i];
+          stage[1 * 32 * kStageRow + lane * kStageRow + i] = cg[i];
+          stage[2 * 32 * kStageRow + lane * kStageRow + i] = cb[i];
         }
+        __syncwarp();
+        const int tex0 = 2 * blk * kOct + tx;  // texel (tx, 2 blk); + 8 for the second row
+        const float s16a = __ldg(&it.wsum16[tex0]), s32a = __ldg(&it.wsum32[tex0]);
+        const float s16b = __ldg(&it.wsum16[tex0 + kOct]), s32b = __ldg(&it.wsum32[tex0 + kOct]);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          int tex = blk * 16 + i;
-          int tx = tex % kOct, ty = tex / kOct;
-          size_t ai = (size_t)(kProbePix * pzAll + 1 + ty) * it.atlasW + (kProbePix * px + 1 + tx);
-          float4 old = olds[i];
-          float s16 = __ldg(&it.wsum16[tex]), s32 = __ldg(&it.wsum32[tex]);
+        for (int k = 0; k < 16; ++k) {
+          const int g = k >> 1, row2 = k & 1, ty = 2 * blk + row2;
+          if (!((liveMask >> g) & 1u)) continue;
+          const int sp = (4 * g + pp) * kStageRow + row2 * kOct + tx;
+          const float rr0 = stage[sp], gg0 = stage[32 * kStageRow + sp], bb0 = stage[2 * 32 * kStageRow + sp];
+          const float s16 = row2 ? s16b : s16a, s32 = row2 ? s32b : s32a;
+          const float4 old = olds[k];
           float4 out;
           if (bake) {
             float tw = old.w + s32;
-            float rr = cr[i] + old.x * old.w, gg = cg[i] + old.y * old.w, bb = cb[i] + old.z * old.w;
+            float rr = rr0 + old.x * old.w, gg = gg0 + old.y * old.w, bb = bb0 + old.z * old.w;
             if (tw > 1e-6f) { rr /= tw; gg /= tw; bb /= tw; }
             out = make_float4(rr, gg, bb, tw);
           } else {
-            float rr = cr[i], gg = cg[i], bb = cb[i];
+            float rr = rr0, gg = gg0, bb = bb0;
             if (s16 > 1e-6f) { float inv = 1.0f / s16; rr *= inv; gg *= inv; bb *= inv; }
             out = make_float4(rr * a + old.x * h, gg * a + old.y * h, bb * a + old.z * h, s32 * a + old.w * h);
           }
-          storeTexel(it.atlas, it.atlasFmt, ai, out);
+          storeTexel(it.atlas, it.atlasFmt, base[g] + (size_t)ty * it.atlasW, out);
         }
+        __syncwarp();  // the stage is rewritten by the next block
       }
+      if (!ok) break;
       tcFenceBefore();
       mbarArrive(&accEmpty[b]);
     }
@@ -500,7 +537,7 @@ cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const vo
     memcpy(&maps.r[i], hostItems[i].mapR, sizeof(CUtensorMap));
     memcpy(&maps.w[i], hostItems[i].mapW, sizeof(CUtensorMap));
   }
-  size_t smem = (size_t)kStages * kStageBytes + 1024;
+  size_t smem = kSmemTc;
   auto kern = elemFmt == 0 ? k_conv_tc<0> : k_conv_tc<1>;
   // per-process, per-device launch setup (the attribute is a property of the function on each device)
   static std::mutex mu;

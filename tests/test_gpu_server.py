@@ -22,15 +22,17 @@ def _scenes(ctx):
 
 def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30):
     srv = ddgi.Server(ctx, budget, max_batch=max_batch, in_flight=in_flight, conv_mode=conv_mode)
-    outs, ids = [], []
+    # outputs and descriptions first, so the requests arrive back to back (a pinned allocation between two
+    # submissions would let each request finish before the next one arrives)
+    outs = [torch.empty(10 * dims[0] * 10 * dims[2] * dims[1] * 4, dtype=torch.float32).pin_memory()
+            for dims, _, _ in REQS]
+    work = [(ddgi.grid_desc(dims, rays_per_probe=n, hysteresis=0.97),
+             ddgi.FrameParams(camera_pos=(0.3 * i, 1.0, -0.2 * i), rotation=scenes.rotation(i, 0)), si)
+            for i, (dims, n, si) in enumerate(REQS)]
+    ids = []
     try:
-        for i, (dims, n, si) in enumerate(REQS):
-            d = ddgi.grid_desc(dims, rays_per_probe=n, hysteresis=0.97)
-            nbytes = 10 * dims[0] * 10 * dims[2] * dims[1] * 16
-            out = torch.empty(nbytes // 4, dtype=torch.float32).pin_memory()
-            fp = ddgi.FrameParams(camera_pos=(0.3 * i, 1.0, -0.2 * i), rotation=scenes.rotation(i, 0))
-            ids.append(srv.submit(scs[si], d, fp, out.data_ptr(), tag=i))
-            outs.append(out)
+        for i, (d, fp, si) in enumerate(work):
+            ids.append(srv.submit(scs[si], d, fp, outs[i].data_ptr(), tag=i))
         srv.drain(120.0)
         for rid in ids:
             assert srv.status(rid).state == L.DDGI_REQUEST_DONE
