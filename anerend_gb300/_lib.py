@@ -48,6 +48,9 @@ MESH_INFO = np.dtype([("minPos", "<f4", 4), ("maxPos", "<f4", 4), ("vertexOffset
 MATERIAL_INFO = np.dtype([("baseColFac", "<f4", 4), ("emissive", "<f4", 4), ("bindlessIndices", "<i4", 4),
                           ("metRough", "<f4", 4)])
 INSTANCE = np.dtype([("transform", "<f4", 12), ("mesh", "<u4"), ("material", "<u4"), ("reserved", "<u4", 2)])
+SURFACE_POINT = np.dtype([("position", "<f4", 3), ("metallic", "<f4"), ("normal", "<f4", 3), ("roughness", "<f4"),
+                          ("albedo", "<f4", 3), ("shadow", "<f4")])
+assert SURFACE_POINT.itemsize == 48
 assert PACKED_VERTEX.itemsize == 96 and MESH_INFO.itemsize == 48
 assert MATERIAL_INFO.itemsize == 64 and INSTANCE.itemsize == 64
 
@@ -156,6 +159,7 @@ SIGNATURES = {
     "ddgi_atlas_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_atlas_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_rays_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ddgi_query_irradiance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ddgi_batch_create": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int, C.POINTER(C.c_void_p)]),
     "ddgi_batch_destroy": (None, [C.c_void_p]),
     "ddgi_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),

@@ -738,6 +738,22 @@ int ddgi_rays_download(DdgiGrid* g, float* radiance, int32_t* hits, float* latti
   return DDGI_OK;
 }
 
+int ddgi_query_irradiance(DdgiGrid* g, const DdgiFrame* frame, const DdgiSurfacePoint* points, uint64_t count,
+                          float* ambient, void* stream) {
+  if (!g || !frame) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_query_irradiance");
+  DdgiContext* ctx = g->ctx;
+  if (count == 0) return DDGI_OK;
+  if (!points || !ambient) return fail(ctx, DDGI_EINVAL, "NULL points or output");
+  if (((uintptr_t)points | (uintptr_t)ambient) & 15) return fail(ctx, DDGI_EINVAL, "points and ambient must be 16-byte aligned");
+  FrameGPU f{};
+  int rc = frameToGPU(ctx, frame, f);
+  if (rc) return rc;
+  CK(launchQueryIrradiance(g->g, f, g->atlas[g->cur], points, (long long)count, (float4*)ambient,
+                           (cudaStream_t)stream),
+     "irradiance query");
+  return DDGI_OK;
+}
+
 // ---- raw kernels --------------------------------------------------------------------------------------
 int ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* stream) {
   if (numRays <= 0 || numRays > (1 << 20) || !rot || !dirs) return DDGI_EINVAL;

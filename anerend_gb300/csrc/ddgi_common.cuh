@@ -240,6 +240,7 @@ struct GridGPU {
   void* rad16;     // when set, the trace also writes planar 16-bit radiance (row c * pTotal + p, N per row)
   int rad16Fmt;    // 0 FP16, 1 BF16
   int pTotal;      // probes of the grid (rows per channel of rad16)
+  int samplerClamp;  // atlas sampler addressing: 0 REPEAT (the trace pass), 1 CLAMP_TO_EDGE (the deferred pass)
 };
 
 struct FrameGPU {

@@ -39,6 +39,10 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream);
 
 
+// Ambient term of G-buffer points from an atlas (deferred_tiled.comp:263-299), CLAMP_TO_EDGE sampling.
+cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const void* atlas, const DdgiSurfacePoint* pts,
+                                  long long count, float4* out, cudaStream_t stream);
+
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream);
 // Convolution + hysteresis (or bake accumulation) of layers [layerBegin, layerEnd) into `atlas`.

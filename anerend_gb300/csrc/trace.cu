@@ -52,14 +52,22 @@ DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int
   float fx = ox - fx0, fy = oy - fy0;
   int x0 = sx + (int)fx0, y0 = sy + (int)fy0;
   int x1 = x0 + 1, y1 = y0 + 1;
-  // REPEAT wrap. The indices are never negative (ix, iy, iz >= 0; the octahedral offset is >= -1 and sx,
-  // sy >= 1) and stay below W + 10 and H + 10 Z + 10 <= 3 H, so conditional subtractions equal the modulo.
-  if (x0 >= g.atlasW) x0 -= g.atlasW;
-  if (x1 >= g.atlasW) x1 -= g.atlasW;
-  if (y0 >= g.atlasH) y0 -= g.atlasH;
-  if (y0 >= g.atlasH) y0 -= g.atlasH;
-  if (y1 >= g.atlasH) y1 -= g.atlasH;
-  if (y1 >= g.atlasH) y1 -= g.atlasH;
+  // The indices are never negative (ix, iy, iz >= 0; the octahedral offset is >= -1 and sx, sy >= 1) and
+  // stay below W + 10 and H + 10 Z + 10 <= 3 H. REPEAT: conditional subtractions equal the modulo;
+  // CLAMP_TO_EDGE: the last texel row / column.
+  if (g.samplerClamp) {
+    x0 = min(x0, g.atlasW - 1);
+    x1 = min(x1, g.atlasW - 1);
+    y0 = min(y0, g.atlasH - 1);
+    y1 = min(y1, g.atlasH - 1);
+  } else {
+    if (x0 >= g.atlasW) x0 -= g.atlasW;
+    if (x1 >= g.atlasW) x1 -= g.atlasW;
+    if (y0 >= g.atlasH) y0 -= g.atlasH;
+    if (y0 >= g.atlasH) y0 -= g.atlasH;
+    if (y1 >= g.atlasH) y1 -= g.atlasH;
+    if (y1 >= g.atlasH) y1 -= g.atlasH;
+  }
   float4 t00 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x0);
   float4 t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
   float4 t01 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x0);
@@ -435,6 +443,45 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
       id = -1;
     }
   }
+}
+
+// Atlas consumer (deferred_tiled.comp:263-299): the ambient term of G-buffer points, one thread per point.
+__global__ void __launch_bounds__(256) k_query_irradiance(GridGPU g, FrameGPU f, const void* __restrict__ atlas,
+                                                          const DdgiSurfacePoint* __restrict__ pts, long long count,
+                                                          float4* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const DdgiSurfacePoint& p = pts[i];
+    const float3 wp = f3(p.position[0], p.position[1], p.position[2]);
+    const float3 n = normalize3(f3(p.normal[0], p.normal[1], p.normal[2]));  // :177
+    const float3 albedo = f3(p.albedo[0], p.albedo[1], p.albedo[2]);
+    const float shade = clampf(p.shadow, 0.3f, 1.0f);
+    float3 amb = f3(0.f, 0.f, 0.f);  // :203
+    if (f.flags & DDGI_UBO_DDGI_FLAG) {
+      const float3 d = f.camPos - wp;
+      if (sqrtf(dot3(d, d)) > (float)g.X * g.step.x / 2.0f)  // :271-273
+        amb += f3(0.3f, 0.3f, 0.3f) * f.skyIntensity * albedo * shade;
+      else
+        amb += calcIndirectDiffuse(g, f, atlas, n, albedo, p.metallic, p.roughness, wp, f.camPos);  // :289-295
+    } else {
+      amb = f3(0.3f, 0.3f, 0.3f) * albedo * shade;  // :298
+    }
+    out[i] = make_float4(amb.x, amb.y, amb.z, 0.0f);
+  }
+}
+
+cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const void* atlas, const DdgiSurfacePoint* pts,
+                                  long long count, float4* out, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  GridGPU gc = g;
+  gc.samplerClamp = 1;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long blocks = (count + 255) / 256;
+  if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+  k_query_irradiance<<<(unsigned)blocks, 256, 0, stream>>>(gc, f, atlas, pts, count, out);
+  return cudaGetLastError();
 }
 
 // Rotated lattices of many grids: one block row per item.

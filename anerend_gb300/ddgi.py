@@ -198,6 +198,14 @@ class ProbeGrid:
                                                        _ptr(lat), stream))
         return rad, hit, lat
 
+    def query_irradiance(self, frame: "FrameParams", points_ptr: int, count: int, ambient_ptr: int,
+                         stream: int = 0) -> None:
+        """Ambient term of `count` device DdgiSurfacePoint records into device float4 (deferred_tiled.comp's
+        DDGI block, CLAMP_TO_EDGE sampling), stream-ordered."""
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_query_irradiance(self.handle, C.byref(f), points_ptr, count, ambient_ptr,
+                                                          stream))
+
     def close(self) -> None:
         if self.handle:
             self.ctx.lib.ddgi_grid_destroy(self.handle)

@@ -249,6 +249,28 @@ int  ddgi_atlas_upload(DdgiGrid* grid, const void* host, uint64_t bytes, void* s
  * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
 int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
 
+/* ---- atlas consumer: indirect diffuse light of G-buffer points ------------------------------------------- */
+
+/* One G-buffer point (48 bytes): what deferred_tiled.comp:166-194 reads for a pixel. `normal` need not be
+ * unit length (the shader normalises it); `shadow` is the direct-light visibility the pass computed (1 lit). */
+typedef struct DdgiSurfacePoint {
+  float position[3];
+  float metallic;
+  float normal[3];
+  float roughness;
+  float albedo[3];
+  float shadow;
+} DdgiSurfacePoint;
+
+/* Ambient term of each point from the grid's current atlas: the DDGI block of deferred_tiled.comp:263-299 with
+ * the CLAMP_TO_EDGE sampler the deferred pass binds (DeferredLightingRenderPass.cpp:192-199), no baked tile
+ * atlases. With DDGI_UBO_DDGI_FLAG in frame->flags: calcIndirectDiffuseLight seen from frame->cameraPos, or
+ * skyIntensity * 0.3 * albedo * clamp(shadow, 0.3, 1) beyond X * step.x / 2 from the camera; without it:
+ * 0.3 * albedo * clamp(shadow, 0.3, 1). points: device array of `count` records; ambient: device array of
+ * `count` float4 (rgb, w = 0). Stream-ordered; no counterpart call in the reference (a shader block). */
+int  ddgi_query_irradiance(DdgiGrid* grid, const DdgiFrame* frame, const DdgiSurfacePoint* points, uint64_t count,
+                           float* ambient, void* stream);
+
 /* ---- batched form: many grids in one persistent trace launch and one convolution launch ---------------- */
 
 typedef struct DdgiBatch DdgiBatch;

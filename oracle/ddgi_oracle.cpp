@@ -335,6 +335,7 @@ struct Grid {
   d3 step;
   double originY;
   uint32_t options;
+  bool clampToEdge = false;  // atlas sampler addressing: REPEAT (trace pass) or CLAMP_TO_EDGE (deferred pass)
 };
 Grid makeGrid(const DdgiGridDesc* d) {
   Grid g;
@@ -367,7 +368,8 @@ void probeFrame(const Grid& g, const DdgiFrame* f, d3& stepv, d3& offv) {
   }
 }
 
-// sampleSingleProbe (pbr_light.glsl:168-188) with exact bilinear weights and REPEAT addressing
+// sampleSingleProbe (pbr_light.glsl:168-188) with exact bilinear weights; REPEAT addressing, or
+// CLAMP_TO_EDGE for the deferred pass (DeferredLightingRenderPass.cpp:192-199)
 d3 sampleSingleProbe(const Grid& g, const double* atlas, int ix, int iy, int iz, d3 n) {
   if (g.options & DDGI_GRID_EDGE_CLAMP) {
     ix = std::min(std::max(ix, 0), g.X - 1);
@@ -381,7 +383,8 @@ d3 sampleSingleProbe(const Grid& g, const double* atlas, int ix, int iy, int iz,
   double fx0 = std::floor(tx), fy0 = std::floor(ty);
   double fx = tx - fx0, fy = ty - fy0;
   int x0 = sx + (int)fx0, y0 = sy + (int)fy0;
-  auto wrap = [](int v, int m) { return ((v % m) + m) % m; };
+  const bool clampEdge = g.clampToEdge;
+  auto wrap = [clampEdge](int v, int m) { return clampEdge ? std::min(std::max(v, 0), m - 1) : ((v % m) + m) % m; };
   int xs[2] = {wrap(x0, g.atlasW), wrap(x0 + 1, g.atlasW)};
   int ys[2] = {wrap(y0, g.atlasH), wrap(y0 + 1, g.atlasH)};
   double wx[2] = {1.0 - fx, fx}, wy[2] = {1.0 - fy, fy};
@@ -671,6 +674,36 @@ int oracle_translate(const DdgiGridDesc* desc, const void* in, void* out, int dx
     for (int y = 0; y < h; ++y)
       std::memcpy(dst + ((size_t)(dstY + y) * g.atlasW + dstX) * texelBytes,
                   tmp.data() + ((size_t)(srcY + y) * g.atlasW + srcX) * texelBytes, (size_t)w * texelBytes);
+  }
+  return 0;
+}
+
+// Ambient term of G-buffer points (deferred_tiled.comp:166-203, 263-299): points are DdgiSurfacePoint
+// records, atlas the current atlas in FP64 RGBA, out 3 doubles per point.
+int oracle_query_irradiance(const DdgiGridDesc* desc, const DdgiFrame* f, const double* atlas,
+                            const DdgiSurfacePoint* pts, int64_t count, double* out) {
+  Grid g = makeGrid(desc);
+  g.clampToEdge = true;
+  const d3 cam = D3(f->cameraPos[0], f->cameraPos[1], f->cameraPos[2]);
+  for (int64_t i = 0; i < count; ++i) {
+    const DdgiSurfacePoint& p = pts[i];
+    const d3 wp = D3(p.position[0], p.position[1], p.position[2]);
+    const d3 n = normalize(D3(p.normal[0], p.normal[1], p.normal[2]));  // :177
+    const d3 albedo = D3(p.albedo[0], p.albedo[1], p.albedo[2]);
+    const double shade = std::min(std::max((double)p.shadow, 0.3), 1.0);
+    d3 amb = D3(0, 0, 0);
+    if (f->flags & DDGI_UBO_DDGI_FLAG) {
+      const d3 d = cam - wp;
+      if (std::sqrt(dot(d, d)) > g.X * g.step.x / 2.0)  // :271-273
+        amb = amb + albedo * (f->skyIntensity * 0.3 * shade);
+      else
+        amb = amb + calcIndirect(g, f, atlas, n, albedo, p.metallic, p.roughness, wp, cam);  // :289-295
+    } else {
+      amb = albedo * (0.3 * shade);  // :298
+    }
+    out[3 * i] = amb.x;
+    out[3 * i + 1] = amb.y;
+    out[3 * i + 2] = amb.z;
   }
   return 0;
 }

@@ -57,6 +57,8 @@ def load():
         lib.oracle_num_triangles.argtypes = [vp]
         lib.oracle_closest_hit.restype = ip
         lib.oracle_closest_hit.argtypes = [vp, vp, vp, vp, vp, vp]
+        lib.oracle_query_irradiance.restype = ip
+        lib.oracle_query_irradiance.argtypes = [vp, vp, vp, vp, C.c_int64, vp]
         _lib = lib
     return _lib
 
@@ -201,3 +203,13 @@ def translate(desc, atlas: np.ndarray, dx: int, dz: int) -> np.ndarray:
     out = np.empty_like(a)
     load().oracle_translate(C.addressof(desc), _p(a), _p(out), dx, dz, a.itemsize * a.shape[-1])
     return out
+
+
+def query_irradiance(desc, frame, atlas: np.ndarray, points: np.ndarray) -> np.ndarray:
+    """deferred_tiled.comp:263-299 on FP64: ambient term (count x 3) of SURFACE_POINT records from `atlas`."""
+    a = np.ascontiguousarray(atlas, np.float64)
+    pts = np.ascontiguousarray(points)
+    out = np.empty((len(pts), 3), np.float64)
+    load().oracle_query_irradiance(C.addressof(desc), C.addressof(frame), _p(a), _p(pts), len(pts), _p(out))
+    return out
+

@@ -206,3 +206,84 @@ def test_octant_fan_closed():
                 assert gid >= 0
     finally:
         s.close()
+
+
+# ---- atlas consumer (deferred_tiled.comp:263-299) --------------------------------------------------
+
+def _consumer_desc(dims=(8, 4, 8)):
+    d = L.GridDesc()
+    d.dims[:] = list(dims)
+    d.step[:] = [1.0, 2.0, 1.0]
+    d.raysPerProbe = 64
+    d.hysteresis = 0.97
+    return d
+
+
+def _points(pos, normal, albedo=(0.5, 0.6, 0.7), metallic=0.0, roughness=0.5, shadow=1.0):
+    p = np.zeros(len(pos), L.SURFACE_POINT)
+    p["position"] = pos
+    p["normal"] = normal
+    p["albedo"] = albedo
+    p["metallic"] = metallic
+    p["roughness"] = roughness
+    p["shadow"] = shadow
+    return p
+
+
+def _frame(flags, cam=(0.0, 0.0, 0.0), sky=1.0):
+    f = L.Frame()
+    f.cameraPos[:] = list(cam)
+    f.flags = flags
+    f.skyIntensity = sky
+    return f
+
+
+def test_consumer_constant_atlas_closed_form():
+    """A constant atlas c: every probe sample is c, so sampleProbe = c * 0.5 * 3.1415926 and the ambient term is
+    kD * (that * albedo) with kS = fresnelSchlickRoughness(max(n.V, 0), F0, roughness^2) (pbr_light.glsl)."""
+    d = _consumer_desc()
+    atlas = np.zeros((10 * 8 * 4, 10 * 8, 4))
+    atlas[..., :3] = [0.2, 0.4, 0.8]
+    cam = np.array([0.3, 1.0, -0.4])
+    pos = np.array([[0.5, 1.7, 0.25], [-2.2, 3.1, 1.9]])
+    nrm = np.array([[0.0, 1.0, 0.0], [1.0, 1.0, 0.0]])
+    out = oracle.query_irradiance(d, _frame(L.DDGI_UBO_DDGI_FLAG, cam), atlas, _points(pos, nrm))
+    albedo = np.array([0.5, 0.6, 0.7])
+    for k in range(2):
+        n = nrm[k] / np.linalg.norm(nrm[k])
+        v = cam - pos[k]
+        v /= np.linalg.norm(v)
+        ndv = max(float(n @ v), 0.0)
+        f0 = np.full(3, 0.04)
+        ks = f0 + (np.maximum(1.0 - 0.25, f0) - f0) * (1.0 - ndv) ** 5
+        want = (1.0 - ks) * (np.array([0.2, 0.4, 0.8]) * 0.5 * 3.1415926 * albedo)
+        assert np.allclose(out[k], want, rtol=1e-6, atol=0)  # float32 inputs
+
+
+def test_consumer_far_points_and_no_ddgi():
+    d = _consumer_desc()
+    atlas = np.ones((320, 80, 4))
+    pts = _points(np.array([[10.0, 1.0, 0.0], [0.0, 1.0, 0.0]]), np.array([[0, 1, 0], [0, 1, 0]]), shadow=0.1)
+    # beyond X * step.x / 2 = 4 from the camera: skyIntensity * 0.3 * albedo * clamp(shadow, 0.3, 1)
+    far = oracle.query_irradiance(d, _frame(L.DDGI_UBO_DDGI_FLAG, sky=2.0), atlas, pts[:1])
+    assert np.allclose(far[0], 2.0 * 0.3 * np.array([0.5, 0.6, 0.7]) * 0.3)
+    off = oracle.query_irradiance(d, _frame(0), atlas, pts)
+    assert np.allclose(off, 0.3 * np.array([0.5, 0.6, 0.7]) * 0.3)
+
+
+def test_consumer_clamps_to_edge():
+    """At the +x edge of the grid the +1 neighbour's texels lie past the atlas: the deferred pass's
+    CLAMP_TO_EDGE sampler reads the last column (the trace pass would wrap to column 0)."""
+    d = _consumer_desc()
+    atlas = np.zeros((320, 80, 4))
+    atlas[:, :40, :3] = 1.0   # left half bright: reached only by wrapping
+    atlas[:, 40:, :3] = 0.25
+    # a point in the last probe cell along x (camera at the origin: probes x = -4..3), normal +x
+    pts = _points(np.array([[3.6, 1.0, 0.5]]), np.array([[1.0, 0.0, 0.0]]))
+    out = oracle.query_irradiance(d, _frame(L.DDGI_UBO_DDGI_FLAG), atlas, pts)
+    n = np.array([1.0, 0.0, 0.0])
+    v = -np.array([3.6, 1.0, 0.5])
+    v /= np.linalg.norm(v)
+    ks = 0.04 + (np.maximum(0.75, 0.04) - 0.04) * (1.0 - max(float(n @ v), 0.0)) ** 5
+    want = (1.0 - ks) * (0.25 * 0.5 * 3.1415926 * np.array([0.5, 0.6, 0.7]))
+    assert np.allclose(out[0], want, rtol=1e-6)  # every sample from the dim right half
