@@ -725,6 +725,46 @@ int ddgi_atlas_upload(DdgiGrid* g, const void* host, uint64_t bytes, void* strea
   return DDGI_OK;
 }
 
+int ddgi_atlas_export_rgba16f(DdgiGrid* g, void* host, uint64_t bytes, void* stream) {
+  if (!g || !host) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_export_rgba16f");
+  DdgiContext* ctx = g->ctx;
+  const long long texels = (long long)g->g.atlasW * g->g.atlasH;
+  if (bytes != 8ull * (uint64_t)texels) return fail(ctx, DDGI_EINVAL, "RGBA16F atlas is %llu bytes", 8ull * texels);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->desc.atlasFormat == DDGI_FORMAT_RGBA16F) {
+    CK(cudaMemcpyAsync(host, g->atlas[g->cur], bytes, cudaMemcpyDeviceToHost, st), "atlas export");
+  } else {
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, bytes, st), "atlas export scratch");
+    cudaError_t e = launchAtlasToHalf((const float4*)g->atlas[g->cur], tmp, texels, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(tmp, st);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "atlas export");
+  }
+  CK(cudaStreamSynchronize(st), "atlas export sync");
+  return DDGI_OK;
+}
+
+int ddgi_atlas_import_rgba16f(DdgiGrid* g, const void* host, uint64_t bytes, void* stream) {
+  if (!g || !host) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_import_rgba16f");
+  DdgiContext* ctx = g->ctx;
+  const long long texels = (long long)g->g.atlasW * g->g.atlasH;
+  if (bytes != 8ull * (uint64_t)texels) return fail(ctx, DDGI_EINVAL, "RGBA16F atlas is %llu bytes", 8ull * texels);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->desc.atlasFormat == DDGI_FORMAT_RGBA16F) {
+    CK(cudaMemcpyAsync(g->atlas[g->cur], host, bytes, cudaMemcpyHostToDevice, st), "atlas import");
+  } else {
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, bytes, st), "atlas import scratch");
+    cudaError_t e = cudaMemcpyAsync(tmp, host, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launchAtlasFromHalf(tmp, (float4*)g->atlas[g->cur], texels, st);
+    cudaFreeAsync(tmp, st);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "atlas import");
+  }
+  CK(cudaStreamSynchronize(st), "atlas import sync");
+  return DDGI_OK;
+}
+
 int ddgi_rays_download(DdgiGrid* g, float* radiance, int32_t* hits, float* lattice, void* stream) {
   if (!g) return DDGI_EINVAL;
   DdgiContext* ctx = g->ctx;

@@ -90,6 +90,9 @@ cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad
 
 // Translation copy (IrradianceProbeTranslationPass.cpp:83-168): out = in shifted by (sx, sz) probes.
 cudaError_t launchTranslate(const GridGPU& g, const void* in, void* out, int sx, int sz, cudaStream_t stream);
+// RGBA32F <-> RGBA16F texel conversion (round to nearest even) of `texels` atlas texels.
+cudaError_t launchAtlasToHalf(const float4* in, void* out, long long texels, cudaStream_t stream);
+cudaError_t launchAtlasFromHalf(const void* in, float4* out, long long texels, cudaStream_t stream);
 // Fill every texel of the atlas with (0,0,0,1) (clearConvTex, IrradianceProbeConvolvePass.cpp:9-47).
 cudaError_t launchClearAtlas(const GridGPU& g, void* atlas, cudaStream_t stream);
 

@@ -73,4 +73,30 @@ cudaError_t launchClearAtlas(const GridGPU& g, void* atlas, cudaStream_t stream)
   return cudaGetLastError();
 }
 
+// RGBA32F <-> RGBA16F atlas texels (round to nearest even), for persistence in the reference's layout.
+__global__ void k_atlas_to_half(const float4* __restrict__ in, uint2* __restrict__ out, long long total) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const float4 v = in[i];
+    __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    out[i] = make_uint2(*reinterpret_cast<uint32_t*>(&a), *reinterpret_cast<uint32_t*>(&b));
+  }
+}
+__global__ void k_atlas_from_half(const uint2* __restrict__ in, float4* __restrict__ out, long long total) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const uint2 u = in[i];
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    out[i] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+cudaError_t launchAtlasToHalf(const float4* in, void* out, long long texels, cudaStream_t stream) {
+  k_atlas_to_half<<<gridFor(texels), 256, 0, stream>>>(in, (uint2*)out, texels);
+  return cudaGetLastError();
+}
+cudaError_t launchAtlasFromHalf(const void* in, float4* out, long long texels, cudaStream_t stream) {
+  k_atlas_from_half<<<gridFor(texels), 256, 0, stream>>>((const uint2*)in, out, texels);
+  return cudaGetLastError();
+}
+
 }  // namespace ddgi

@@ -198,6 +198,17 @@ class ProbeGrid:
                                                        _ptr(lat), stream))
         return rad, hit, lat
 
+    def export_atlas_rgba16f(self, stream: int = 0) -> np.ndarray:
+        """The atlas in the reference's persisted layout: (10 Z Y, 10 X, 4) float16 (downloadDDGIAtlas)."""
+        b = self.buffers
+        out = np.empty((b.atlasHeight, b.atlasWidth, 4), np.float16)
+        self.ctx.check(self.ctx.lib.ddgi_atlas_export_rgba16f(self.handle, _ptr(out), out.nbytes, stream))
+        return out
+
+    def import_atlas_rgba16f(self, arr: np.ndarray, stream: int = 0) -> None:
+        arr = np.ascontiguousarray(arr, np.float16)
+        self.ctx.check(self.ctx.lib.ddgi_atlas_import_rgba16f(self.handle, _ptr(arr), arr.nbytes, stream))
+
     def query_irradiance(self, frame: "FrameParams", points_ptr: int, count: int, ambient_ptr: int,
                          stream: int = 0) -> None:
         """Ambient term of `count` device DdgiSurfacePoint records into device float4 (deferred_tiled.comp's

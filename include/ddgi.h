@@ -244,6 +244,13 @@ int  ddgi_update(DdgiGrid* grid, const DdgiScene* scene, const DdgiFrame* frame,
 int  ddgi_atlas_download(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
 int  ddgi_atlas_upload(DdgiGrid* grid, const void* host, uint64_t bytes, void* stream);
 
+/* Baked-atlas persistence in the reference's layout: the atlas as RGBA16F texels, 8 bytes each, width 10 X,
+ * height 10 Z Y - the data of the asset::Texture that downloadDDGIAtlas returns (VulkanRenderer.cpp:2706-2771,
+ * format RGBA16F_SFLOAT, one mip) - converted from / to the grid's atlas format (round to nearest even).
+ * `bytes` must be 8 x atlasWidth x atlasHeight. Both calls are complete when they return. */
+int  ddgi_atlas_export_rgba16f(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
+int  ddgi_atlas_import_rgba16f(DdgiGrid* grid, const void* host, uint64_t bytes, void* stream);
+
 /* Reads back the grid's ray buffers into host memory (any pointer may be NULL): radiance is
  * rayWidth*rayHeight RGBA floats, hits rayWidth*rayHeight int32 (needs DDGI_GRID_RECORD_HITS; global triangle
  * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
