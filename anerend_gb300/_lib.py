@@ -51,6 +51,9 @@ INSTANCE = np.dtype([("transform", "<f4", 12), ("mesh", "<u4"), ("material", "<u
 SURFACE_POINT = np.dtype([("position", "<f4", 3), ("metallic", "<f4"), ("normal", "<f4", 3), ("roughness", "<f4"),
                           ("albedo", "<f4", 3), ("shadow", "<f4")])
 assert SURFACE_POINT.itemsize == 48
+RAY = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("direction", "<f4", 3), ("tmax", "<f4")])
+HIT = np.dtype([("t", "<f4"), ("b1", "<f4"), ("b2", "<f4"), ("triangle", "<i4")])
+DDGI_RAY_ANY_HIT = 1
 assert PACKED_VERTEX.itemsize == 96 and MESH_INFO.itemsize == 48
 assert MATERIAL_INFO.itemsize == 64 and INSTANCE.itemsize == 64
 
@@ -161,6 +164,8 @@ SIGNATURES = {
     "ddgi_rays_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ddgi_atlas_export_rgba16f": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_atlas_import_rgba16f": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "ddgi_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "ddgi_shadow_mask": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ddgi_query_irradiance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ddgi_batch_create": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int, C.POINTER(C.c_void_p)]),
     "ddgi_batch_destroy": (None, [C.c_void_p]),

@@ -778,6 +778,42 @@ int ddgi_rays_download(DdgiGrid* g, float* radiance, int32_t* hits, float* latti
   return DDGI_OK;
 }
 
+namespace {
+int traceQuery(DdgiScene* sc, const DdgiRay* rays, const float* points, uint64_t count, bool anyHit, DdgiHit* hits,
+               float3 shadowDir, float* vis, cudaStream_t st) {
+  DdgiContext* ctx = sc->ctx;
+  if (count == 0) return DDGI_OK;
+  unsigned long long* counter = nullptr;
+  CK(cudaMallocAsync(&counter, sizeof(unsigned long long), st), "ray query counter");
+  cudaError_t e = launchTraceRays(sc->view.bvh, sc->view.bvh.wnodes != nullptr, rays, (long long)count, anyHit, hits,
+                                  (const float4*)points, shadowDir, vis, counter, ctx->dErr, st);
+  cudaFreeAsync(counter, st);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "ray query");
+  return DDGI_OK;
+}
+}  // namespace
+
+int ddgi_trace_rays(DdgiScene* sc, const DdgiRay* rays, uint64_t count, uint32_t flags, DdgiHit* hits, void* stream) {
+  if (!sc) return DDGI_EINVAL;
+  DdgiContext* ctx = sc->ctx;
+  if (count && (!rays || !hits)) return fail(ctx, DDGI_EINVAL, "NULL rays or hits");
+  if (flags & ~DDGI_RAY_ANY_HIT) return fail(ctx, DDGI_EINVAL, "unknown ray flags 0x%x", flags);
+  if (((uintptr_t)rays | (uintptr_t)hits) & 15) return fail(ctx, DDGI_EINVAL, "rays and hits must be 16-byte aligned");
+  return traceQuery(sc, rays, nullptr, count, (flags & DDGI_RAY_ANY_HIT) != 0, hits, f3(0.f, 0.f, 0.f), nullptr,
+                    (cudaStream_t)stream);
+}
+
+int ddgi_shadow_mask(DdgiScene* sc, const DdgiFrame* frame, const float* points, uint64_t count, float* visibility,
+                     void* stream) {
+  if (!sc || !frame) return DDGI_EINVAL;
+  DdgiContext* ctx = sc->ctx;
+  if (count && (!points || !visibility)) return fail(ctx, DDGI_EINVAL, "NULL points or visibility");
+  if ((uintptr_t)points & 15) return fail(ctx, DDGI_EINVAL, "points must be 16-byte aligned");
+  // shadow.rgen:58: direction = -ubo.lightDir.xyz, as given (not normalised)
+  const float3 dir = f3(-frame->lightDir[0], -frame->lightDir[1], -frame->lightDir[2]);
+  return traceQuery(sc, nullptr, points, count, true, nullptr, dir, visibility, (cudaStream_t)stream);
+}
+
 int ddgi_query_irradiance(DdgiGrid* g, const DdgiFrame* frame, const DdgiSurfacePoint* points, uint64_t count,
                           float* ambient, void* stream) {
   if (!g || !frame) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_query_irradiance");

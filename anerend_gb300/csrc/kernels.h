@@ -39,6 +39,11 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream);
 
 
+// Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's
+// visibility mask along shadowDir. counter: one device word of scratch.
+cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
+                            DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream);
 // Ambient term of G-buffer points from an atlas (deferred_tiled.comp:263-299), CLAMP_TO_EDGE sampling.
 cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const void* atlas, const DdgiSurfacePoint* pts,
                                   long long count, float4* out, cudaStream_t stream);

@@ -445,6 +445,107 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
   }
 }
 
+// Ray queries (DdgiRay -> DdgiHit) on the persistent refill loop of the probe traversal. kShadowMask:
+// the rays are shadow.rgen's (origin = the point, direction = -lightDir, [0.1, 50], any hit) and the output
+// is its visibility mask; points with w != 0 are sky pixels (visibility 1, no ray).
+template <bool kWide, bool kAnyHit, bool kShadowMask>
+__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+    k_trace_rays(BvhRef bvh, const DdgiRay* __restrict__ rays, const float4* __restrict__ points, float3 shadowDir,
+                 long long count, unsigned long long* __restrict__ counter, int refillLanes, DdgiHit* __restrict__ hits,
+                 float* __restrict__ vis, uint32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  long long id = -1;
+  bool drained = false;
+  WRay ray;
+  HitInfo hit;
+  typename TravOf<kWide>::T st;
+  float tmin = kTMin;
+  auto finish = [&](long long i) {
+    if (kShadowMask) {
+      vis[i] = hit.leaf >= 0 ? 0.0f : 1.0f;  // shadow.rchit:14 / shadow.rmiss:12
+    } else {
+      int gid = -1;
+      if (hit.leaf >= 0) gid = __float_as_int(__ldg(&bvh.tris[3 * hit.leaf].w));
+      hits[i] = DdgiHit{hit.leaf >= 0 ? hit.t : 0.0f, hit.leaf >= 0 ? hit.b1 : 0.0f, hit.leaf >= 0 ? hit.b2 : 0.0f, gid};
+    }
+  };
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, id < 0);
+    if (drained && idle == 0xffffffffu) break;
+    if (!drained && __popc(idle) >= refillLanes) {
+      const int need = __popc(idle);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(counter, (unsigned long long)need);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((long long)base + need >= count) drained = true;
+      const long long cand = (long long)base + __popc(idle & below);
+      if (id < 0 && cand < count) {
+        float3 o, d;
+        float t1;
+        bool sky = false;
+        if (kShadowMask) {
+          const float4 p = points[cand];
+          o = xyz(p);
+          d = shadowDir;
+          tmin = kTMin;
+          t1 = kTMax;
+          sky = p.w != 0.0f;
+        } else {
+          const DdgiRay r = rays[cand];
+          o = f3(r.origin[0], r.origin[1], r.origin[2]);
+          d = f3(r.direction[0], r.direction[1], r.direction[2]);
+          tmin = r.tmin;
+          t1 = r.tmax;
+        }
+        if (sky) {
+          vis[cand] = 1.0f;  // shadow.rgen:44-47
+        } else {
+          ray = makeRay(o, d);
+          bool done;
+          if constexpr (kWide) done = wideInit<kAnyHit>(bvh, ray, t1, st, hit);
+          else done = binInit<kAnyHit>(bvh, ray, tmin, t1, st, hit);
+          if (done) finish(cand);
+          else id = cand;
+        }
+      }
+    }
+    if (id >= 0) {
+      bool done;
+      if constexpr (kWide) done = wideStep<kAnyHit>(bvh, ray, tmin, st, hit, err);
+      else done = binStep<kAnyHit>(bvh, ray, tmin, st, hit, err);
+      if (done) {
+        finish(id);
+        id = -1;
+      }
+    }
+  }
+}
+
+cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
+                            DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8;
+  const int refill = 8;
+  if (points) {  // shadow mask: any hit
+    if (wide) k_trace_rays<true, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, err);
+    else k_trace_rays<false, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, err);
+  } else if (anyHit) {
+    if (wide) k_trace_rays<true, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+    else k_trace_rays<false, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+  } else {
+    if (wide) k_trace_rays<true, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+    else k_trace_rays<false, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+  }
+  return cudaGetLastError();
+}
+
 // Atlas consumer (deferred_tiled.comp:263-299): the ambient term of G-buffer points, one thread per point.
 __global__ void __launch_bounds__(256) k_query_irradiance(GridGPU g, FrameGPU f, const void* __restrict__ atlas,
                                                           const DdgiSurfacePoint* __restrict__ pts, long long count,

@@ -70,6 +70,16 @@ class Scene:
         self.ctx.check(self.ctx.lib.ddgi_scene_info(self.handle, C.byref(i)))
         return i
 
+    def trace_rays(self, rays_ptr: int, count: int, hits_ptr: int, any_hit: bool = False, stream: int = 0) -> None:
+        """Closest (or any) hit of `count` device DdgiRay records into device DdgiHit records."""
+        self.ctx.check(self.ctx.lib.ddgi_trace_rays(self.handle, rays_ptr, count, L.DDGI_RAY_ANY_HIT if any_hit else 0,
+                                                    hits_ptr, stream))
+
+    def shadow_mask(self, frame: "FrameParams", points_ptr: int, count: int, vis_ptr: int, stream: int = 0) -> None:
+        """The RT shadow pass (shadow.rgen): visibility of device float4 points (w != 0: sky) along -lightDir."""
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_shadow_mask(self.handle, C.byref(f), points_ptr, count, vis_ptr, stream))
+
     def close(self) -> None:
         if self.handle:
             self.ctx.lib.ddgi_scene_destroy(self.handle)

@@ -256,6 +256,33 @@ int  ddgi_atlas_import_rgba16f(DdgiGrid* grid, const void* host, uint64_t bytes,
  * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
 int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
 
+/* ---- ray queries on a scene: the other ray-traced passes ------------------------------------------------- */
+
+typedef struct DdgiRay {    /* 32 bytes */
+  float origin[3];
+  float tmin;
+  float direction[3];       /* any length; t is in units of it, as traceRayEXT's */
+  float tmax;
+} DdgiRay;
+typedef struct DdgiHit {    /* 16 bytes */
+  float t, b1, b2;          /* distance and the barycentric weights of the triangle's 2nd and 3rd vertices */
+  int32_t triangle;         /* global triangle id (instance order, primitive order), -1 for a miss */
+} DdgiHit;
+#define DDGI_RAY_ANY_HIT (1u << 0) /* stop at the first hit (gl_RayFlagsTerminateOnFirstHitEXT); t, b of it */
+
+/* Closest (or any) hit of each ray in [tmin, tmax] against the scene's BVH: the traceRayEXT of the reference's
+ * other ray-traced passes, on the same traversal as the probe update (watertight test, double-sided, ties
+ * to the lowest global triangle id). rays / hits: device arrays of `count` records. Stream-ordered. */
+int  ddgi_trace_rays(DdgiScene* scene, const DdgiRay* rays, uint64_t count, uint32_t flags, DdgiHit* hits,
+                     void* stream);
+
+/* The RT shadow pass (shadow.rgen:29-82, shadow.rmiss, shadow.rchit): for each point a ray from the point
+ * along -frame->lightDir over [0.1, 50], terminating on the first hit; visibility 1 on a miss, 0 on a hit.
+ * points: device float4 per point (xyz world position; w != 0 marks a sky pixel, depth == 1, which gets 1
+ * without a ray); visibility: device float per point. Stream-ordered. */
+int  ddgi_shadow_mask(DdgiScene* scene, const DdgiFrame* frame, const float* points, uint64_t count,
+                      float* visibility, void* stream);
+
 /* ---- atlas consumer: indirect diffuse light of G-buffer points ------------------------------------------- */
 
 /* One G-buffer point (48 bytes): what deferred_tiled.comp:166-194 reads for a pixel. `normal` need not be
