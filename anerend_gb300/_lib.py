@@ -54,6 +54,8 @@ assert SURFACE_POINT.itemsize == 48
 RAY = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("direction", "<f4", 3), ("tmax", "<f4")])
 HIT = np.dtype([("t", "<f4"), ("b1", "<f4"), ("b2", "<f4"), ("triangle", "<i4")])
 DDGI_RAY_ANY_HIT = 1
+DDGI_SCENE_REFIT = 0
+DDGI_SCENE_REBUILD = 1
 assert PACKED_VERTEX.itemsize == 96 and MESH_INFO.itemsize == 48
 assert MATERIAL_INFO.itemsize == 64 and INSTANCE.itemsize == 64
 
@@ -164,6 +166,8 @@ SIGNATURES = {
     "ddgi_rays_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ddgi_atlas_export_rgba16f": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_atlas_import_rgba16f": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "ddgi_scene_update_transforms": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]),
+    "ddgi_scene_update_vertices": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]),
     "ddgi_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p]),
     "ddgi_shadow_mask": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ddgi_query_irradiance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),

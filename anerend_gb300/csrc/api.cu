@@ -206,26 +206,21 @@ void shearOf(const double d[3], int k[3], double S[3]) {
 // Builds (or reuses) the shadow BVH of `sc` for light direction lightDir: the instance transforms are
 // composed with the shear of L = normalize(-lightDir) on the host (FP64) and the LBVH is built over the
 // sheared triangles. Synchronizes `st` when it builds.
-int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
-  DdgiContext* ctx = sc->ctx;
-  std::lock_guard<std::mutex> lk(sc->mu);
-  if (sc->shadowValid && sc->shadowLight[0] == lightDir[0] && sc->shadowLight[1] == lightDir[1] &&
-      sc->shadowLight[2] == lightDir[2])
-    return DDGI_OK;
-  if (sc->view.bvh.numTris == 0) return DDGI_OK;
+// The scene's instances with their transforms composed with the shear of L = normalize(-lightDir) (FP64 on
+// the host): the transforms of the light-space shadow BVH. k, S: the shear's axes and factors.
+bool shearedInstances(const std::vector<InstanceGPU>& src, const float lightDir[3], std::vector<InstanceGPU>& out,
+                      int k[3], double S[3]) {
   double n = std::sqrt((double)lightDir[0] * lightDir[0] + (double)lightDir[1] * lightDir[1] +
                        (double)lightDir[2] * lightDir[2]);
-  if (!(n > 0)) return fail(ctx, DDGI_EINVAL, "lightDir has zero length");
+  if (!(n > 0)) return false;
   double L[3] = {-lightDir[0] / n, -lightDir[1] / n, -lightDir[2] / n};
-  int k[3];
-  double S[3];
   shearOf(L, k, S);
   double Sm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   Sm[0][k[0]] = 1.0; Sm[0][k[2]] = -S[0];
   Sm[1][k[1]] = 1.0; Sm[1][k[2]] = -S[1];
   Sm[2][k[2]] = S[2];
-  std::vector<InstanceGPU> sh = sc->hostInst;
-  for (InstanceGPU& in : sh) {
+  out = src;
+  for (InstanceGPU& in : out) {
     double m[12];
     for (int i = 0; i < 12; ++i) m[i] = in.o2w[i];
     for (int r = 0; r < 3; ++r)
@@ -235,6 +230,20 @@ int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
         in.o2w[4 * r + c] = (float)v;
       }
   }
+  return true;
+}
+
+int ensureShadowBvh(DdgiScene* sc, const float lightDir[3], cudaStream_t st) {
+  DdgiContext* ctx = sc->ctx;
+  std::lock_guard<std::mutex> lk(sc->mu);
+  if (sc->shadowValid && sc->shadowLight[0] == lightDir[0] && sc->shadowLight[1] == lightDir[1] &&
+      sc->shadowLight[2] == lightDir[2])
+    return DDGI_OK;
+  if (sc->view.bvh.numTris == 0) return DDGI_OK;
+  int k[3];
+  double S[3];
+  std::vector<InstanceGPU> sh;
+  if (!shearedInstances(sc->hostInst, lightDir, sh, k, S)) return fail(ctx, DDGI_EINVAL, "lightDir has zero length");
   InstanceGPU* dInst = nullptr;
   CK(cudaMalloc(&dInst, sizeof(InstanceGPU) * sh.size()), "shadow instances");
   cudaError_t e = cudaMemcpyAsync(dInst, sh.data(), sizeof(InstanceGPU) * sh.size(), cudaMemcpyHostToDevice, st);
@@ -514,6 +523,89 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
   sc->numVertices = d->numVertices;
   *out = sc;
   return DDGI_OK;
+}
+
+namespace {
+// Brings the scene BVH and, if built, the light-space shadow BVH up to date with the scene's current
+// instances and vertices. Synchronizes st.
+int updateBvhs(DdgiScene* sc, int mode, cudaStream_t st) {
+  DdgiContext* ctx = sc->ctx;
+  std::lock_guard<std::mutex> lk(sc->mu);
+  const int tris = sc->view.bvh.numTris;
+  const int numInst = (int)sc->hostInst.size();
+  if (tris == 0) return DDGI_OK;
+  auto refresh = [&](LbvhResult& bvh, const InstanceGPU* dInst) -> cudaError_t {
+    if (mode == DDGI_SCENE_REFIT) {
+      cudaError_t e = lbvhRefit(&bvh, dInst, sc->meshes, sc->indices, sc->numIndices, sc->vertices, sc->numVertices,
+                                ctx->dErr, st);
+      if (e != cudaErrorNotSupported) return e;
+    }
+    LbvhResult r;
+    cudaError_t e = lbvhBuild(dInst, numInst, sc->meshes, sc->indices, sc->numIndices, sc->vertices, sc->numVertices,
+                              tris, ctx->dErr, st, &r);
+    if (e != cudaSuccess) return e;
+    lbvhFree(&bvh);
+    bvh = r;
+    return cudaSuccess;
+  };
+  cudaError_t e = refresh(sc->bvh, sc->instances);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "scene BVH update");
+  sc->view.bvh = BvhRef{sc->bvh.nodes, sc->bvh.wnodes, sc->bvh.tris, tris, sc->bvh.numNodes, sc->bvh.numWNodes};
+  if (sc->shadowValid) {
+    int k[3];
+    double S[3];
+    std::vector<InstanceGPU> sh;
+    shearedInstances(sc->hostInst, sc->shadowLight, sh, k, S);
+    InstanceGPU* dInst = nullptr;
+    CK(cudaMalloc(&dInst, sizeof(InstanceGPU) * sh.size()), "shadow instances");
+    e = cudaMemcpyAsync(dInst, sh.data(), sizeof(InstanceGPU) * sh.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = refresh(sc->shadowBvh, dInst);
+    cudaStreamSynchronize(st);
+    cudaFree(dInst);
+    if (e != cudaSuccess) {
+      sc->shadowValid = false;
+      return cudaFail(ctx, e, "shadow BVH update");
+    }
+    const LbvhResult& r = sc->shadowBvh;
+    sc->view.shadow = BvhRef{r.nodes, r.wnodes, r.tris, r.numTris, r.numNodes, r.numWNodes};
+  }
+  return DDGI_OK;
+}
+}  // namespace
+
+int ddgi_scene_update_transforms(DdgiScene* sc, const float* transforms, uint64_t numInstances, int mode,
+                                 void* stream) {
+  if (!sc || !transforms) return fail(sc ? sc->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_scene_update_transforms");
+  DdgiContext* ctx = sc->ctx;
+  if (mode != DDGI_SCENE_REFIT && mode != DDGI_SCENE_REBUILD) return fail(ctx, DDGI_EINVAL, "mode %d unknown", mode);
+  if (numInstances != sc->hostInst.size())
+    return fail(ctx, DDGI_EINVAL, "the scene has %zu instances, got %llu transforms", sc->hostInst.size(),
+                (unsigned long long)numInstances);
+  std::vector<InstanceGPU> inst = sc->hostInst;
+  for (size_t i = 0; i < inst.size(); ++i) {
+    memcpy(inst[i].o2w, transforms + 12 * i, sizeof(inst[i].o2w));
+    if (!invert3(inst[i].o2w, inst[i].w2oLin)) return fail(ctx, DDGI_EINVAL, "instance %zu: singular transform", i);
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(sc->instances, inst.data(), sizeof(InstanceGPU) * inst.size(), cudaMemcpyHostToDevice, st),
+     "instance upload");
+  sc->hostInst = inst;
+  return updateBvhs(sc, mode, st);
+}
+
+int ddgi_scene_update_vertices(DdgiScene* sc, const DdgiPackedVertex* vertices, uint64_t first, uint64_t count,
+                               int mode, void* stream) {
+  if (!sc || (count && !vertices)) return fail(sc ? sc->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_scene_update_vertices");
+  DdgiContext* ctx = sc->ctx;
+  if (mode != DDGI_SCENE_REFIT && mode != DDGI_SCENE_REBUILD) return fail(ctx, DDGI_EINVAL, "mode %d unknown", mode);
+  if (first > sc->numVertices || count > sc->numVertices - first)
+    return fail(ctx, DDGI_EINVAL, "vertex range [%llu, +%llu) beyond the scene's %llu vertices", (unsigned long long)first,
+                (unsigned long long)count, (unsigned long long)sc->numVertices);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (count)
+    CK(cudaMemcpyAsync(sc->vertices + first, vertices, sizeof(DdgiPackedVertex) * count, cudaMemcpyHostToDevice, st),
+       "vertex upload");
+  return updateBvhs(sc, mode, st);
 }
 
 void ddgi_scene_destroy(DdgiScene* s) {

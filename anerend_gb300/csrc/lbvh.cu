@@ -445,8 +445,8 @@ cudaError_t lbvhBuild(const InstanceGPU* dInst, int numInst, const DdgiMeshInfo*
     DDGI_TRY(cudaMemcpyAsync(ht.data(), out->tris, sizeof(float4) * ht.size(), cudaMemcpyDeviceToHost, stream));
     DDGI_TRY(cudaStreamSynchronize(stream));
     std::vector<float4> wide;
-    std::vector<int> order;
-    if (!wbvh::collapse(hn.data(), ht.data(), n, wide, order)) {
+    std::vector<int> order, slotRef;
+    if (!wbvh::collapse(hn.data(), ht.data(), n, wide, order, &slotRef)) {
       e = cudaErrorUnknown;
       goto done;
     }
@@ -460,6 +460,20 @@ cudaError_t lbvhBuild(const InstanceGPU* dInst, int numInst, const DdgiMeshInfo*
       if (c0 < 0) hn[4 * i + 3].x = wbvh::asFloatH((uint32_t)~inv[~c0]);
       if (c1 < 0) hn[4 * i + 3].y = wbvh::asFloatH((uint32_t)~inv[~c1]);
     }
+    for (int& r : slotRef)
+      if (r != wbvh::kEmptySlot && r < 0) r = ~inv[~r];
+    std::vector<int> parI(std::max(1, out->numNodes), -1), parL(n, -1);
+    for (int i = 0; i < out->numNodes; ++i)
+      for (int k = 0; k < 2; ++k) {
+        int c = wbvh::asIntH(k ? hn[4 * i + 3].y : hn[4 * i + 3].x);
+        if (c >= 0) parI[c] = i; else parL[~c] = i;
+      }
+    DDGI_TRY(cudaMalloc(&out->parentInternal, sizeof(int) * parI.size()));
+    DDGI_TRY(cudaMalloc(&out->parentLeaf, sizeof(int) * parL.size()));
+    DDGI_TRY(cudaMalloc(&out->slotRef, sizeof(int) * slotRef.size()));
+    DDGI_TRY(cudaMemcpyAsync(out->parentInternal, parI.data(), sizeof(int) * parI.size(), cudaMemcpyHostToDevice, stream));
+    DDGI_TRY(cudaMemcpyAsync(out->parentLeaf, parL.data(), sizeof(int) * parL.size(), cudaMemcpyHostToDevice, stream));
+    DDGI_TRY(cudaMemcpyAsync(out->slotRef, slotRef.data(), sizeof(int) * slotRef.size(), cudaMemcpyHostToDevice, stream));
     out->numWNodes = (int)(wide.size() / kWideNodeF4);
     DDGI_TRY(cudaMalloc(&out->wnodes, sizeof(float4) * wide.size()));
     DDGI_TRY(cudaMemcpyAsync(out->wnodes, wide.data(), sizeof(float4) * wide.size(), cudaMemcpyHostToDevice, stream));
@@ -478,13 +492,137 @@ done:
   return e;
 }
 
+namespace {
+
+// Refit 1: the triangle records again from the object-space vertices (the arithmetic of k_flatten); the
+// record keeps its global id, instance and primitive in .w.
+__global__ void k_refit_tris(float4* __restrict__ tris, int n, const InstanceGPU* __restrict__ inst,
+                             const DdgiMeshInfo* __restrict__ meshes, const uint32_t* __restrict__ indices,
+                             const DdgiPackedVertex* __restrict__ verts, uint64_t numIndices, uint64_t numVerts,
+                             uint32_t* __restrict__ err) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int in = __float_as_int(tris[3 * k + 1].w), prim = __float_as_int(tris[3 * k + 2].w);
+  const InstanceGPU& I = inst[in];
+  const DdgiMeshInfo& m = meshes[I.mesh];
+  for (int v = 0; v < 3; ++v) {
+    uint64_t ii = (uint64_t)m.indexOffset + 3ull * prim + v;
+    uint32_t vi = ii < numIndices ? indices[ii] : 0u;
+    uint64_t vv = (uint64_t)m.vertexOffset + vi;
+    if (ii >= numIndices || vv >= numVerts) { atomicOr(err, DDGI_DEVERR_BOUNDS); vv = 0; }
+    const float* d0 = verts[vv].d0;
+    const float3 w = xform(I.o2w, f3(d0[0], d0[1], d0[2]));
+    const float keep = tris[3 * k + v].w;
+    tris[3 * k + v] = make_float4(w.x, w.y, w.z, keep);
+  }
+}
+
+DDGI_D void recordBox(const float4* tris, int rec, float3& lo, float3& hi) {
+  const float4 a = __ldcg(&tris[3 * rec]), b = __ldcg(&tris[3 * rec + 1]), c = __ldcg(&tris[3 * rec + 2]);
+  lo = f3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+  hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+}
+
+// Refit 2: binary boxes bottom-up, the second child to arrive at a node computes it (as k_bounds).
+__global__ void k_refit_binary(const float4* __restrict__ tris, int n, float4* __restrict__ nodes,
+                               const int* __restrict__ parentInternal, const int* __restrict__ parentLeaf,
+                               float4* __restrict__ nodeLo, float4* __restrict__ nodeHi, int* __restrict__ flags) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int cur = parentLeaf[k];
+  while (cur >= 0) {
+    __threadfence();
+    if (atomicAdd(&flags[cur], 1) == 0) return;
+    __threadfence();
+    const float4 n3 = __ldcg(&nodes[4 * cur + 3]);
+    const int cs[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
+    float3 lo[2], hi[2];
+    for (int c = 0; c < 2; ++c) {
+      if (cs[c] < 0) {
+        recordBox(tris, ~cs[c], lo[c], hi[c]);
+      } else {
+        lo[c] = xyz(__ldcg(&nodeLo[cs[c]]));
+        hi[c] = xyz(__ldcg(&nodeHi[cs[c]]));
+      }
+    }
+    __stcg(&nodes[4 * cur + 0], make_float4(lo[0].x, hi[0].x, lo[0].y, hi[0].y));
+    __stcg(&nodes[4 * cur + 1], make_float4(lo[1].x, hi[1].x, lo[1].y, hi[1].y));
+    __stcg(&nodes[4 * cur + 2], make_float4(lo[0].z, hi[0].z, lo[1].z, hi[1].z));
+    __stcg(&nodeLo[cur], make_float4(fminf(lo[0].x, lo[1].x), fminf(lo[0].y, lo[1].y), fminf(lo[0].z, lo[1].z), 0.f));
+    __stcg(&nodeHi[cur], make_float4(fmaxf(hi[0].x, hi[1].x), fmaxf(hi[0].y, hi[1].y), fmaxf(hi[0].z, hi[1].z), 0.f));
+    cur = parentInternal[cur];
+  }
+}
+
+// Refit 3: every wide slot takes the box of the binary subtree it holds (FP32 node layout).
+__global__ void k_refit_wide(float4* __restrict__ wnodes, int numWide, const int* __restrict__ slotRef,
+                             const float4* __restrict__ tris, const float4* __restrict__ nodeLo,
+                             const float4* __restrict__ nodeHi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= numWide * 8) return;
+  const int node = i >> 3, sl = i & 7;
+  const int ref = slotRef[i];
+  if (ref == INT_MIN) return;
+  float3 lo, hi;
+  if (ref < 0) {
+    recordBox(tris, ~ref, lo, hi);
+  } else {
+    lo = xyz(nodeLo[ref]);
+    hi = xyz(nodeHi[ref]);
+  }
+  float* f = reinterpret_cast<float*>(wnodes + (size_t)node * kWideNodeF4);
+  const int c = (sl >> 2), q = sl & 3;  // plane row p -> float4 1 + 2p + c, component q
+  f[4 * (1 + 0 + c) + q] = lo.x;
+  f[4 * (1 + 2 + c) + q] = hi.x;
+  f[4 * (1 + 4 + c) + q] = lo.y;
+  f[4 * (1 + 6 + c) + q] = hi.y;
+  f[4 * (1 + 8 + c) + q] = lo.z;
+  f[4 * (1 + 10 + c) + q] = hi.z;
+}
+
+}  // namespace
+
+cudaError_t lbvhRefit(LbvhResult* r, const InstanceGPU* dInst, const DdgiMeshInfo* dMeshes, const uint32_t* dIndices,
+                      uint64_t numIndices, const DdgiPackedVertex* dVerts, uint64_t numVerts, uint32_t* dErr,
+                      cudaStream_t stream) {
+#if DDGI_WIDE_QUANT
+  return cudaErrorNotSupported;  // quantized nodes re-quantize on a rebuild
+#else
+  const int n = r->numTris;
+  if (n <= 0) return cudaSuccess;
+  k_refit_tris<<<blocks(n, 256), 256, 0, stream>>>(r->tris, n, dInst, dMeshes, dIndices, dVerts, numIndices, numVerts,
+                                                   dErr);
+  float4* box = nullptr;
+  int* flags = nullptr;
+  const int ni = std::max(1, r->numNodes);
+  cudaError_t e = cudaMallocAsync(&box, sizeof(float4) * 2 * (size_t)ni, stream);
+  if (e == cudaSuccess) e = cudaMallocAsync(&flags, sizeof(int) * (size_t)ni, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)ni, stream);
+  if (e == cudaSuccess && r->numNodes > 0)
+    k_refit_binary<<<blocks(n, 256), 256, 0, stream>>>(r->tris, n, r->nodes, r->parentInternal, r->parentLeaf, box,
+                                                       box + ni, flags);
+  if (e == cudaSuccess)
+    k_refit_wide<<<blocks((long long)r->numWNodes * 8, 256), 256, 0, stream>>>(r->wnodes, r->numWNodes, r->slotRef,
+                                                                             r->tris, box, box + ni);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (box) cudaFreeAsync(box, stream);
+  if (flags) cudaFreeAsync(flags, stream);
+  cudaError_t s = cudaStreamSynchronize(stream);
+  return e != cudaSuccess ? e : s;
+#endif
+}
+
 void lbvhFree(LbvhResult* r) {
   if (r->tris) cudaFree(r->tris);
   if (r->nodes) cudaFree(r->nodes);
   if (r->wnodes) cudaFree(r->wnodes);
+  cudaFree(r->parentInternal);
+  cudaFree(r->parentLeaf);
+  cudaFree(r->slotRef);
   r->tris = nullptr;
   r->nodes = nullptr;
   r->wnodes = nullptr;
+  r->parentInternal = r->parentLeaf = r->slotRef = nullptr;
 }
 
 }  // namespace ddgi

@@ -12,6 +12,7 @@
 #pragma once
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -49,13 +50,18 @@ struct Cand {
   int count;  // triangles below
 };
 
+constexpr int kEmptySlot = INT_MIN;  // slotRef of an empty slot
+
 // nodes2: numTris - 1 binary nodes (4 float4 each, root 0; none when numTris == 1); tris: numTris records.
-// Output: wide nodes (kWideNodeF4 float4 each, root 0) and `order` (new record index -> old record index).
+// Output: wide nodes (kWideNodeF4 float4 each, root 0), `order` (new record index -> old record index) and,
+// if asked, slotRef: per wide node 8 binary child ids, the subtree each slot holds (>= 0 binary node, < 0
+// ~record in the OLD record order, kEmptySlot for an empty slot) - what a refit reads the slot boxes from.
 // Returns false only for numTris <= 0.
 inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std::vector<float4>& out,
-                     std::vector<int>& order) {
+                     std::vector<int>& order, std::vector<int>* slotRef = nullptr) {
   out.clear();
   order.clear();
+  if (slotRef) slotRef->clear();
   if (numTris <= 0) return false;
   const int numNodes2 = numTris - 1;
   auto childOf = [&](int node, int k) { return asIntH(k == 0 ? nodes2[4 * node + 3].x : nodes2[4 * node + 3].y); };
@@ -210,6 +216,10 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
     }
     numWide += rank;
     out.resize((size_t)numWide * kWideNodeF4);
+    if (slotRef) {
+      slotRef->resize((size_t)numWide * 8, kEmptySlot);
+      for (int sl = 0; sl < 8; ++sl) (*slotRef)[(size_t)index * 8 + sl] = kidOf[sl] >= 0 ? kids[kidOf[sl]].ref : kEmptySlot;
+    }
     float4* nd = out.data() + (size_t)index * kWideNodeF4;
     uint32_t m0 = 0, m1 = 0;
     for (int s = 0; s < 4; ++s) m0 |= (uint32_t)meta[s] << (8 * s);

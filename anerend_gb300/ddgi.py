@@ -70,6 +70,20 @@ class Scene:
         self.ctx.check(self.ctx.lib.ddgi_scene_info(self.handle, C.byref(i)))
         return i
 
+    def update_transforms(self, transforms: np.ndarray, rebuild: bool = False, stream: int = 0) -> None:
+        """New (numInstances, 3, 4) object-to-world transforms; the BVHs are refitted (or rebuilt)."""
+        t = np.ascontiguousarray(transforms, np.float32).reshape(-1, 12)
+        self.ctx.check(self.ctx.lib.ddgi_scene_update_transforms(self.handle, _ptr(t), len(t),
+                                                                 L.DDGI_SCENE_REBUILD if rebuild else L.DDGI_SCENE_REFIT,
+                                                                 stream))
+
+    def update_vertices(self, vertices: np.ndarray, first: int = 0, rebuild: bool = False, stream: int = 0) -> None:
+        """New PACKED_VERTEX records starting at `first`; the BVHs are refitted (or rebuilt)."""
+        v = np.ascontiguousarray(vertices)
+        self.ctx.check(self.ctx.lib.ddgi_scene_update_vertices(self.handle, _ptr(v), first, len(v),
+                                                               L.DDGI_SCENE_REBUILD if rebuild else L.DDGI_SCENE_REFIT,
+                                                               stream))
+
     def trace_rays(self, rays_ptr: int, count: int, hits_ptr: int, any_hit: bool = False, stream: int = 0) -> None:
         """Closest (or any) hit of `count` device DdgiRay records into device DdgiHit records."""
         self.ctx.check(self.ctx.lib.ddgi_trace_rays(self.handle, rays_ptr, count, L.DDGI_RAY_ANY_HIT if any_hit else 0,

@@ -256,6 +256,22 @@ int  ddgi_atlas_import_rgba16f(DdgiGrid* grid, const void* host, uint64_t bytes,
  * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
 int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
 
+/* ---- dynamic scenes -------------------------------------------------------------------------------------- */
+
+#define DDGI_SCENE_REFIT   0  /* keep the BVH topology, refit its boxes on the device */
+#define DDGI_SCENE_REBUILD 1  /* build the BVH again (a fresh build's tree quality) */
+
+/* New object-to-world transforms for all of the scene's instances (numInstances x 12 floats, 3 x 4 row-major
+ * as DdgiInstance.transform): the per-frame TLAS update of UpdateTLASPass.cpp:176-205. The scene's BVHs (and
+ * its light-space shadow BVH, if built) are refitted or rebuilt; the traced hits are the same either way.
+ * Not concurrent with work that reads the scene. Synchronizes `stream`. */
+int  ddgi_scene_update_transforms(DdgiScene* scene, const float* transforms, uint64_t numInstances, int mode,
+                                  void* stream);
+/* New vertex records [first, first + count) (host DdgiPackedVertex, e.g. skinned positions and normals): the
+ * dynamic BLAS refit of UpdateBlasPass.cpp:18-19. Same BVH handling and synchronization as above. */
+int  ddgi_scene_update_vertices(DdgiScene* scene, const DdgiPackedVertex* vertices, uint64_t first, uint64_t count,
+                                int mode, void* stream);
+
 /* ---- ray queries on a scene: the other ray-traced passes ------------------------------------------------- */
 
 typedef struct DdgiRay {    /* 32 bytes */
