@@ -554,6 +554,7 @@ __global__ void k_refit_binary(const float4* __restrict__ tris, int n, float4* _
   }
 }
 
+#if !DDGI_WIDE_QUANT
 // Refit 3: every wide slot takes the box of the binary subtree it holds (FP32 node layout).
 __global__ void k_refit_wide(float4* __restrict__ wnodes, int numWide, const int* __restrict__ slotRef,
                              const float4* __restrict__ tris, const float4* __restrict__ nodeLo,
@@ -579,15 +580,42 @@ __global__ void k_refit_wide(float4* __restrict__ wnodes, int numWide, const int
   f[4 * (1 + 8 + c) + q] = lo.z;
   f[4 * (1 + 10 + c) + q] = hi.z;
 }
+#endif
+
+#if DDGI_WIDE_QUANT
+// Refit 3 (quantized layout): one thread per wide node re-quantizes its slots against the union of their
+// refitted boxes, by the collapse's rules (quantizeSlots); the header (nd[1]) stays.
+__global__ void k_refit_wide_quant(float4* __restrict__ wnodes, int numWide, const int* __restrict__ slotRef,
+                                   const float4* __restrict__ tris, const float4* __restrict__ nodeLo,
+                                   const float4* __restrict__ nodeHi) {
+  const int node = blockIdx.x * blockDim.x + threadIdx.x;
+  if (node >= numWide) return;
+  float lo[8][3], hi[8][3];
+  uint32_t used = 0;
+  for (int sl = 0; sl < 8; ++sl) {
+    const int ref = slotRef[(size_t)node * 8 + sl];
+    float3 l = f3(0.f, 0.f, 0.f), h = f3(0.f, 0.f, 0.f);
+    if (ref != INT_MIN) {
+      used |= 1u << sl;
+      if (ref < 0) {
+        recordBox(tris, ~ref, l, h);
+      } else {
+        l = xyz(nodeLo[ref]);
+        h = xyz(nodeHi[ref]);
+      }
+    }
+    lo[sl][0] = l.x; lo[sl][1] = l.y; lo[sl][2] = l.z;
+    hi[sl][0] = h.x; hi[sl][1] = h.y; hi[sl][2] = h.z;
+  }
+  quantizeSlots(lo, hi, used, wnodes + (size_t)node * kWideNodeF4);
+}
+#endif
 
 }  // namespace
 
 cudaError_t lbvhRefit(LbvhResult* r, const InstanceGPU* dInst, const DdgiMeshInfo* dMeshes, const uint32_t* dIndices,
                       uint64_t numIndices, const DdgiPackedVertex* dVerts, uint64_t numVerts, uint32_t* dErr,
                       cudaStream_t stream) {
-#if DDGI_WIDE_QUANT
-  return cudaErrorNotSupported;  // quantized nodes re-quantize on a rebuild
-#else
   const int n = r->numTris;
   if (n <= 0) return cudaSuccess;
   k_refit_tris<<<blocks(n, 256), 256, 0, stream>>>(r->tris, n, dInst, dMeshes, dIndices, dVerts, numIndices, numVerts,
@@ -601,15 +629,20 @@ cudaError_t lbvhRefit(LbvhResult* r, const InstanceGPU* dInst, const DdgiMeshInf
   if (e == cudaSuccess && r->numNodes > 0)
     k_refit_binary<<<blocks(n, 256), 256, 0, stream>>>(r->tris, n, r->nodes, r->parentInternal, r->parentLeaf, box,
                                                        box + ni, flags);
+#if DDGI_WIDE_QUANT
+  if (e == cudaSuccess)
+    k_refit_wide_quant<<<blocks(r->numWNodes, 128), 128, 0, stream>>>(r->wnodes, r->numWNodes, r->slotRef, r->tris,
+                                                                      box, box + ni);
+#else
   if (e == cudaSuccess)
     k_refit_wide<<<blocks((long long)r->numWNodes * 8, 256), 256, 0, stream>>>(r->wnodes, r->numWNodes, r->slotRef,
                                                                              r->tris, box, box + ni);
+#endif
   if (e == cudaSuccess) e = cudaGetLastError();
   if (box) cudaFreeAsync(box, stream);
   if (flags) cudaFreeAsync(flags, stream);
   cudaError_t s = cudaStreamSynchronize(stream);
   return e != cudaSuccess ? e : s;
-#endif
 }
 
 void lbvhFree(LbvhResult* r) {

@@ -8,7 +8,8 @@
 // breadth-first order so the internal children of a node are consecutive (childBase + rank). Children are
 // placed in slots by a greedy octant assignment (slot s = the child lying most toward the corner with
 // sign bits s). The method follows the greedy variant of Ylitie, Karras, Laine 2017 ("Efficient
-// incoherent ray traversal on GPUs through compressed wide BVHs"), with uncompressed FP32 child boxes.
+// incoherent ray traversal on GPUs through compressed wide BVHs"); child boxes are stored as FP32 planes
+// or, in the default layout, as bytes on a per-node power-of-two grid (quantizeSlots).
 #pragma once
 
 #include <algorithm>
@@ -21,6 +22,53 @@
 #include "traverse.cuh"
 
 namespace ddgi {
+
+// Quantized wide node (the DDGI_WIDE_QUANT layout): from the boxes of the used slots (bit sl of `used`)
+// writes nd[0] = (origin, biased exponents) and the byte planes nd[2..4]; nd[1], the header, is the
+// caller's. Origin = the union's minimum; per axis the smallest e with 255 * 2^e >= extent (e = -100 for
+// a flat axis), limited to [-126, 126]; slot planes rounded outward, floor / ceil of (plane - origin) / 2^e
+// in double arithmetic on the float boxes (exact). Unused slots get zero bytes. The host collapse and
+// the device refit both call it.
+DDGI_HD void quantizeSlots(const float lo[8][3], const float hi[8][3], uint32_t used, float4* nd) {
+  float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int sl = 0; sl < 8; ++sl)
+    if (used >> sl & 1u)
+      for (int a = 0; a < 3; ++a) {
+        nlo[a] = fminf(nlo[a], lo[sl][a]);
+        nhi[a] = fmaxf(nhi[a], hi[sl][a]);
+      }
+  if (!used)
+    for (int a = 0; a < 3; ++a) nlo[a] = nhi[a] = 0.0f;
+  uint32_t eb = 0, words[12];
+  for (int a = 0; a < 3; ++a) {
+    const double ext = (double)nhi[a] - (double)nlo[a];
+    int e = -100;
+    if (ext > 0.0) {
+      e = ilogb(ext) - 7;  // ext in [2^k, 2^(k+1)) and 255 * 2^(k-8) < 2^k: e is k - 7 or k - 6
+      if (ldexp(255.0, e) < ext) ++e;
+    }
+    e = e < -126 ? -126 : e > 126 ? 126 : e;
+    const double sc = ldexp(1.0, e);
+    uint32_t wl[2] = {0u, 0u}, wh[2] = {0u, 0u};
+    for (int sl = 0; sl < 8; ++sl) {
+      if (!(used >> sl & 1u)) continue;
+      const double ql = floor(((double)lo[sl][a] - (double)nlo[a]) / sc);
+      const double qh = ceil(((double)hi[sl][a] - (double)nlo[a]) / sc);
+      wl[sl >> 2] |= (uint32_t)fmax(0.0, fmin(255.0, ql)) << (8 * (sl & 3));
+      wh[sl >> 2] |= (uint32_t)fmax(0.0, fmin(255.0, qh)) << (8 * (sl & 3));
+    }
+    eb |= (uint32_t)(e + 127) << (8 * a);
+    words[2 * a] = wl[0];
+    words[2 * a + 1] = wl[1];
+    words[6 + 2 * a] = wh[0];
+    words[6 + 2 * a + 1] = wh[1];
+  }
+  nd[0] = make_float4(nlo[0], nlo[1], nlo[2], asFloatHd(eb));
+  for (int k = 0; k < 3; ++k)
+    nd[2 + k] = make_float4(asFloatHd(words[4 * k]), asFloatHd(words[4 * k + 1]), asFloatHd(words[4 * k + 2]),
+                            asFloatHd(words[4 * k + 3]));
+}
+
 namespace wbvh {
 
 struct Box {
@@ -225,40 +273,18 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
     for (int s = 0; s < 4; ++s) m0 |= (uint32_t)meta[s] << (8 * s);
     for (int s = 0; s < 4; ++s) m1 |= (uint32_t)meta[4 + s] << (8 * s);
 #if DDGI_WIDE_QUANT
-    // origin = node box min; per axis the smallest power-of-two scale with extent <= 255 s; child planes
-    // rounded outward (exact double arithmetic on float inputs)
-    uint32_t eb = 0;
-    float pf[3];
-    double sc[3];
-    for (int a = 0; a < 3; ++a) {
-      pf[a] = nb.lo[a];
-      const double ext = (double)nb.hi[a] - (double)pf[a];
-      int e = -100;
-      if (ext > 0) e = (int)std::ceil(std::log2(ext / 255.0));
-      e = std::max(-126, std::min(126, e));
-      while (std::ldexp(255.0, e) < ext) ++e;
-      sc[a] = std::ldexp(1.0, e);
-      eb |= (uint32_t)(e + 127) << (8 * a);
-    }
-    uint8_t qlo[3][8], qhi[3][8];
+    float slo[8][3], shi[8][3];
+    uint32_t used = 0;
     for (int sl = 0; sl < 8; ++sl) {
       const int i = kidOf[sl];
       for (int a = 0; a < 3; ++a) {
-        if (i < 0) { qlo[a][sl] = 0; qhi[a][sl] = 0; continue; }
-        double lo = std::floor(((double)kids[i].box.lo[a] - (double)pf[a]) / sc[a]);
-        double hi = std::ceil(((double)kids[i].box.hi[a] - (double)pf[a]) / sc[a]);
-        qlo[a][sl] = (uint8_t)std::max(0.0, std::min(255.0, lo));
-        qhi[a][sl] = (uint8_t)std::max(0.0, std::min(255.0, hi));
+        slo[sl][a] = i >= 0 ? kids[i].box.lo[a] : 0.0f;
+        shi[sl][a] = i >= 0 ? kids[i].box.hi[a] : 0.0f;
       }
+      if (i >= 0) used |= 1u << sl;
     }
-    auto word = [&](const uint8_t* q, int h) {
-      return (uint32_t)q[4 * h] | (uint32_t)q[4 * h + 1] << 8 | (uint32_t)q[4 * h + 2] << 16 | (uint32_t)q[4 * h + 3] << 24;
-    };
-    nd[0] = make_float4(pf[0], pf[1], pf[2], asFloatH(eb));
+    quantizeSlots(slo, shi, used, nd);
     nd[1] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
-    nd[2] = make_float4(asFloatH(word(qlo[0], 0)), asFloatH(word(qlo[0], 1)), asFloatH(word(qlo[1], 0)), asFloatH(word(qlo[1], 1)));
-    nd[3] = make_float4(asFloatH(word(qlo[2], 0)), asFloatH(word(qlo[2], 1)), asFloatH(word(qhi[0], 0)), asFloatH(word(qhi[0], 1)));
-    nd[4] = make_float4(asFloatH(word(qhi[1], 0)), asFloatH(word(qhi[1], 1)), asFloatH(word(qhi[2], 0)), asFloatH(word(qhi[2], 1)));
 #else
     nd[0] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
     float pl[6][8];
