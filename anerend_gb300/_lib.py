@@ -51,6 +51,8 @@ INSTANCE = np.dtype([("transform", "<f4", 12), ("mesh", "<u4"), ("material", "<u
 SURFACE_POINT = np.dtype([("position", "<f4", 3), ("metallic", "<f4"), ("normal", "<f4", 3), ("roughness", "<f4"),
                           ("albedo", "<f4", 3), ("shadow", "<f4")])
 assert SURFACE_POINT.itemsize == 48
+MIRROR_POINT = np.dtype([("position", "<f4", 3), ("sky", "<f4"), ("normal", "<f4", 3), ("reserved", "<f4")])
+assert MIRROR_POINT.itemsize == 32
 RAY = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("direction", "<f4", 3), ("tmax", "<f4")])
 HIT = np.dtype([("t", "<f4"), ("b1", "<f4"), ("b2", "<f4"), ("triangle", "<i4")])
 DDGI_RAY_ANY_HIT = 1
@@ -171,6 +173,8 @@ SIGNATURES = {
     "ddgi_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p]),
     "ddgi_shadow_mask": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ddgi_query_irradiance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "ddgi_mirror_reflections": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                          C.c_void_p]),
     "ddgi_batch_create": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_int, C.POINTER(C.c_void_p)]),
     "ddgi_batch_destroy": (None, [C.c_void_p]),
     "ddgi_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),

@@ -922,6 +922,33 @@ int ddgi_query_irradiance(DdgiGrid* g, const DdgiFrame* frame, const DdgiSurface
   return DDGI_OK;
 }
 
+int ddgi_mirror_reflections(DdgiGrid* g, DdgiScene* sc, const DdgiFrame* frame, const DdgiMirrorPoint* points,
+                            uint64_t count, float* out, void* stream) {
+  if (!g || !sc || !frame) return fail(g ? g->ctx : sc ? sc->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_mirror_reflections");
+  DdgiContext* ctx = g->ctx;
+  if (sc->ctx != ctx) return fail(ctx, DDGI_EINVAL, "grid and scene belong to different contexts");
+  if (count == 0) return DDGI_OK;
+  if (!points || !out) return fail(ctx, DDGI_EINVAL, "NULL points or output");
+  if (((uintptr_t)points | (uintptr_t)out) & 15) return fail(ctx, DDGI_EINVAL, "points and out must be 16-byte aligned");
+  if (count > (1ull << 40)) return fail(ctx, DDGI_EINVAL, "count %llu too large", (unsigned long long)count);
+  FrameGPU f{};
+  int rc = frameToGPU(ctx, frame, f);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // rays, hits, shadow points, shadowed radiance, visibility; released once the stream has consumed them
+  void* scratch = nullptr;
+  unsigned long long* counter = nullptr;
+  CK(cudaMallocAsync(&scratch, mirrorScratchBytes((long long)count), st), "mirror scratch");
+  cudaError_t e = cudaMallocAsync(&counter, sizeof(unsigned long long), st);
+  if (e == cudaSuccess)
+    e = launchMirror(sc->view, g->g, f, g->atlas[g->cur], points, (long long)count, (float4*)out, scratch, counter,
+                     ctx->dErr, st);
+  cudaFreeAsync(scratch, st);
+  if (counter) cudaFreeAsync(counter, st);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "mirror reflections");
+  return DDGI_OK;
+}
+
 // ---- raw kernels --------------------------------------------------------------------------------------
 int ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* stream) {
   if (numRays <= 0 || numRays > (1 << 20) || !rot || !dirs) return DDGI_EINVAL;

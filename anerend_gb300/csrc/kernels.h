@@ -40,13 +40,21 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
 
 
 // Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's
-// visibility mask along shadowDir. counter: one device word of scratch.
+// visibility mask along shadowDir. counter: one device word of scratch. recordIds: DdgiHit.triangle holds the
+// hit's triangle record (BVH order) instead of its global id.
 cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
                             DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
-                            unsigned long long* counter, uint32_t* err, cudaStream_t stream);
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds = false);
 // Ambient term of G-buffer points from an atlas (deferred_tiled.comp:263-299), CLAMP_TO_EDGE sampling.
 cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const void* atlas, const DdgiSurfacePoint* pts,
                                   long long count, float4* out, cudaStream_t stream);
+// Specular GI mirror pass (mirror_reflections.rgen/.rchit/.rmiss): radiance and hit distance per G-buffer
+// point, sampling `atlas` as the probe update does (REPEAT). scratch: mirrorScratchBytes(count) device bytes, 16-byte
+// aligned; counter: one device word.
+size_t mirrorScratchBytes(long long count);
+cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const void* atlas,
+                         const DdgiMirrorPoint* pts, long long count, float4* out, void* scratch,
+                         unsigned long long* counter, uint32_t* err, cudaStream_t stream);
 
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream);

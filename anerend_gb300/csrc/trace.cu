@@ -279,6 +279,65 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
   }
 }
 
+// Surface at a hit: world position, shading normal, colour and material of triangle record `leaf` at
+// barycentric weights (b1, b2) of its 2nd and 3rd vertices.
+struct HitSurface {
+  float3 pos, normal, color, emissive;  // emissive = emissive.rgb * emissive.w
+  float metallic, roughness;
+};
+
+// Hit reconstruction (irradiance_probe_update.rchit:137-187; getSurfaceDataFromMat bindless.glsl:181-237
+// without textures). kMirrorNormal: the normal through mat3(ObjectToWorld) (mirror_reflections.rchit:73)
+// instead of normal * WorldToObject (irradiance_probe_update.rchit:72).
+template <bool kMirrorNormal>
+DDGI_D HitSurface reconstructHit(const SceneGPU& s, int leaf, float b1, float b2) {
+  const int inst = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 1].w));
+  const int prim = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 2].w));
+  const InstanceGPU& in = s.instances[inst];
+  const DdgiMeshInfo& mesh = s.meshes[in.mesh];
+  const uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
+  const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
+  const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
+  const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
+  const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
+  const float b0 = 1.0f - b1 - b2;
+  const float4 a0 = __ldg((const float4*)v0.d0), a1 = __ldg((const float4*)v1.d0), a2 = __ldg((const float4*)v2.d0);
+  const float4 c0 = __ldg((const float4*)v0.d1), c1 = __ldg((const float4*)v1.d1), c2 = __ldg((const float4*)v2.d1);
+  const float4 e0 = __ldg((const float4*)v0.d2), e1 = __ldg((const float4*)v1.d2), e2 = __ldg((const float4*)v2.d2);
+  HitSurface h;
+  const float3 posObj = xyz(a0) * b0 + xyz(a1) * b1 + xyz(a2) * b2;
+  const float* m = in.o2w;
+  h.pos = f3(m[0] * posObj.x + m[1] * posObj.y + m[2] * posObj.z + m[3],
+             m[4] * posObj.x + m[5] * posObj.y + m[6] * posObj.z + m[7],
+             m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
+  const DdgiMaterialInfo& mat = s.materials[in.material];
+  float3 nObj = f3(c0.z, c0.w, e0.x) * b0 + f3(c1.z, c1.w, e1.x) * b1 + f3(c2.z, c2.w, e2.x) * b2;
+  nObj = normalize3(nObj);
+  if (kMirrorNormal) {
+    h.normal = normalize3(f3(m[0] * nObj.x + m[1] * nObj.y + m[2] * nObj.z, m[4] * nObj.x + m[5] * nObj.y + m[6] * nObj.z,
+                             m[8] * nObj.x + m[9] * nObj.y + m[10] * nObj.z));
+  } else {
+    const float* wi = in.w2oLin;  // normal * WorldToObject (row vector times the inverse 3x3)
+    h.normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6], nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
+                             nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
+  }
+  // the base colour factor wins when its sum exceeds 0.1; otherwise the interpolated vertex colour in
+  // linear space (rchit:183-184, bindless.glsl:199-203)
+  const float4 bcf = __ldg((const float4*)mat.baseColFac);
+  if (bcf.x + bcf.y + bcf.z > 0.1f) {
+    h.color = xyz(bcf);
+  } else {
+    const float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
+    h.color = toLinear(vcol);
+  }
+  const float4 mr = __ldg((const float4*)mat.metRough);
+  const float4 em = __ldg((const float4*)mat.emissive);
+  h.metallic = mr.x;
+  h.roughness = mr.y;
+  h.emissive = xyz(em) * em.w;
+  return h;
+}
+
 // Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
 // computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
 // shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
@@ -307,26 +366,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
       if (leaf < 0) {
         L = toLinear(f.skyColor * f.skyIntensity);  // rmiss:20
       } else {
-        // hit reconstruction (rchit:137-152)
+        const HitSurface h = reconstructHit<false>(s, leaf, hr.z, hr.w);
+        const float3 pos = h.pos;
         const float4 r0 = __ldg(&s.bvh.tris[3 * leaf]);
-        const int inst = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 1].w));
-        const int prim = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 2].w));
-        const InstanceGPU& in = s.instances[inst];
-        const DdgiMeshInfo& mesh = s.meshes[in.mesh];
-        const uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
-        const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
-        const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
-        const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
-        const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
-        const float b1 = hr.z, b2 = hr.w, b0 = 1.0f - b1 - b2;
-        const float4 a0 = __ldg((const float4*)v0.d0), a1 = __ldg((const float4*)v1.d0), a2 = __ldg((const float4*)v2.d0);
-        const float4 c0 = __ldg((const float4*)v0.d1), c1 = __ldg((const float4*)v1.d1), c2 = __ldg((const float4*)v2.d1);
-        const float4 e0 = __ldg((const float4*)v0.d2), e1 = __ldg((const float4*)v1.d2), e2 = __ldg((const float4*)v2.d2);
-        const float3 posObj = xyz(a0) * b0 + xyz(a1) * b1 + xyz(a2) * b2;
-        const float* m = in.o2w;
-        const float3 pos = f3(m[0] * posObj.x + m[1] * posObj.y + m[2] * posObj.z + m[3],
-                              m[4] * posObj.x + m[5] * posObj.y + m[6] * posObj.z + m[7],
-                              m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
         // shadow ray origin toward the sun (rchit:155-176): the light's sheared space when built
         if (s.shadow.tris != nullptr) {
           const float pk[3] = {pos.x, pos.y, pos.z};
@@ -336,37 +378,16 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
           so = pos;
         }
         cast = true;
-        // surface (rchit:179-187, getSurfaceDataFromMat bindless.glsl:181-237 without textures)
-        const DdgiMaterialInfo& mat = s.materials[in.material];
-        float3 nObj = f3(c0.z, c0.w, e0.x) * b0 + f3(c1.z, c1.w, e1.x) * b1 + f3(c2.z, c2.w, e2.x) * b2;
-        nObj = normalize3(nObj);
-        const float* wi = in.w2oLin;  // normal * WorldToObject (row vector times the inverse 3x3)
-        const float3 normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6],
-                                            nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
-                                            nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
-        // the base colour factor wins when its sum exceeds 0.1; otherwise the interpolated vertex colour in
-        // linear space (rchit:183-184, bindless.glsl:199-203)
-        const float4 bcf = __ldg((const float4*)mat.baseColFac);
-        float3 color;
-        if (bcf.x + bcf.y + bcf.z > 0.1f) {
-          color = xyz(bcf);
-        } else {
-          const float3 vcol = f3(a0.w, c0.x, c0.y) * b0 + f3(a1.w, c1.x, c1.y) * b1 + f3(a2.w, c2.x, c2.y) * b2;
-          color = toLinear(vcol);
-        }
-        const float4 mr = __ldg((const float4*)mat.metRough);
-        const float4 em = __ldg((const float4*)mat.emissive);
-        const float metallic = mr.x, roughness = mr.y;
         // lit: L = calcLight; shadowed: L = 0; then += indirect, += emissive (rchit:195-214)
-        L = calcLightDirectional(normal, color, metallic, roughness, pos, origin, f.lightDir, f.sunIntensity);
+        L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, pos, origin, f.lightDir, f.sunIntensity);
         float3 Ls = f3(0.f, 0.f, 0.f);
         if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG) {
-          const float3 ind = calcIndirectDiffuse(g, f, T.atlasPrev, normal, color, metallic, roughness, pos, origin);
+          const float3 ind = calcIndirectDiffuse(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
           L += ind;
           Ls += ind;
         }
-        L += xyz(em) * em.w;
-        Ls += xyz(em) * em.w;
+        L += h.emissive;
+        Ls += h.emissive;
         hits[id] = make_float4(Ls.x, Ls.y, Ls.z, 0.f);
         hitCode = __float_as_int(r0.w) * 2;
       }
@@ -452,7 +473,7 @@ template <bool kWide, bool kAnyHit, bool kShadowMask>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
     k_trace_rays(BvhRef bvh, const DdgiRay* __restrict__ rays, const float4* __restrict__ points, float3 shadowDir,
                  long long count, unsigned long long* __restrict__ counter, int refillLanes, DdgiHit* __restrict__ hits,
-                 float* __restrict__ vis, uint32_t* __restrict__ err) {
+                 float* __restrict__ vis, bool recordIds, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   long long id = -1;
@@ -466,7 +487,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
       vis[i] = hit.leaf >= 0 ? 0.0f : 1.0f;  // shadow.rchit:14 / shadow.rmiss:12
     } else {
       int gid = -1;
-      if (hit.leaf >= 0) gid = __float_as_int(__ldg(&bvh.tris[3 * hit.leaf].w));
+      if (hit.leaf >= 0) gid = recordIds ? hit.leaf : __float_as_int(__ldg(&bvh.tris[3 * hit.leaf].w));
       hits[i] = DdgiHit{hit.leaf >= 0 ? hit.t : 0.0f, hit.leaf >= 0 ? hit.b1 : 0.0f, hit.leaf >= 0 ? hit.b2 : 0.0f, gid};
     }
   };
@@ -524,7 +545,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
 
 cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
                             DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
-                            unsigned long long* counter, uint32_t* err, cudaStream_t stream) {
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds) {
   if (count <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
@@ -534,14 +555,14 @@ cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, l
   const int blocks = sms * 8;
   const int refill = 8;
   if (points) {  // shadow mask: any hit
-    if (wide) k_trace_rays<true, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, err);
-    else k_trace_rays<false, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, err);
+    if (wide) k_trace_rays<true, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err);
+    else k_trace_rays<false, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err);
   } else if (anyHit) {
-    if (wide) k_trace_rays<true, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
-    else k_trace_rays<false, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+    if (wide) k_trace_rays<true, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
+    else k_trace_rays<false, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
   } else {
-    if (wide) k_trace_rays<true, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
-    else k_trace_rays<false, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, err);
+    if (wide) k_trace_rays<true, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
+    else k_trace_rays<false, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
   }
   return cudaGetLastError();
 }
@@ -582,6 +603,120 @@ cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const voi
   long long blocks = (count + 255) / 256;
   if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
   k_query_irradiance<<<(unsigned)blocks, 256, 0, stream>>>(gc, f, atlas, pts, count, out);
+  return cudaGetLastError();
+}
+
+// ---- specular GI mirror pass (SpecularGIRTPass.cpp:111-128; mirror_reflections.rgen/.rchit/.rmiss) ----------
+
+// Ray of each G-buffer point (rgen:38-80): origin = the point, direction = reflect(v, n) = v - 2 dot(n, v) n
+// with v = normalize(point - cameraPos), n = normalize(normal), range [0.1, 50]. A sky point (rgen:52-55) gets
+// an empty range, so the trace reports a miss and the shading writes 0.
+__global__ void __launch_bounds__(256) k_mirror_rays(FrameGPU f, const DdgiMirrorPoint* __restrict__ pts,
+                                                     long long count, DdgiRay* __restrict__ rays) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const DdgiMirrorPoint p = pts[i];
+    const float3 pos = f3(p.position[0], p.position[1], p.position[2]);
+    DdgiRay r;
+    r.origin[0] = pos.x; r.origin[1] = pos.y; r.origin[2] = pos.z;
+    if (p.sky != 0.0f) {
+      r.direction[0] = 0.0f; r.direction[1] = 0.0f; r.direction[2] = 1.0f;
+      r.tmin = 1.0f;
+      r.tmax = 0.0f;
+    } else {
+      const float3 n = normalize3(f3(p.normal[0], p.normal[1], p.normal[2]));
+      const float3 v = normalize3(pos - f.camPos);
+      const float3 d = v - n * (2.0f * dot3(n, v));
+      r.direction[0] = d.x; r.direction[1] = d.y; r.direction[2] = d.z;
+      r.tmin = kTMin;
+      r.tmax = kTMax;
+    }
+    rays[i] = r;
+  }
+}
+
+// Mirror hits (rchit:24-117) and misses (rmiss:17-21), one thread per point. A hit gets both radiance
+// values, lit = calcLight + indirect + emissive and shadowed = indirect + emissive (the reference's order of
+// additions), with the indirect term when DDGI_UBO_DDGI_FLAG is set (rchit:106) and the hit distance in .w
+// (rchit:90); its world position becomes the point of a shadow ray (w = 0). Misses: the linear sky with
+// distance 1e6; sky points: 0. Neither casts a shadow ray (w = 1).
+__global__ void __launch_bounds__(256) k_mirror_shade(SceneGPU s, GridGPU g, FrameGPU f, const void* __restrict__ atlas,
+                                                      const DdgiMirrorPoint* __restrict__ pts,
+                                                      const DdgiHit* __restrict__ hits, long long count,
+                                                      float4* __restrict__ out, float4* __restrict__ shadowed,
+                                                      float4* __restrict__ spts) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const DdgiMirrorPoint& p = pts[i];
+    const DdgiHit hr = hits[i];
+    float4 lit = make_float4(0.f, 0.f, 0.f, 0.f), dark = lit, sp = make_float4(0.f, 0.f, 0.f, 1.f);
+    if (p.sky == 0.0f) {
+      if (hr.triangle < 0) {
+        const float3 sky = toLinear(f.skyColor * f.skyIntensity);
+        lit = dark = make_float4(sky.x, sky.y, sky.z, 1e6f);
+      } else {
+        const float3 origin = f3(p.position[0], p.position[1], p.position[2]);
+        const HitSurface h = reconstructHit<true>(s, hr.triangle, hr.b1, hr.b2);
+        const float3 d = h.pos - origin;
+        const float dist = sqrtf(dot3(d, d));
+        float3 L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, h.pos, origin, f.lightDir,
+                                        f.sunIntensity);
+        float3 Ls = f3(0.f, 0.f, 0.f);
+        if (f.flags & DDGI_UBO_DDGI_FLAG) {
+          const float3 ind = calcIndirectDiffuse(g, f, atlas, h.normal, h.color, h.metallic, h.roughness, h.pos, origin);
+          L += ind;
+          Ls += ind;
+        }
+        L += h.emissive;
+        Ls += h.emissive;
+        lit = make_float4(L.x, L.y, L.z, dist);
+        dark = make_float4(Ls.x, Ls.y, Ls.z, dist);
+        sp = make_float4(h.pos.x, h.pos.y, h.pos.z, 0.f);
+      }
+    }
+    out[i] = lit;
+    shadowed[i] = dark;
+    spts[i] = sp;
+  }
+}
+
+// A hit whose shadow ray found geometry takes the shadowed radiance (rchit:92-104).
+__global__ void __launch_bounds__(256) k_mirror_resolve(const float* __restrict__ vis, const float4* __restrict__ shadowed,
+                                                        float4* __restrict__ out, long long count) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    if (vis[i] == 0.0f) out[i] = shadowed[i];
+}
+
+size_t mirrorScratchBytes(long long count) { return (size_t)count * (32 + 16 + 16 + 16 + 4); }
+
+cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f, const void* atlas,
+                         const DdgiMirrorPoint* pts, long long count, float4* out, void* scratch,
+                         unsigned long long* counter, uint32_t* err, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  char* b = static_cast<char*>(scratch);
+  DdgiRay* rays = reinterpret_cast<DdgiRay*>(b);
+  DdgiHit* hits = reinterpret_cast<DdgiHit*>(b + (size_t)count * 32);
+  float4* spts = reinterpret_cast<float4*>(b + (size_t)count * 48);
+  float4* dark = reinterpret_cast<float4*>(b + (size_t)count * 64);
+  float* vis = reinterpret_cast<float*>(b + (size_t)count * 80);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long blocks = (count + 255) / 256;
+  if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+  k_mirror_rays<<<(unsigned)blocks, 256, 0, stream>>>(f, pts, count, rays);
+  const bool wide = s.bvh.wnodes != nullptr;
+  cudaError_t e = launchTraceRays(s.bvh, wide, rays, count, false, hits, nullptr, f3(0.f, 0.f, 0.f), nullptr, counter,
+                                  err, stream, true);
+  if (e != cudaSuccess) return e;
+  k_mirror_shade<<<(unsigned)blocks, 256, 0, stream>>>(s, g, f, atlas, pts, hits, count, out, dark, spts);
+  // the shadow ray of rchit:45-66: normalize(-lightDir) over [0.1, 50], terminating on the first hit
+  const float3 ld = f.lightDir * -1.0f;
+  const float3 sdir = ld * (1.0f / sqrtf(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z));
+  e = launchTraceRays(s.bvh, wide, nullptr, count, true, nullptr, spts, sdir, vis, counter, err, stream, false);
+  if (e != cudaSuccess) return e;
+  k_mirror_resolve<<<(unsigned)blocks, 256, 0, stream>>>(vis, dark, out, count);
   return cudaGetLastError();
 }
 

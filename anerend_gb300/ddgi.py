@@ -241,6 +241,15 @@ class ProbeGrid:
         self.ctx.check(self.ctx.lib.ddgi_query_irradiance(self.handle, C.byref(f), points_ptr, count, ambient_ptr,
                                                           stream))
 
+    def mirror_reflections(self, scene: "Scene", frame: "FrameParams", points_ptr: int, count: int, out_ptr: int,
+                           stream: int = 0) -> None:
+        """The specular GI mirror pass for `count` device DdgiMirrorPoint records into device float4
+        (radiance, hit distance), with this grid's current atlas (mirror_reflections.rgen/.rchit/.rmiss),
+        stream-ordered."""
+        f = frame.to_c()
+        self.ctx.check(self.ctx.lib.ddgi_mirror_reflections(self.handle, scene.handle, C.byref(f), points_ptr, count,
+                                                            out_ptr, stream))
+
     def close(self) -> None:
         if self.handle:
             self.ctx.lib.ddgi_grid_destroy(self.handle)

@@ -321,6 +321,29 @@ typedef struct DdgiSurfacePoint {
 int  ddgi_query_irradiance(DdgiGrid* grid, const DdgiFrame* frame, const DdgiSurfacePoint* points, uint64_t count,
                            float* ambient, void* stream);
 
+/* ---- specular GI: mirror reflections of G-buffer points ---------------------------------------------------- */
+
+/* One G-buffer point for the mirror pass (32 bytes): its world position (calcWorldPos of the depth sample,
+ * mirror_reflections.rgen:28-36), `sky` != 0 for a sky pixel (depth == 1), and the normal of Geometry0Image
+ * (need not be unit length; the shader normalises it). */
+typedef struct DdgiMirrorPoint {
+  float position[3];
+  float sky;
+  float normal[3];
+  float reserved;
+} DdgiMirrorPoint;
+
+/* The specular GI ray-traced pass (SpecularGIRTPass.cpp:111-128, mirror_reflections.rgen/.rchit/.rmiss): per
+ * point a ray from the point along reflect(normalize(point - frame->cameraPos), normalize(normal)) over
+ * [0.1, 50], closest hit; a hit is shaded as the probe update's (a shadow ray along normalize(-lightDir),
+ * calcLight when lit, the DDGI indirect term from the grid's current atlas when DDGI_UBO_DDGI_FLAG is set,
+ * emissive) with the normal through mat3(ObjectToWorld); the atlas is sampled with REPEAT addressing, the
+ * default sampler the pass binds, and the grid's DDGI_GRID_EDGE_CLAMP neighbour rule. out: device float4 per point,
+ * (radiance, hit distance); a miss gives (linear sky, 1e6), a sky point 0. FP32 where the reference stores
+ * RGBA16F "ReflectTex". Stream-ordered. */
+int  ddgi_mirror_reflections(DdgiGrid* grid, DdgiScene* scene, const DdgiFrame* frame, const DdgiMirrorPoint* points,
+                             uint64_t count, float* out, void* stream);
+
 /* ---- batched form: many grids in one persistent trace launch and one convolution launch ---------------- */
 
 typedef struct DdgiBatch DdgiBatch;

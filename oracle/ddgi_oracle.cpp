@@ -468,6 +468,53 @@ void parallelFor(long long n, int threads, F&& f) {
 
 }  // namespace
 
+// Radiance of a closest hit seen from `origin` (irradiance_probe_update.rchit:137-214; with `mirror`,
+// mirror_reflections.rchit:24-117: the normal through mat3(ObjectToWorld) instead of normal * WorldToObject,
+// and the DDGI term on UBO_DDGI_FLAG instead of UBO_DDGI_MULTI_FLAG). Returns the world hit position, whether
+// the shadow ray toward normalize(-lightDir) hit, and whether that decision is near a tie.
+d3 shadeHit(const OracleScene& s, const Grid& g, const DdgiFrame* f, const double* atlas, const Query& q, d3 origin,
+            bool mirror, d3& pos, bool& shadowed, bool& sunc) {
+  const d3 lightDir = D3(f->lightDir[0], f->lightDir[1], f->lightDir[2]);
+  const DdgiInstance& in = s.insts[q.inst];
+  const DdgiMeshInfo& m = s.meshes[in.mesh];
+  const DdgiPackedVertex* v[3];
+  for (int k = 0; k < 3; ++k) v[k] = &s.verts[m.vertexOffset + s.indices[m.indexOffset + 3 * q.prim + k]];
+  double b1 = q.b1, b2 = q.b2, b0 = 1.0 - b1 - b2;
+  double bb[3] = {b0, b1, b2};
+  pos = D3(0, 0, 0);
+  d3 nrm = D3(0, 0, 0), col = D3(0, 0, 0);
+  for (int k = 0; k < 3; ++k) {
+    const DdgiPackedVertex& pv = *v[k];
+    pos = pos + D3(pv.d0[0], pv.d0[1], pv.d0[2]) * bb[k];
+    col = col + D3(pv.d0[3], pv.d1[0], pv.d1[1]) * bb[k];
+    nrm = nrm + D3(pv.d1[2], pv.d1[3], pv.d2[0]) * bb[k];
+  }
+  pos = xform(in.transform, pos);
+  sunc = false;
+  shadowed = anyHit(s, pos, normalize(-lightDir), sunc);
+  nrm = normalize(nrm);
+  d3 normal;
+  if (mirror) {
+    const float* t = in.transform;  // mat3(ObjectToWorld) * n
+    normal = normalize(D3(t[0] * nrm.x + t[1] * nrm.y + t[2] * nrm.z, t[4] * nrm.x + t[5] * nrm.y + t[6] * nrm.z,
+                          t[8] * nrm.x + t[9] * nrm.y + t[10] * nrm.z));
+  } else {
+    const double* wi = &s.w2o[9 * q.inst];
+    normal = normalize(D3(nrm.x * wi[0] + nrm.y * wi[3] + nrm.z * wi[6], nrm.x * wi[1] + nrm.y * wi[4] + nrm.z * wi[7],
+                          nrm.x * wi[2] + nrm.y * wi[5] + nrm.z * wi[8]));
+  }
+  d3 color = toLinear(col);
+  const DdgiMaterialInfo& mat = s.mats[in.material];
+  if ((double)mat.baseColFac[0] + mat.baseColFac[1] + mat.baseColFac[2] > 0.1)
+    color = D3(mat.baseColFac[0], mat.baseColFac[1], mat.baseColFac[2]);
+  double metallic = mat.metRough[0], rough = mat.metRough[1];
+  d3 L = D3(0, 0, 0);
+  if (!shadowed) L = calcLight(normal, color, metallic, rough, pos, origin, lightDir, f->sunIntensity);
+  if (f->flags & (mirror ? DDGI_UBO_DDGI_FLAG : DDGI_UBO_DDGI_MULTI_FLAG))
+    L = L + calcIndirect(g, f, atlas, normal, color, metallic, rough, pos, origin);
+  return L + D3(mat.emissive[0], mat.emissive[1], mat.emissive[2]) * (double)mat.emissive[3];
+}
+
 extern "C" {
 
 // Builds the FP64 scene: world-space triangles in global-id order (instance order, then primitive).
@@ -539,7 +586,6 @@ int oracle_trace(void* scene, const DdgiGridDesc* desc, const DdgiFrame* f, cons
   lattice(g.N, f->rotation, dirs);
   d3 stepv, offv;
   probeFrame(g, f, stepv, offv);
-  d3 lightDir = D3(f->lightDir[0], f->lightDir[1], f->lightDir[2]);
   d3 sky = toLinear(D3(f->skyColor[0], f->skyColor[1], f->skyColor[2]) * (double)f->skyIntensity);  // rmiss:20
   long long perLayer = (long long)g.X * g.Z * g.N;
   long long total = perLayer * (layerEnd - layerBegin);
@@ -564,37 +610,10 @@ int oracle_trace(void* scene, const DdgiGridDesc* desc, const DdgiFrame* f, cons
     if (q.gid < 0) {
       L = sky;
     } else {
-      // rchit:137-187
-      const DdgiInstance& in = s.insts[q.inst];
-      const DdgiMeshInfo& m = s.meshes[in.mesh];
-      const DdgiPackedVertex* v[3];
-      for (int k = 0; k < 3; ++k) v[k] = &s.verts[m.vertexOffset + s.indices[m.indexOffset + 3 * q.prim + k]];
-      double b1 = q.b1, b2 = q.b2, b0 = 1.0 - b1 - b2;
-      double bb[3] = {b0, b1, b2};
-      d3 pos = D3(0, 0, 0), nrm = D3(0, 0, 0), col = D3(0, 0, 0);
-      for (int k = 0; k < 3; ++k) {
-        const DdgiPackedVertex& pv = *v[k];
-        pos = pos + D3(pv.d0[0], pv.d0[1], pv.d0[2]) * bb[k];
-        col = col + D3(pv.d0[3], pv.d1[0], pv.d1[1]) * bb[k];
-        nrm = nrm + D3(pv.d1[2], pv.d1[3], pv.d2[0]) * bb[k];
-      }
-      pos = xform(in.transform, pos);
-      bool sunc = false;
-      bool shadowed = anyHit(s, pos, normalize(-lightDir), sunc);
+      bool sunc = false, shadowed = false;
+      d3 pos;
+      L = shadeHit(s, g, f, atlasPrev, q, origin, false, pos, shadowed, sunc);
       if (sunc) unc |= 2;
-      nrm = normalize(nrm);
-      const double* wi = &s.w2o[9 * q.inst];
-      d3 normal = normalize(D3(nrm.x * wi[0] + nrm.y * wi[3] + nrm.z * wi[6], nrm.x * wi[1] + nrm.y * wi[4] + nrm.z * wi[7],
-                               nrm.x * wi[2] + nrm.y * wi[5] + nrm.z * wi[8]));
-      d3 color = toLinear(col);
-      const DdgiMaterialInfo& mat = s.mats[in.material];
-      if ((double)mat.baseColFac[0] + mat.baseColFac[1] + mat.baseColFac[2] > 0.1)
-        color = D3(mat.baseColFac[0], mat.baseColFac[1], mat.baseColFac[2]);
-      double metallic = mat.metRough[0], rough = mat.metRough[1];
-      L = D3(0, 0, 0);
-      if (!shadowed) L = calcLight(normal, color, metallic, rough, pos, origin, lightDir, f->sunIntensity);
-      if (f->flags & DDGI_UBO_DDGI_MULTI_FLAG) L = L + calcIndirect(g, f, atlasPrev, normal, color, metallic, rough, pos, origin);
-      L = L + D3(mat.emissive[0], mat.emissive[1], mat.emissive[2]) * (double)mat.emissive[3];
       code = q.gid * 2 + (shadowed ? 1 : 0);
     }
     int rx = px * g.bw + j % g.bw;
@@ -705,6 +724,49 @@ int oracle_query_irradiance(const DdgiGridDesc* desc, const DdgiFrame* f, const 
     out[3 * i + 1] = amb.y;
     out[3 * i + 2] = amb.z;
   }
+  return 0;
+}
+
+// mirror_reflections.rgen/.rchit/.rmiss on FP64: pts holds 8 floats per point (position, sky, normal, unused),
+// out 4 doubles per point (radiance, hit distance); uncertain: bit 0 the reflected ray's hit is near a tie
+// or an edge, bit 1 its shadow ray's. The atlas is sampled as by the probe update (REPEAT addressing).
+int oracle_mirror_reflections(void* scene, const DdgiGridDesc* desc, const DdgiFrame* f, const double* atlas,
+                              const float* pts, int64_t count, double* out, uint8_t* uncertainOut, int threads) {
+  const OracleScene& s = *static_cast<OracleScene*>(scene);
+  Grid g = makeGrid(desc);
+  const d3 cam = D3(f->cameraPos[0], f->cameraPos[1], f->cameraPos[2]);
+  const d3 sky = toLinear(D3(f->skyColor[0], f->skyColor[1], f->skyColor[2]) * (double)f->skyIntensity);  // rmiss:20
+  parallelFor(count, threads, [&](long long i) {
+    const float* p = pts + 8 * i;
+    double* o = out + 4 * i;
+    uint8_t unc = 0;
+    if (p[3] != 0.0f) {  // rgen:52-55
+      o[0] = o[1] = o[2] = o[3] = 0.0;
+    } else {
+      const d3 origin = D3(p[0], p[1], p[2]);
+      const d3 n = normalize(D3(p[4], p[5], p[6]));
+      const d3 v = normalize(origin - cam);
+      const d3 dir = v - n * (2.0 * dot(n, v));  // reflect (rgen:61)
+      Query q;
+      closestHit(s, origin, dir, q);
+      if (q.gid >= 0) {
+        if (q.bmin < kEpsBary || q.t < kTMin + kEpsT || q.t > kTMax - kEpsT) unc |= 1;
+        if (q.tSecond <= q.t * (1.0 + kEpsTRel) + kEpsT) unc |= 1;
+      }
+      if (q.tFuzzyMin <= (q.gid >= 0 ? q.t * (1.0 + kEpsTRel) + kEpsT : kTMax + kEpsT)) unc |= 1;
+      if (q.gid < 0) {
+        o[0] = sky.x; o[1] = sky.y; o[2] = sky.z; o[3] = 1e6;
+      } else {
+        bool shadowed = false, sunc = false;
+        d3 pos;
+        const d3 L = shadeHit(s, g, f, atlas, q, origin, true, pos, shadowed, sunc);
+        if (sunc) unc |= 2;
+        const d3 dd = pos - origin;
+        o[0] = L.x; o[1] = L.y; o[2] = L.z; o[3] = std::sqrt(dot(dd, dd));  // rchit:90
+      }
+    }
+    if (uncertainOut) uncertainOut[i] = unc;
+  });
   return 0;
 }
 

@@ -59,6 +59,8 @@ def load():
         lib.oracle_closest_hit.argtypes = [vp, vp, vp, vp, vp, vp]
         lib.oracle_query_irradiance.restype = ip
         lib.oracle_query_irradiance.argtypes = [vp, vp, vp, vp, C.c_int64, vp]
+        lib.oracle_mirror_reflections.restype = ip
+        lib.oracle_mirror_reflections.argtypes = [vp, vp, vp, vp, vp, C.c_int64, vp, vp, ip]
         _lib = lib
     return _lib
 
@@ -213,3 +215,14 @@ def query_irradiance(desc, frame, atlas: np.ndarray, points: np.ndarray) -> np.n
     load().oracle_query_irradiance(C.addressof(desc), C.addressof(frame), _p(a), _p(pts), len(pts), _p(out))
     return out
 
+
+def mirror_reflections(scene: OracleScene, desc, frame, atlas: np.ndarray, points: np.ndarray, threads: int = 0):
+    """mirror_reflections.rgen/.rchit/.rmiss on FP64: (radiance, hit distance) per MIRROR_POINT record (count x 4)
+    and the uncertainty bits per point (1: the reflected ray near a tie or an edge, 2: its shadow ray)."""
+    a = np.ascontiguousarray(atlas, np.float64)
+    pts = np.ascontiguousarray(points)
+    out = np.empty((len(pts), 4), np.float64)
+    unc = np.zeros(len(pts), np.uint8)
+    scene.lib.oracle_mirror_reflections(scene.handle, C.addressof(desc), C.addressof(frame), _p(a), _p(pts), len(pts),
+                                        _p(out), _p(unc), threads)
+    return out, unc

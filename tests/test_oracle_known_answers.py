@@ -287,3 +287,76 @@ def test_consumer_clamps_to_edge():
     ks = 0.04 + (np.maximum(0.75, 0.04) - 0.04) * (1.0 - max(float(n @ v), 0.0)) ** 5
     want = (1.0 - ks) * (0.25 * 0.5 * 3.1415926 * np.array([0.5, 0.6, 0.7]))
     assert np.allclose(out[0], want, rtol=1e-6)  # every sample from the dim right half
+
+
+# ---- specular GI mirror pass (mirror_reflections.rgen/.rchit/.rmiss) ---------------------------------------
+
+def _mirror_world():
+    """A floor (y = 0), an emissive wall at z = 3 facing +z and a small occluder above the wall at y = 5."""
+    floor = scenes.floor_quad(0.0, 4.0)
+    wall = np.array([[[-2, 0, 3], [2, 0, 3], [2, 6, 3]], [[-2, 0, 3], [2, 6, 3], [-2, 6, 3]]], np.float64)
+    occ = np.array([[[-1, 5, 2.5], [1, 5, 2.5], [1, 5, 3.5]], [[-1, 5, 2.5], [1, 5, 3.5], [-1, 5, 3.5]]], np.float64)
+    tris = np.concatenate([floor, wall, occ])
+    mats = scenes.random_materials(0, 3)
+    mats["baseColFac"] = [[0.3, 0.3, 0.3, 1.0], [0.5, 0.6, 0.7, 1.0], [0.2, 0.2, 0.2, 1.0]]
+    mats["metRough"][:, :2] = [[0.0, 0.5], [0.0, 0.5], [0.0, 0.5]]
+    mats["emissive"] = [[0, 0, 0, 0], [1.0, 2.0, 3.0, 1.0], [0, 0, 0, 0]]
+    return scenes.assemble(tris, np.array([0, 0, 1, 1, 2, 2]), np.arange(3), mats)
+
+
+def _mirror_points():
+    p = np.zeros(3, L.MIRROR_POINT)
+    p["position"] = [[0.5, 0.0, 0.0], [0.5, 1.0, -6.0], [1.0, 1.0, 1.0]]
+    p["normal"] = [[0.0, 1.0, 0.0], [0.0, 1.0, 0.0], [0.0, 1.0, 0.0]]
+    p["sky"] = [0.0, 0.0, 1.0]
+    return p
+
+
+def _mirror_frame(flags, sun=3.0):
+    f = L.Frame()
+    f.cameraPos[:] = [0.5, 2.0, -2.0]
+    f.lightDir[:] = [0.0, -1.0, 0.0]
+    f.sunIntensity = sun
+    f.skyColor[:] = [0.4, 0.5, 0.7]
+    f.skyIntensity = 1.0
+    f.flags = flags
+    return f
+
+
+def test_mirror_shadowed_emitter_miss_and_sky():
+    """From (0.5,0,0) with normal +y and the camera at (0.5,2,-2) the reflected ray runs along (0,1,1)/sqrt2 to
+    the wall at (0.5,3,3), distance 3 sqrt2, away from the edges of both walls' triangles; the occluder shadows
+    that point and without DDGI the radiance is the
+    wall's emission. The second point reflects into the empty sky: linear sky, 1e6; the sky pixel gets 0."""
+    arrays = _mirror_world()
+    s = oracle.OracleScene(arrays, L.SceneDesc)
+    try:
+        out, unc = oracle.mirror_reflections(s, grid_desc(), _mirror_frame(0), np.zeros((80, 40, 4)), _mirror_points())
+    finally:
+        s.close()
+    assert np.all(unc == 0)
+    assert np.allclose(out[0], [1.0, 2.0, 3.0, 3.0 * math.sqrt(2.0)], rtol=1e-12)
+    c = np.array([0.4, 0.5, 0.7])
+    sky = np.where(c < 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4)  # toLinear (bindless.glsl:240-247)
+    assert np.allclose(out[1], [*sky, 1e6], rtol=1e-7)
+    assert np.array_equal(out[2], np.zeros(4))
+
+
+@pytest.mark.parametrize("flags,indirect", [(L.DDGI_UBO_DDGI_FLAG, True), (L.DDGI_UBO_DDGI_MULTI_FLAG, False)])
+def test_mirror_indirect_term_gated_by_ddgi_flag(flags, indirect):
+    """With the sun off, a constant atlas c gives the wall hit L = kD (c 0.5 3.1415926 albedo) + emission, kD =
+    1 - kS with kS = F0 + (max(1 - r^2, F0) - F0) (1 - max(n.v, 0))^5 = 0.75 (the wall's normal +z points away
+    from the viewer, n.v < 0); the mirror pass gates it on UBO_DDGI_FLAG (rchit:106), not the multi flag."""
+    arrays = _mirror_world()
+    atlas = np.zeros((80, 40, 4))
+    atlas[..., :3] = [0.2, 0.4, 0.8]
+    s = oracle.OracleScene(arrays, L.SceneDesc)
+    try:
+        out, unc = oracle.mirror_reflections(s, grid_desc(), _mirror_frame(flags, sun=0.0), atlas, _mirror_points()[:1])
+    finally:
+        s.close()
+    assert unc[0] == 0
+    want = np.array([1.0, 2.0, 3.0])
+    if indirect:
+        want = want + 0.25 * (np.array([0.2, 0.4, 0.8]) * 0.5 * 3.1415926 * np.array([0.5, 0.6, 0.7]))
+    assert np.allclose(out[0, :3], want, rtol=1e-6)  # float32 material inputs
