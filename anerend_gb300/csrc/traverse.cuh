@@ -280,6 +280,23 @@ constexpr int kWideStack = 64;
 
 static_assert(8 * kWideLeafMax <= 32, "a wide node's triangles must fit the 32-bit pending mask");
 
+// Internal-slot mask (bit s set when slot s holds a wide node: meta byte (7 << 5) | rank) of the two meta
+// words. Per byte the top three bits ANDed into bit 7, then the four bits 7, 15, 23, 31 gathered into the
+// low nibble by one multiply (the partial products land on distinct bits, so nothing carries).
+DDGI_HD uint32_t internalSlots(uint32_t m03, uint32_t m47) {
+  const uint32_t a = (m03 & (m03 << 1) & (m03 << 2) & 0x80808080u) >> 7;
+  const uint32_t b = (m47 & (m47 << 1) & (m47 << 2) & 0x80808080u) >> 7;
+  return ((a * 0x01020408u) >> 24 & 0xfu) | ((b * 0x01020408u) >> 20 & 0xf0u);
+}
+
+// Slot bits to key bits (key = slot ^ oct): swap bit pairs, pairs of pairs and nibbles per octant bit.
+DDGI_HD uint32_t slotsToKeys(uint32_t x, uint32_t oct) {
+  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+  if (oct & 4u) x = ((x & 0x0fu) << 4) | (x >> 4);
+  return x;
+}
+
 // node: the next wide node to test, -1 when the stack is exhausted. tMask: triangles of the last tested
 // node's hit leaves still to test, as bits of offsets from tBase; a step tests one of them.
 struct WideTrav {
@@ -394,12 +411,11 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
   const int nxw = (oct & 1) ? 6 : 0, fxw = 6 - nxw;
   const int nyw = (oct & 2) ? 8 : 2, fyw = 10 - nyw;
   const int nzw = (oct & 4) ? 10 : 4, fzw = 14 - nzw;
-  uint32_t ihits = 0, imask = 0, lhits = 0;
+  uint32_t hm = 0;  // slots whose box the ray meets
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int h = c >> 2, k = c & 3;
     const uint32_t sel = 0x7604u | ((uint32_t)k << 4);
-    const uint32_t m = ((c < 4 ? hd.z : hd.w) >> (8 * k)) & 0xffu;
     const float vnx = asFloatHd(bytePerm(qw[nxw + h], 0x3F800000u, sel));
     const float vfx = asFloatHd(bytePerm(qw[fxw + h], 0x3F800000u, sel));
     const float vny = asFloatHd(bytePerm(qw[nyw + h], 0x3F800000u, sel));
@@ -416,27 +432,20 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
       const float tf = min3f(fmaf(vfx, A[0], Bf[0]), fmaf(vfy, A[1], Bf[1]), fminf(fmaf(vfz, A[2], Bf[2]), hit.t));
       in = tn <= tf * 1.0000004f;
     }
-    const bool internal = (m >> 5) == 7u;
-    imask |= (internal ? 1u : 0u) << c;
-    if (m != 0u && in) {
-      if (internal) ihits |= 1u << (c ^ oct);
-      else lhits |= 1u << c;
-    }
+    hm |= (in ? 1u : 0u) << c;
   }
 #else
   const uint4 hd = ldRo(reinterpret_cast<const uint4*>(nd));
-  uint32_t ihits = 0, imask = 0, lhits = 0;
+  uint32_t hm = 0;  // slots whose box the ray meets
   // two halves of four slots each: six float4 of planes per half keep the register footprint small
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const float4 nx = ldRo(nd + nxo + h), fx = ldRo(nd + fxo + h);
     const float4 ny = ldRo(nd + nyo + h), fy = ldRo(nd + fyo + h);
     const float4 nz = ldRo(nd + nzo + h), fz = ldRo(nd + fzo + h);
-    const uint32_t mh = h ? hd.w : hd.z;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int c = 4 * h + q;
-      const uint32_t m = (mh >> (8 * q)) & 0xffu;
       const float pnx = q == 0 ? nx.x : q == 1 ? nx.y : q == 2 ? nx.z : nx.w;
       const float pfx = q == 0 ? fx.x : q == 1 ? fx.y : q == 2 ? fx.z : fx.w;
       const float pny = q == 0 ? ny.x : q == 1 ? ny.y : q == 2 ? ny.z : ny.w;
@@ -454,15 +463,14 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
                                fminf(fmaf(pfz, r.invd.z, r.fAdd.z), hit.t));
         in = tn <= tf * 1.0000004f;
       }
-      const bool internal = (m >> 5) == 7u;
-      imask |= (internal ? 1u : 0u) << c;
-      if (m != 0u && in) {
-        if (internal) ihits |= 1u << (c ^ oct);
-        else lhits |= 1u << c;
-      }
+      hm |= (in ? 1u : 0u) << c;
     }
   }
 #endif
+  // internal hits in key order; the rest are leaves (an empty slot, meta 0, adds no triangle)
+  const uint32_t imask = internalSlots(hd.z, hd.w);
+  uint32_t ihits = slotsToKeys(hm & imask, oct);
+  uint32_t lhits = hm & ~imask;
   // the hit leaves' triangles: offsets (m & 31) .. + count from triBase
   uint32_t tm = 0;
   while (lhits) {
