@@ -158,17 +158,18 @@ struct RaySlot {
   bool valid;
 };
 
-DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restrict__ order, long long warp,
+DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restrict__ order, uint32_t warp,
                        int lane) {
   RaySlot r;
   r.valid = false;
   const int D = 32 / g.warpProbes;
-  const int dirChunks = g.N / D;
-  const int probeGroups = (g.X * g.Z + g.warpProbes - 1) / g.warpProbes;
-  const int dc = (int)(warp % dirChunks);
-  const long long rest = warp / dirChunks;
-  const int pg = (int)(rest % probeGroups);
-  r.layer = f.layerBegin + (int)(rest / probeGroups);
+  const uint32_t dirChunks = (uint32_t)(g.N / D);
+  const uint32_t probeGroups = (uint32_t)((g.X * g.Z + g.warpProbes - 1) / g.warpProbes);
+  const uint32_t rest = warp / dirChunks;
+  const int dc = (int)(warp - rest * dirChunks);
+  const uint32_t lq = rest / probeGroups;
+  const int pg = (int)(rest - lq * probeGroups);
+  r.layer = f.layerBegin + (int)lq;
   if (r.layer >= f.layerEnd) return r;
   const int p = pg * g.warpProbes + lane / D;
   if (p >= g.X * g.Z) return r;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
       if (id < 0 && cand < totalRays) {
         const long long warp = cand >> 5;
         const TraceItem& T = items[findItem(items, numItems, warp)];
-        const RaySlot rs = raySlot(T.g, T.f, T.order, warp - T.warpBegin, (int)(cand & 31));
+        const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(cand & 31));
         if (!rs.valid) {
           hits[cand] = make_float4(__int_as_float(kNoRay), 0.f, 0.f, 0.f);
         } else {
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
       const SceneGPU& s = T.s;
       const GridGPU& g = T.g;
       const FrameGPU& f = T.f;
-      const RaySlot rs = raySlot(g, f, T.order, warp - T.warpBegin, (int)(id & 31));
+      const RaySlot rs = raySlot(g, f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
       const float3 origin = probeOrigin(g, f, rs);
       const float3 dir = xyz(__ldg(&T.lattice[rs.j]));
       float3 L;
@@ -411,19 +412,19 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
   }
 }
 
-// Shadow rays (rchit:155-176): any hit in [0.1, 50] toward the sun; a shadowed ray's radiance becomes the
-// shadowed value the shading pass parked in its hit record, and its hit code gets the shadow bit.
+// Shadow rays (rchit:155-176): any hit in [0.1, 50] toward the sun; a shadowed ray gets the top bit of its
+// shadow record's slot id set, and k_shadow_resolve gives it the shadowed radiance. Keeping the output
+// writes out of this kernel keeps its finishing lanes (a few per warp at a time) to one store.
 // kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
 template <bool kWide, bool kLightSpace>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
-    k_trace_shadow(const TraceItem* __restrict__ items, int numItems, const float4* __restrict__ shadowList,
-                   unsigned long long* __restrict__ counters, int refillLanes, const float4* __restrict__ hits,
-                   uint32_t* __restrict__ err) {
+    k_trace_shadow(const TraceItem* __restrict__ items, int numItems, float4* __restrict__ shadowList,
+                   unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const long long total = (long long)counters[1];
-  long long id = -1;
-  int item = 0;
+  long long id = -1;  // shadow record index of this lane's ray
+  uint32_t slot = 0;
   bool drained = total == 0;
   BvhRef bvh;
   WRay ray;
@@ -442,9 +443,9 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
       const long long k = (long long)base + __popc(idle & below);
       if (id < 0 && k < total) {
         const float4 rec = shadowList[k];
-        id = (long long)__float_as_uint(rec.w);
-        item = findItem(items, numItems, id >> 5);
-        const TraceItem& T = items[item];
+        id = k;
+        slot = __float_as_uint(rec.w);
+        const TraceItem& T = items[findItem(items, numItems, (long long)(slot >> 5))];
         bvh = kLightSpace ? T.s.shadow : T.s.bvh;
         ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
@@ -452,17 +453,33 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
     }
     if (id >= 0 && !finished) finished = travStep<kWide, true, kLightSpace>(bvh, ray, st, hit, err);
     if (id >= 0 && finished) {
-      if (hit.leaf >= 0) {
-        const TraceItem& T = items[item];
-        const RaySlot rs = raySlot(T.g, T.f, T.order, (id >> 5) - T.warpBegin, (int)(id & 31));
-        const float3 Ls = xyz(hits[id]);
-        const size_t idx = rayIndex(T.g, rs);
-        T.rayRad[idx] = make_float4(Ls.x, Ls.y, Ls.z, 1.0f);
-        if (T.rayHit) T.rayHit[idx] |= 1;
-        if (T.g.rad16) storeRad16(T.g, rs, Ls);
-      }
+      if (hit.leaf >= 0) reinterpret_cast<uint32_t*>(shadowList + id)[3] = slot | 0x80000000u;
       id = -1;
     }
+  }
+}
+
+// Shadowed rays' outputs, one thread per shadow record: the shadowed radiance k_shade parked in the hit
+// record replaces the lit one in the ray image (and the planar 16-bit copy), and the hit code gets its
+// shadow bit.
+__global__ void __launch_bounds__(256) k_shadow_resolve(const TraceItem* __restrict__ items, int numItems,
+                                                        const float4* __restrict__ shadowList,
+                                                        const unsigned long long* __restrict__ counters,
+                                                        const float4* __restrict__ hits) {
+  const long long total = (long long)counters[1];
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+       k += (long long)gridDim.x * blockDim.x) {
+    const uint32_t u = __float_as_uint(shadowList[k].w);
+    if (!(u & 0x80000000u)) continue;
+    const uint32_t id = u & 0x7fffffffu;
+    const long long warp = id >> 5;
+    const TraceItem& T = items[findItem(items, numItems, warp)];
+    const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
+    const float3 Ls = xyz(hits[id]);
+    const size_t idx = rayIndex(T.g, rs);
+    T.rayRad[idx] = make_float4(Ls.x, Ls.y, Ls.z, 1.0f);
+    if (T.rayHit) T.rayHit[idx] |= 1;
+    if (T.g.rad16) storeRad16(T.g, rs, Ls);
   }
 }
 
@@ -763,7 +780,7 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   k_lattice_batch<<<lg, 128, 0, stream>>>(dItems, dRots);
   if (totalWarps <= 0) return cudaGetLastError();
   const long long rays = totalWarps * 32;
-  if (rays > 0xffffffffll) return cudaErrorInvalidValue;  // shadow records carry 32-bit slot ids
+  if (rays > 0x7fffffffll) return cudaErrorInvalidValue;  // shadow records carry 31-bit slot ids + a flag
   const int refill = refillLanes < 1 ? 1 : (refillLanes > 32 ? 32 : refillLanes);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -777,7 +794,8 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   k_shade<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters);
   auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true> : k_trace_shadow<true, false>)
                      : (lightSpace ? k_trace_shadow<false, true> : k_trace_shadow<false, false>);
-  shadow<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, dHits, err);
+  shadow<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, err);
+  k_shadow_resolve<<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, dShadow, dCounters, dHits);
   return cudaGetLastError();
 }
 

@@ -501,7 +501,7 @@ def run_ours(args, rank, local, world):
         e[2].record()
         grid.convolve(fp, stream)
         e[3].record()
-        launches += 6 + (1 if moved else 0)  # lattice, closest hit, shade, shadow, weights, convolve (+ translate)
+        launches += 7 + (1 if moved else 0)  # lattice, closest hit, shade, shadow, shadow resolve, weights, convolve (+ translate)
         f += 1
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
@@ -569,7 +569,7 @@ def run_ours(args, rank, local, world):
             "wall_s": wall,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 116,
                     "d2h_bytes_per_step": int(grid.buffers.atlasBytes)},
-            "roofline": {"kernel": "trace (k_trace_closest + k_shade + k_trace_shadow)", "bound": "hbm",
+            "roofline": {"kernel": "trace (k_trace_closest + k_shade + k_trace_shadow + k_shadow_resolve)", "bound": "hbm",
                          "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "traffic": traffic, "peak_source": peaks["source"],
