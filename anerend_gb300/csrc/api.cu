@@ -730,7 +730,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
   CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, g->dHits, g->dShadow,
                       ctx->numSms * 8, g->tuning.refillLanes, g->tuning.bvhWidth != 2, g->tuning.shadowMode == 1,
-                      ctx->dErr, st),
+                      ctx->dErr, st, &ti),
      "trace");
   g->tracedBegin = b;
   g->tracedEnd = e;

@@ -33,10 +33,13 @@ constexpr int kTraceCounters = 4;
 // Scratch of one trace launch per ray slot: the hit record and the shadow-list entry (16 B each).
 constexpr size_t kTraceScratchPerRay = 32;
 // Lattices of every item (rotation per item), then the wavefront trace of all items' ray slots:
-// closest-hit traversal, shading, shadow traversal. dHits and dShadow hold 32 * totalWarps float4 each.
+// closest-hit traversal, shading, shadow traversal, shadowed-ray resolve. dHits and dShadow hold
+// 32 * totalWarps float4 each. hOne (numItems == 1): the host copy of the record, passed to the wavefront
+// kernels as a kernel parameter so their per-ray record reads go through the constant bank.
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
-                             int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream);
+                             int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
+                             const TraceItem* hOne = nullptr);
 
 
 // Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's

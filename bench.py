@@ -350,6 +350,8 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
     out = {}
     if only == "precision":
         return {"precision_tc": measure_precision(ctx, stream)}
+    if only == "batched":
+        return measure_batched(ctx, stream, serving=False)
     rays = w.probes * w.rays
     g = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
 
@@ -372,7 +374,18 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
                                            / out["single_grid_tuned_fp32"]["ms_per_update"])
 
     out["precision_tc"] = measure_precision(ctx, stream)
+    out.update(measure_batched(ctx, stream, serving=True))
+    return out
 
+
+def measure_batched(ctx, stream, serving=True):
+    """The 64-grid batched workload against its plain one-grid-at-a-time form and, with `serving`, the serving
+    loop over the same resident scenes."""
+    import torch
+
+    from anerend_gb300 import ddgi, scenes
+
+    out = {}
     # batched workload: 64 grids over 8 scenes, batched tensor-core form vs plain one-grid-at-a-time form
     bwl = scenes.BATCHED
     tris, specs = scenes.batch_layout(bwl)
@@ -415,6 +428,11 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
     batch.close()
     for gg in grids:
         gg.close()
+    if not serving:
+        for sc in scs:
+            sc.close()
+        ctx.sync(stream)
+        return out
 
     # serving: Poisson arrivals over the 8 resident scenes above, at the workload's 2,000 req/s and at 200 req/s
     sw = scenes.SERVING
@@ -596,7 +614,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the other forms (batched, precision, serving)")
-    ap.add_argument("--form", choices=["precision"], help="run only this form and print its measurements")
+    ap.add_argument("--form", choices=["precision", "batched"], help="run only this form and print its measurements")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal tree (8-wide or binary)")
     ap.add_argument("--refill-lanes", type=int, default=8, help="idle lanes before a traversal warp refills (1..32)")
     args = ap.parse_args()
