@@ -180,11 +180,6 @@ DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restric
   return r;
 }
 
-// The record of a warp: with kOne (single-item launches) the kernel parameter copy `one`, read through the
-// constant bank; otherwise a binary search of the launch's record table in global memory.
-template <bool kOne>
-DDGI_D const TraceItem& itemOf(const TraceItem* __restrict__ items, int numItems, const TraceItem& one, long long warp);
-
 DDGI_D int findItem(const TraceItem* __restrict__ items, int numItems, long long warp) {
   int lo = 0, hi = numItems - 1;
   while (lo < hi) {
@@ -194,11 +189,21 @@ DDGI_D int findItem(const TraceItem* __restrict__ items, int numItems, long long
   return lo;
 }
 
-template <bool kOne>
-DDGI_D const TraceItem& itemOf(const TraceItem* __restrict__ items, int numItems, const TraceItem& one, long long warp) {
-  if (kOne) return one;
-  return items[findItem(items, numItems, warp)];
-}
+
+// Where a trace launch's records come from: the first argument of the wavefront kernels, passed by value
+// (__grid_constant__). ItemsOne carries a single-item launch's record itself, so the kernels' per-ray record
+// reads become constant-bank reads at fixed offsets; ItemsGlobal points at the table in global memory (a
+// by-value table of many records, indexed at run time, measured no faster than the L1-resident table).
+// at(warp) is the record that owns ray-slot warp `warp`.
+struct ItemsGlobal {
+  const TraceItem* items;
+  int n;
+  DDGI_D const TraceItem& at(long long warp) const { return items[findItem(items, n, warp)]; }
+};
+struct ItemsOne {
+  TraceItem it;
+  DDGI_D const TraceItem& at(long long) const { return it; }
+};
 
 // ray generation (rgen:51-88)
 DDGI_D float3 probeOrigin(const GridGPU& g, const FrameGPU& f, const RaySlot& rs) {
@@ -245,11 +250,10 @@ DDGI_D bool travStep(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& 
 
 // Closest hits of every ray slot (rgen:90-106). Each lane owns one ray; once at least refillLanes lanes of
 // a warp are idle the warp takes that many new slots from the queue (counters[0]) with one atomic.
-template <bool kWide, bool kOne>
+template <bool kWide, class Src>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
-    k_trace_closest(const TraceItem* __restrict__ items, int numItems, long long totalRays,
-                    unsigned long long* __restrict__ counters, int refillLanes, float4* __restrict__ hits,
-                    uint32_t* __restrict__ err, const __grid_constant__ TraceItem one) {
+    k_trace_closest(const __grid_constant__ Src src, long long totalRays, unsigned long long* __restrict__ counters,
+                    int refillLanes, float4* __restrict__ hits, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   long long id = -1;
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
       const long long cand = (long long)base + __popc(idle & below);
       if (id < 0 && cand < totalRays) {
         const long long warp = cand >> 5;
-        const TraceItem& T = itemOf<kOne>(items, numItems, one, warp);
+        const TraceItem& T = src.at(warp);
         const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(cand & 31));
         if (!rs.valid) {
           hits[cand] = make_float4(__int_as_float(kNoRay), 0.f, 0.f, 0.f);
@@ -353,11 +357,10 @@ DDGI_D HitSurface reconstructHit(const SceneGPU& s, int leaf, float b1, float b2
 // Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
 // computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
 // shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
-template <bool kOne>
-__global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ items, int numItems, long long totalRays,
+template <class Src>
+__global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src src, long long totalRays,
                                                float4* __restrict__ hits, float4* __restrict__ shadowList,
-                                               unsigned long long* __restrict__ counters,
-                                               const __grid_constant__ TraceItem one) {
+                                               unsigned long long* __restrict__ counters) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < totalRays;
@@ -368,7 +371,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
     float3 so = f3(0.f, 0.f, 0.f);
     if (leaf != kNoRay) {
       const long long warp = id >> 5;
-      const TraceItem& T = itemOf<kOne>(items, numItems, one, warp);
+      const TraceItem& T = src.at(warp);
       const SceneGPU& s = T.s;
       const GridGPU& g = T.g;
       const FrameGPU& f = T.f;
@@ -429,11 +432,10 @@ __global__ void __launch_bounds__(256, 4) k_shade(const TraceItem* __restrict__ 
 // shadow record's slot id set, and k_shadow_resolve gives it the shadowed radiance. Keeping the output
 // writes out of this kernel keeps its finishing lanes (a few per warp at a time) to one store.
 // kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
-template <bool kWide, bool kLightSpace, bool kOne>
+template <bool kWide, bool kLightSpace, class Src>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
-    k_trace_shadow(const TraceItem* __restrict__ items, int numItems, float4* __restrict__ shadowList,
-                   unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err,
-                   const __grid_constant__ TraceItem one) {
+    k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList,
+                   unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const long long total = (long long)counters[1];
@@ -459,7 +461,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
         const float4 rec = shadowList[k];
         id = k;
         slot = __float_as_uint(rec.w);
-        const TraceItem& T = itemOf<kOne>(items, numItems, one, (long long)(slot >> 5));
+        const TraceItem& T = src.at((long long)(slot >> 5));
         bvh = kLightSpace ? T.s.shadow : T.s.bvh;
         ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
@@ -476,12 +478,11 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
 // Shadowed rays' outputs, one thread per shadow record: the shadowed radiance k_shade parked in the hit
 // record replaces the lit one in the ray image (and the planar 16-bit copy), and the hit code gets its
 // shadow bit.
-template <bool kOne>
-__global__ void __launch_bounds__(256) k_shadow_resolve(const TraceItem* __restrict__ items, int numItems,
+template <class Src>
+__global__ void __launch_bounds__(256) k_shadow_resolve(const __grid_constant__ Src src,
                                                         const float4* __restrict__ shadowList,
                                                         const unsigned long long* __restrict__ counters,
-                                                        const float4* __restrict__ hits,
-                                                        const __grid_constant__ TraceItem one) {
+                                                        const float4* __restrict__ hits) {
   const long long total = (long long)counters[1];
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
        k += (long long)gridDim.x * blockDim.x) {
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(256) k_shadow_resolve(const TraceItem* __restr
     if (!(u & 0x80000000u)) continue;
     const uint32_t id = u & 0x7fffffffu;
     const long long warp = id >> 5;
-    const TraceItem& T = itemOf<kOne>(items, numItems, one, warp);
+    const TraceItem& T = src.at(warp);
     const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
     const float3 Ls = xyz(hits[id]);
     const size_t idx = rayIndex(T.g, rs);
@@ -788,29 +789,28 @@ long long traceWarps(const GridGPU& g, const FrameGPU& f) {
 }
 
 namespace {
-// The wavefront kernels of one trace launch; kOne: the single record `one` as a kernel parameter.
-template <bool kOne>
-void launchWavefront(const TraceItem* dItems, int numItems, long long rays, unsigned long long* dCounters,
-                     float4* dHits, float4* dShadow, int blocks, int refill, long long shadeBlocks, bool wide,
-                     bool lightSpace, uint32_t* err, cudaStream_t stream, const TraceItem& one) {
+// The wavefront kernels of one trace launch with records from `src`.
+template <class Src>
+void launchWavefront(const Src& src, long long rays, unsigned long long* dCounters, float4* dHits, float4* dShadow,
+                     int blocks, int refill, long long shadeBlocks, bool wide, bool lightSpace, uint32_t* err,
+                     cudaStream_t stream) {
   if (wide)
-    k_trace_closest<true, kOne><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits,
-                                                                      err, one);
+    k_trace_closest<true, Src><<<blocks, kTraceThreads, 0, stream>>>(src, rays, dCounters, refill, dHits, err);
   else
-    k_trace_closest<false, kOne><<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, rays, dCounters, refill, dHits,
-                                                                       err, one);
-  k_shade<kOne><<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, rays, dHits, dShadow, dCounters, one);
-  auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, kOne> : k_trace_shadow<true, false, kOne>)
-                     : (lightSpace ? k_trace_shadow<false, true, kOne> : k_trace_shadow<false, false, kOne>);
-  shadow<<<blocks, kTraceThreads, 0, stream>>>(dItems, numItems, dShadow, dCounters, refill, err, one);
-  k_shadow_resolve<kOne><<<(unsigned)shadeBlocks, 256, 0, stream>>>(dItems, numItems, dShadow, dCounters, dHits, one);
+    k_trace_closest<false, Src><<<blocks, kTraceThreads, 0, stream>>>(src, rays, dCounters, refill, dHits, err);
+  k_shade<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, rays, dHits, dShadow, dCounters);
+  auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, Src> : k_trace_shadow<true, false, Src>)
+                     : (lightSpace ? k_trace_shadow<false, true, Src> : k_trace_shadow<false, false, Src>);
+  shadow<<<blocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
+  k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters, dHits);
 }
+
 }  // namespace
 
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
-                             const TraceItem* hOne) {
+                             const TraceItem* hItems) {
   cudaError_t e = cudaMemsetAsync(dCounters, 0, kTraceCounters * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   dim3 lg((maxN + 127) / 128, numItems);
@@ -824,13 +824,15 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long shadeBlocks = (rays + 255) / 256;
   if (shadeBlocks > (long long)sms * 16) shadeBlocks = (long long)sms * 16;
-  if (hOne && numItems == 1)
-    launchWavefront<true>(dItems, numItems, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide,
-                          lightSpace, err, stream, *hOne);
-  else
-    launchWavefront<false>(dItems, numItems, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide,
-                           lightSpace, err, stream, TraceItem{});
+  if (hItems && numItems == 1) {
+    launchWavefront(ItemsOne{hItems[0]}, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide, lightSpace,
+                    err, stream);
+  } else {
+    launchWavefront(ItemsGlobal{dItems, numItems}, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide,
+                    lightSpace, err, stream);
+  }
   return cudaGetLastError();
 }
+
 
 }  // namespace ddgi
