@@ -374,8 +374,54 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
                                            / out["single_grid_tuned_fp32"]["ms_per_update"])
 
     out["precision_tc"] = measure_precision(ctx, stream)
+    out["mirror"] = measure_mirror(ctx, scene, w, stream)
     out.update(measure_batched(ctx, stream, serving=True))
     return out
+
+
+def measure_mirror(ctx, scene, w, stream):
+    """The specular GI mirror pass (ddgi_mirror_reflections) on a 1920 x 1080 G-buffer of points on the workload's
+    triangles (face normals, camera at the grid's camera, 1 in 23 sky pixels), device-resident, with the grid's
+    atlas after two updates: ms per pass and reflected rays / s."""
+    import torch
+
+    from anerend_gb300 import _lib as L
+    from anerend_gb300 import ddgi, scenes
+
+    arrays = scene.arrays
+    n = 1920 * 1080
+    v = arrays.vertices["d0"][:, :3].astype(np.float64)
+    tri = arrays.indices.reshape(-1, 3)
+    u = [scenes.uniform(17, 960 + k, n) for k in range(3)]
+    k = (u[0] * len(tri)).astype(np.int64) % len(tri)
+    a, b = u[1].copy(), u[2].copy()
+    flip = a + b > 1
+    a[flip], b[flip] = 1 - a[flip], 1 - b[flip]
+    pts = np.zeros(n, L.MIRROR_POINT)
+    pts["position"] = (v[tri[k, 0]] * (1 - a - b)[:, None] + v[tri[k, 1]] * a[:, None] + v[tri[k, 2]] * b[:, None])
+    pts["normal"] = np.cross(v[tri[k, 1]] - v[tri[k, 0]], v[tri[k, 2]] - v[tri[k, 0]])
+    pts["sky"][::23] = 1.0
+    dp = torch.from_numpy(pts.view(np.uint8).copy()).cuda()
+    out = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    g = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
+    try:
+        for f in range(2):
+            g.update(scene, ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f)), stream)
+        fp = ddgi.FrameParams(camera_pos=scenes.camera(w, 1))
+        for _ in range(3):
+            g.mirror_reflections(scene, fp, dp.data_ptr(), n, out.data_ptr(), stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 10
+        e0.record()
+        for _ in range(reps):
+            g.mirror_reflections(scene, fp, dp.data_ptr(), n, out.data_ptr(), stream)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        hit = float((out[:, 3] < 1e6).logical_and(out[:, 3] > 0).float().mean())
+    finally:
+        g.close()
+    return {"points": n, "ms": ms, "reflected_rays_per_s": n / ms * 1e3, "hit_fraction": hit}
 
 
 def measure_batched(ctx, stream, serving=True):
