@@ -2,8 +2,8 @@
 //
 // batchLaunch runs, for every (grid, scene, frame) item, the translation (host decision + copy kernel,
 // outside the captured part), then one persistent trace launch whose warps pull work from a single queue
-// spanning all items' rays (k_trace_batch), then one convolution launch over all items (tensor cores:
-// k_conv_tc over every item's tiles; FP32: k_conv_fp32_batch). The per-item records (grid, frame, scene
+// spanning all items' rays (the wavefront kernels of launchTraceBatch), then one convolution launch over
+// all items (tensor cores: k_conv_tc over every item's tiles; FP32: k_conv_fp32_batch). The per-item records (grid, frame, scene
 // views, atlas pointers) are copied from pinned host memory into device records before the launches, so the
 // launch sequence itself only depends on the batch's shape; once the same shape repeats it is captured into a
 // CUDA graph and replayed. A LaunchState owns the records, their staging and the captured graph; DdgiBatch

@@ -137,13 +137,15 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Wavefront trace of one launch (every item of a batch, or one grid): three kernels in stream order.
-//   k_trace_closest  persistent closest-hit traversal; writes one hit record per ray slot
-//   k_shade          one thread per ray slot: hit reconstruction, shading, probe lookup, outputs; appends
-//                    a shadow ray (origin + slot id) to a list for each hit
-//   k_trace_shadow   persistent any-hit traversal over the list; overwrites the radiance of shadowed rays
-// Splitting keeps each kernel small (registers, instruction cache) and lets the traversal kernels refill
-// idle lanes with new rays instead of waiting for a warp's longest ray.
+// Wavefront trace of one launch (every item of a batch, or one grid): four kernels in stream order.
+//   k_trace_closest   persistent closest-hit traversal; writes one hit record per ray slot
+//   k_shade           one thread per ray slot: hit reconstruction, shading, probe lookup, outputs; appends
+//                     a shadow ray (origin + slot id) to a list for each hit
+//   k_trace_shadow    persistent any-hit traversal over the list; flags the records of shadowed rays
+//   k_shadow_resolve  one thread per shadow record: the shadowed radiance of the flagged rays
+// Splitting keeps each kernel small (registers, instruction cache), lets the traversal kernels refill
+// idle lanes with new rays instead of waiting for a warp's longest ray, and keeps scattered per-ray output
+// writes out of the traversal loops.
 //
 // Ray slots: item i owns slots [32 warpBegin_i, 32 (warpBegin_i + traceWarps_i)); slot 32 w + l of an item
 // is lane l of its warp w. Warp w traces D = 32 / warpProbes directions, consecutive in the grid's ray
