@@ -154,6 +154,9 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 #ifndef DDGI_TRACE_MIN_BLOCKS
 #define DDGI_TRACE_MIN_BLOCKS 8
 #endif
+// The light-space shadow traversal (exact +z box test) fits 48 registers: 10 resident blocks per SM, and
+// its launch scales the traversal grid by 10 / 8 (measured 1 % faster per probe update than 8 blocks).
+constexpr int kShadowLightBlocks = 10;
 
 struct RaySlot {
   int px, pz, layer, j;
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
 // writes out of this kernel keeps its finishing lanes (a few per warp at a time) to one store.
 // kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
 template <bool kWide, bool kLightSpace, class Src>
-__global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlocks : DDGI_TRACE_MIN_BLOCKS)
     k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList,
                    unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
@@ -803,7 +806,8 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
   k_shade<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, rays, dHits, dShadow, dCounters);
   auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, Src> : k_trace_shadow<true, false, Src>)
                      : (lightSpace ? k_trace_shadow<false, true, Src> : k_trace_shadow<false, false, Src>);
-  shadow<<<blocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
+  const int shadowBlocks = lightSpace ? blocks * kShadowLightBlocks / DDGI_TRACE_MIN_BLOCKS : blocks;
+  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
   k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters, dHits);
 }
 
