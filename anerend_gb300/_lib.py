@@ -110,7 +110,7 @@ class BatchStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memoryBudget", C.c_uint64), ("maxBatch", C.c_int32), ("inFlight", C.c_int32),
-                ("convMode", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("convMode", C.c_int32), ("maxBatchMRays", C.c_uint32), ("reserved", C.c_int32 * 4)]
 
 
 class Request(C.Structure):

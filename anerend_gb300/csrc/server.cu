@@ -27,6 +27,7 @@ struct Req {
   DdgiRequest r{};
   DdgiGrid* grid = nullptr;
   uint64_t bytes = 0;
+  uint64_t rays = 0;  // probes x rays per probe (all layers)
   int state = DDGI_REQUEST_QUEUED;
   int error = DDGI_OK;
   double tSubmit = 0, tAdmit = 0, tDone = 0;
@@ -105,10 +106,13 @@ void workerLoop(DdgiServer* s) {
     for (Slot& sl : s->slots)
       if (!sl.busy) { free = &sl; break; }
     std::vector<Req*> batch;
+    uint64_t batchRays = 0;
+    const uint64_t rayCap = (uint64_t)s->cfg.maxBatchMRays * 1000000ull;
     if (free) {
       while (!s->pending.empty() && (int)batch.size() < s->cfg.maxBatch) {
         Req* r = s->pending.front();
         if (s->usedBytes + r->bytes > s->cfg.memoryBudget) break;  // head of line waits for memory
+        if (rayCap && !batch.empty() && batchRays + r->rays > rayCap) break;  // the next launch takes it
         s->pending.pop_front();
         int rc = gridCreate(s->ctx, &r->r.grid, free->stream, true, &r->grid);
         if (!rc) rc = tuneGridForBatch(r->grid, s->tuning);
@@ -122,6 +126,7 @@ void workerLoop(DdgiServer* s) {
           continue;
         }
         s->usedBytes += r->bytes;
+        batchRays += r->rays;
         s->peakBytes = std::max(s->peakBytes, s->usedBytes);
         r->state = DDGI_REQUEST_RUNNING;
         r->tAdmit = s->now();
@@ -248,6 +253,7 @@ int ddgi_server_submit(DdgiServer* s, const DdgiRequest* req, uint64_t* id) {
   if (!r) return fail(ctx, DDGI_ENOMEM, "host allocation");
   r->r = *req;
   r->bytes = gridFootprint(&req->grid, s->tuning.convMode);
+  r->rays = (uint64_t)req->grid.dims[0] * req->grid.dims[1] * req->grid.dims[2] * (uint64_t)req->grid.raysPerProbe;
   std::lock_guard<std::mutex> lk(s->mu);
   r->id = s->nextId++;
   r->tSubmit = s->now();

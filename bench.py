@@ -480,12 +480,13 @@ def measure_batched(ctx, stream, serving=True):
         ctx.sync(stream)
         return out
 
-    # serving: Poisson arrivals over the 8 resident scenes above, at the workload's 2,000 req/s and at 200 req/s
+    # serving: Poisson arrivals over the 8 resident scenes above, at the workload's 2,000 req/s and at 1,000, 500
+    # and 200 req/s (where the p99 latency crosses one 30 Hz update period)
     sw = scenes.SERVING
     serv = {"scenes": len(scs), "note": "resident scenes of the batched workload (8, 17k..495k triangles)"}
-    for rate, dur in ((2000.0, 1.5), (200.0, 2.0)):
+    for rate, dur in ((2000.0, 1.5), (1000.0, 1.5), (500.0, 2.0), (200.0, 2.0)):
         reqs = scenes.serving_requests(sw, int(rate * dur), rate)
-        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=2)
+        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=2, max_batch_mrays=8)
         t0 = time.perf_counter()
         for (ta, si, dms, rr, cam, k) in reqs:
             now = time.perf_counter() - t0

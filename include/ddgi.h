@@ -394,7 +394,10 @@ typedef struct DdgiServerConfig {
   int32_t  maxBatch;      /* requests per launch (1..64) */
   int32_t  inFlight;      /* launches running at once, each on its own stream (1..4) */
   int32_t  convMode;      /* DdgiTuning.convMode of the served grids */
-  int32_t  reserved[5];
+  uint32_t maxBatchMRays; /* rays per launch, in millions, admitted at most (a request larger than that runs
+                             alone); 0: no limit. Short launches free their slot sooner, so later arrivals
+                             wait less behind large ones */
+  int32_t  reserved[4];
 } DdgiServerConfig;
 
 /* One probe update of a grid of its own over a resident scene. The grid starts cleared, is translated,

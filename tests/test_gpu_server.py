@@ -90,3 +90,35 @@ def test_budget_admission_and_rejection(ctx):
     finally:
         for s in scs:
             s.close()
+
+
+def test_ray_cap_splits_launches(ctx):
+    """maxBatchMRays: a launch admits requests while their rays stay within the cap (a larger request runs
+    alone); the atlases are the same as without the cap."""
+    scs = _scenes(ctx)
+    d = ddgi.grid_desc((16, 4, 16), rays_per_probe=512)  # 524,288 rays: two exceed 1 million
+    frames = [ddgi.FrameParams(camera_pos=(0.2 * k, 1.0, 0.1), rotation=scenes.rotation(k, 2)) for k in range(6)]
+
+    def run(cap):
+        srv = ddgi.Server(ctx, 8 << 30, max_batch=64, in_flight=1, conv_mode=0, max_batch_mrays=cap)
+        outs = [torch.empty(10 * 16 * 10 * 16 * 4 * 4, dtype=torch.float32).pin_memory() for _ in frames]
+        try:
+            for k, fp in enumerate(frames):
+                srv.submit(scs[k % 2], d, fp, outs[k].data_ptr(), tag=k)
+            srv.drain(120.0)
+            st = srv.stats
+            assert st.completed == len(frames) and st.failed == 0
+            ctx.sync()
+            return [o.numpy().copy() for o in outs], st
+        finally:
+            srv.close()
+
+    try:
+        free, _ = run(0)
+        capped, st = run(1)
+        assert st.batches == len(frames)  # one request per launch
+        for k, (a, b) in enumerate(zip(free, capped)):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
+    finally:
+        for s in scs:
+            s.close()
