@@ -399,7 +399,6 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         } else {
           so = pos;
         }
-        cast = true;
         // lit: L = calcLight; shadowed: L = 0; then += indirect, += emissive (rchit:195-214)
         L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, pos, origin, f.lightDir, f.sunIntensity);
         float3 Ls = f3(0.f, 0.f, 0.f);
@@ -410,6 +409,11 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         }
         L += h.emissive;
         Ls += h.emissive;
+        // The shadow ray only picks between L and Ls. When they have the same bits (a surface facing away
+        // from the sun, N.L <= 0, makes calcLight exactly 0) its outcome cannot change the radiance, so it
+        // is cast only when the values differ or the caller records per-ray hit codes (their shadow bit).
+        cast = T.rayHit != nullptr || __float_as_uint(L.x) != __float_as_uint(Ls.x) ||
+               __float_as_uint(L.y) != __float_as_uint(Ls.y) || __float_as_uint(L.z) != __float_as_uint(Ls.z);
         hits[id] = make_float4(Ls.x, Ls.y, Ls.z, 0.f);
         hitCode = __float_as_int(r0.w) * 2;
       }
@@ -710,7 +714,11 @@ __global__ void __launch_bounds__(256) k_mirror_shade(SceneGPU s, GridGPU g, Fra
         Ls += h.emissive;
         lit = make_float4(L.x, L.y, L.z, dist);
         dark = make_float4(Ls.x, Ls.y, Ls.z, dist);
-        sp = make_float4(h.pos.x, h.pos.y, h.pos.z, 0.f);
+        // no shadow ray when it cannot change the result: lit and shadowed radiance with the same bits
+        // (calcLight exactly 0 on a surface facing away from the sun)
+        const bool same = __float_as_uint(L.x) == __float_as_uint(Ls.x) && __float_as_uint(L.y) == __float_as_uint(Ls.y) &&
+                          __float_as_uint(L.z) == __float_as_uint(Ls.z);
+        sp = make_float4(h.pos.x, h.pos.y, h.pos.z, same ? 1.f : 0.f);
       }
     }
     out[i] = lit;

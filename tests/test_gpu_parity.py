@@ -407,3 +407,31 @@ def test_bvh_width_is_validated(ctx):
             grid.set_tuning(bvh_width=4)
     finally:
         grid.close()
+
+
+@pytest.mark.parametrize("shadow_mode", [0, 1])
+def test_skipped_shadow_rays_leave_radiance_unchanged(ctx, shadow_mode):
+    """A trace without per-ray hit codes casts no shadow ray for a hit whose lit and shadowed radiance have
+    the same bits (calcLight is exactly 0 on a surface facing away from the sun); a recorded trace casts all
+    of them. Ray radiance and atlas must stay bit-identical between the two over several multi-bounce frames
+    of the 4096-triangle workload."""
+    w = scenes.CPU_REFERENCE
+    scene = ddgi.Scene(ctx, scenes.build_scene(w))
+    grids = [ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=o)
+             for o in (0, L.DDGI_GRID_RECORD_HITS)]
+    try:
+        for g in grids:
+            g.set_tuning(shadow_mode=shadow_mode)
+        for f in range(4):
+            fp = ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f))
+            for g in grids:
+                g.update(scene, fp)
+            ctx.sync()
+            (rad0, _, _), (rad1, hits, _) = grids[0].download_rays(), grids[1].download_rays(hits=True)
+            assert np.array_equal(rad0.view(np.uint32), rad1.view(np.uint32)), f
+            assert np.array_equal(grids[0].download_atlas().view(np.uint32), grids[1].download_atlas().view(np.uint32))
+        assert (hits >= 0).mean() > 0.3  # the frames hit geometry (about half of it facing away from the sun)
+    finally:
+        for g in grids:
+            g.close()
+        scene.close()
