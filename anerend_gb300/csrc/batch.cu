@@ -3,7 +3,7 @@
 // batchLaunch runs, for every (grid, scene, frame) item, the translation (host decision + copy kernel,
 // outside the captured part), then one persistent trace launch whose warps pull work from a single queue
 // spanning all items' rays (the wavefront kernels of launchTraceBatch), then one convolution launch over
-// all items (tensor cores: k_conv_tc over every item's tiles; FP32: k_conv_fp32_batch). The per-item records (grid, frame, scene
+// all items (tensor cores: k_conv_tc over every item's 64-probe units; FP32: k_conv_fp32_batch). The per-item records (grid, frame, scene
 // views, atlas pointers) are copied from pinned host memory into device records before the launches, so the
 // launch sequence itself only depends on the batch's shape; once the same shape repeats it is captured into a
 // CUDA graph and replayed. A LaunchState owns the records, their staging and the captured graph; DdgiBatch
@@ -115,7 +115,7 @@ namespace {
 
 // Records the launch sequence on `st` (eagerly or under capture).
 int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long totalWarps, long long totalGroups,
-          int totalTiles, cudaStream_t st) {
+          int totalUnits, cudaStream_t st) {
   DdgiContext* ctx = S->ctx;
   int blocks = ctx->numSms * t.blocksPerSm;
   CK(launchTraceBatch(S->dTrace(), S->dRots(), n, maxN, totalWarps, S->dQueue, S->dHits, S->dShadow, blocks,
@@ -123,7 +123,7 @@ int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long t
      "batched trace");
   if (t.convMode != 0) {
     int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
-    CK(launchConvTcItems(fmt, S->tcHost.data(), S->dTc(), n, totalTiles, ctx->dErr, st),
+    CK(launchConvTcItems(fmt, S->tcHost.data(), S->dTc(), n, totalUnits, ctx->dErr, st),
        "batched tensor-core convolve");
   } else {
     CK(launchConvFp32Batch(S->dConv(), n, totalGroups, st), "batched convolve");
@@ -144,7 +144,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
   const int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
   if (tc && (int)S->tcHost.size() < n) S->tcHost.resize(n);
   long long warps = 0, groups = 0, rays = 0;
-  int tiles = 0, maxN = 0, moved = 0;
+  int units = 0, maxN = 0, moved = 0;
   int slot = 0;
   unsigned char* rec = S->ring.acquire(&slot);
   TraceItem* hTrace = reinterpret_cast<TraceItem*>(rec);
@@ -201,10 +201,10 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     if (tc) {
       TcItemHost& h = S->tcHost[i];
       if (!tcPrepareItem(g->g, fmt, g->rad16, gg.pTotal, g->lattice, g->tcScratch, g->atlas[g->cur], lb, le,
-                         g->desc.hysteresis, fr.flags, tiles, &h))
+                         g->desc.hysteresis, fr.flags, units, &h))
         return fail(ctx, DDGI_EINVAL, "tensor-core item %d could not be prepared", i);
       memcpy(hTc + 128 * (size_t)i, h.item, 128);
-      tiles += h.tiles;
+      units += h.units;
     } else {
       ConvItem& ci = hConv[i];
       ci.g = g->g;
@@ -233,13 +233,13 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     stats->translations = (uint32_t)moved;
   }
   // the captured sequence depends only on these (per-item values live in the device records)
-  S->shape = {n, maxN, warps, groups, tiles, t.convMode, t.blocksPerSm, t.refillLanes, t.bvhWidth};
+  S->shape = {n, maxN, warps, groups, units, t.convMode, t.blocksPerSm, t.refillLanes, t.bvhWidth};
   const bool stable = allowGraph && t.useGraph && S->shape == S->lastShape;
   if (stable && !S->exec) {
     cudaGraph_t graph = nullptr;
     cudaStream_t cs = S->captureStream;
     CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
-    rc = issue(S, t, n, maxN, warps, groups, tiles, cs);
+    rc = issue(S, t, n, maxN, warps, groups, units, cs);
     cudaError_t ce = cudaStreamEndCapture(cs, &graph);
     if (rc) {
       if (graph) cudaGraphDestroy(graph);
@@ -258,7 +258,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     if (stats) stats->graphLaunches++;
   } else {
     if (S->exec) S->dropGraph();
-    rc = issue(S, t, n, maxN, warps, groups, tiles, st);
+    rc = issue(S, t, n, maxN, warps, groups, units, st);
     if (rc) return rc;
     if (stats) stats->eagerLaunches++;
   }

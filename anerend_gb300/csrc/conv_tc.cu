@@ -3,13 +3,18 @@
 // All probes of a dispatch share the N ray directions, so the convolution of channel c is the product
 //   D_c[probe][texel] = sum_j R_c[probe][j] * W[texel][j],   W[t][j] = max(0, d_j . omega_t) (0 if <= 1e-6)
 // with R_c the 16-bit (FP16 or BF16) radiance of channel c, stored planar: row c * P + p, N rays per row.
-// One CTA per SM walks tiles of 128 probes. Per tile and 64-ray K-chunk a TMA producer warp loads the three
-// 128 x 64 radiance tiles and the 64 x 64 weight tile (SWIZZLE_128B); one thread of the MMA warp issues
-// 4 K-steps x 3 channels of tcgen05.mma (M = 128 probes, N = 64 texels, K = 16) into FP32 accumulators in
-// TMEM (3 x 64 columns, double-buffered = 384 of 512 columns). Eight epilogue warps read the accumulators with
-// tcgen05.ld (thread = probe), stage them in shared memory and walk the atlas coalesced (lanes = 4 probes x
-// 8 texels of a row), normalising by the texel's weight sum and applying the hysteresis blend (or the bake
-// accumulation) in FP32 against the old atlas texel.
+// The probes of every item are cut into units of 64; each CTA (one per SM) takes an equal contiguous run of
+// the launch's units and walks it in tiles of two units (128 probes), or one at the end of its run or of an
+// item, so no SM carries more than one unit above the average. Per tile and 64-ray K-chunk a TMA producer
+// warp loads the three radiance tiles (64-row boxes, one or two per channel) and the 64 x 64 weight tile
+// (SWIZZLE_128B); one thread of the MMA warp issues 4 K-steps x 3 channels of tcgen05.mma (M = 128 probe
+// rows, N = 64 texels, K = 16) into FP32 accumulators in TMEM (3 x 64 columns, double-buffered = 384 of 512
+// columns); the rows of a one-unit tile past its 64 probes hold stale operands and are never read. Eight
+// epilogue warps read the accumulators with tcgen05.ld (thread = probe), stage them in shared memory and walk
+// the atlas coalesced (lanes = 4 probes x 8 texels of a row), normalising by the texel's weight sum and
+// applying the hysteresis blend (or the bake accumulation) in FP32 against the old atlas texel.
+// A single-item launch carries its record and tensor maps in the kernel parameters (TcOne); a batch reads
+// its records from device memory (TcMany), so a captured launch sees per-frame values written between replays.
 //
 // Every mbarrier wait is bounded: on timeout the kernel raises DDGI_DEVERR_TIMEOUT, stops issuing work,
 // waits (bounded) for its own TMA loads and MMAs in flight, frees its TMEM and returns.
@@ -27,10 +32,12 @@ namespace ddgi {
 
 namespace {
 
-constexpr int kTileP = 128;                  // probes per tile (MMA M)
+constexpr int kTileP = 128;                  // probe rows per tile (MMA M)
+constexpr int kUnitP = 64;                   // probes per work unit (one TMA box of radiance rows)
 constexpr int kChunkK = 64;                  // rays per K-chunk (128 bytes of 16-bit values)
 constexpr int kStages = 3;  // 3 x 56 KB of operand staging
 constexpr int kATileBytes = kTileP * kChunkK * 2;   // 16 KB per channel
+constexpr int kAUnitBytes = kUnitP * kChunkK * 2;   // 8 KB: one unit's rows of one channel
 constexpr int kWTileBytes = kOctTexels * kChunkK * 2;  // 8 KB
 constexpr int kStageBytes = 3 * kATileBytes + kWTileBytes;  // 56 KB
 constexpr int kTmemCols = 512;
@@ -70,6 +77,12 @@ DDGI_D bool mbarWait(uint64_t* bar, uint32_t parity) {
   }
   return false;
 }
+
+// Programmatic dependent launch: the convolution is launched while the weights kernel before it still runs
+// (its prologue and its first radiance loads overlap that kernel); it waits for the weights kernel's results
+// here before reading them. Without the launch attribute the wait returns at once.
+DDGI_D void gridDependencyWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+DDGI_D void gridDependentsMayLaunch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 DDGI_D void tmaLoad2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
   asm volatile(
@@ -136,14 +149,15 @@ __host__ __device__ constexpr uint32_t instrDesc(uint32_t fmt) {
 
 constexpr int kMaxTcItems = 64;
 
-// Per-grid record of a (batched) tensor-core convolution, in device memory so that per-frame values (atlas
-// after a translation, layer range, flags) can change between replays of a captured launch.
+// Per-grid record of a (batched) tensor-core convolution. A batch keeps the records in device memory so that
+// per-frame values (atlas after a translation, layer range, flags) can change between replays of a captured
+// launch; a single-item launch passes its record by value.
 struct TcItem {
   int X, atlasW, atlasFmt;
   int pBegin, pEnd;       // probe range (linear over the grid, layer-major)
   int pTotal;             // rows per channel of the radiance matrix
   int numChunks;          // N / 64
-  int tileBegin;          // first batch tile of this item
+  int unitBegin;          // first 64-probe unit of this item in the launch
   float hysteresis;
   uint32_t flags;
   void* atlas;
@@ -154,7 +168,9 @@ struct TcItem {
   int n;
 };
 
-// Tensor maps of every item (radiance R, weights W); static for a batch, passed as a kernel parameter.
+DDGI_HD int tcUnits(const TcItem& it) { return (it.pEnd - it.pBegin + kUnitP - 1) / kUnitP; }
+
+// Tensor maps of every item (radiance R with 64-row boxes, weights W); static for a batch.
 struct TcMaps {
   CUtensorMap r[kMaxTcItems];
   CUtensorMap w[kMaxTcItems];
@@ -168,19 +184,58 @@ DDGI_HD const TcItem& tcItem(const unsigned char* recs, int i) {
   return *reinterpret_cast<const TcItem*>(recs + (size_t)i * kTcItemStride);
 }
 
-DDGI_D int tcItemOf(const unsigned char* items, int numItems, int tile) {
-  int lo = 0, hi = numItems - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (tcItem(items, mid).tileBegin <= tile) lo = mid; else hi = mid - 1;
+// Where the kernels' records and tensor maps come from (passed by value, __grid_constant__).
+struct TcOne {
+  CUtensorMap r, w;
+  TcItem it;
+  DDGI_D int numItems() const { return 1; }
+  DDGI_D int itemOfUnit(int) const { return 0; }
+  DDGI_D const TcItem& item(int) const { return it; }
+  DDGI_D const CUtensorMap* mapR(int) const { return &r; }
+  DDGI_D const CUtensorMap* mapW(int) const { return &w; }
+};
+struct TcMany {
+  TcMaps maps;
+  const unsigned char* items;
+  int n;
+  DDGI_D int numItems() const { return n; }
+  DDGI_D int itemOfUnit(int unit) const {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (tcItem(items, mid).unitBegin <= unit) lo = mid; else hi = mid - 1;
+    }
+    return lo;
   }
-  return lo;
+  DDGI_D const TcItem& item(int i) const { return tcItem(items, i); }
+  DDGI_D const CUtensorMap* mapR(int i) const { return &maps.r[i]; }
+  DDGI_D const CUtensorMap* mapW(int i) const { return &maps.w[i]; }
+};
+
+// A CTA's run of units, walked in tiles of at most two units that do not cross an item boundary. Every warp
+// role walks the same sequence.
+struct TcTile {
+  int item, p0, units;
+};
+template <class Src>
+DDGI_D bool nextTile(const Src& src, int& unit, int unitEnd, TcTile& t) {
+  if (unit >= unitEnd) return false;
+  const int ii = src.itemOfUnit(unit);
+  const TcItem& it = src.item(ii);
+  const int local = unit - it.unitBegin;
+  int n = tcUnits(it) - local;
+  if (n > 2) n = 2;
+  if (n > unitEnd - unit) n = unitEnd - unit;
+  t.item = ii;
+  t.p0 = it.pBegin + local * kUnitP;
+  t.units = n;
+  unit += n;
+  return true;
 }
 
-template <int kFmt>
+template <int kFmt, class Src>
 __global__ void __launch_bounds__(kThreadsTc, 1)
-    k_conv_tc(const __grid_constant__ TcMaps maps, const unsigned char* __restrict__ items, int numItems, int totalTiles,
-              uint32_t* __restrict__ err) {
+    k_conv_tc(const __grid_constant__ Src src, int totalUnits, uint32_t* __restrict__ err) {
   extern __shared__ uint8_t smemRaw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smemRaw + 1023) & ~(uintptr_t)1023);
   __shared__ uint64_t fullBar[kStages], emptyBar[kStages], accFull[2], accEmpty[2], drainBar;
@@ -188,7 +243,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   __shared__ int abortFlag;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles = totalTiles;
+  // this CTA's units: an equal share of the launch's, contiguous
+  const int unitBegin = (int)((long long)blockIdx.x * totalUnits / gridDim.x);
+  const int unitEnd = (int)((long long)(blockIdx.x + 1) * totalUnits / gridDim.x);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) { mbarInit(&fullBar[s], 1); mbarInit(&emptyBar[s], 1); }
@@ -209,29 +266,41 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   };
   auto aborted = [&]() { return *(volatile int*)&abortFlag != 0; };
 
+  TcTile tile;
+  int unit = unitBegin;
   if (warp == 0) {
     // ---- TMA producer ----
     if (lane == 0) {
       bool pending[kStages] = {};
       uint32_t pendingParity[kStages] = {};
+      bool weightsReady = false;
       int s = 0;
       uint32_t phase = 0;
-      for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x) {
-        const int ii = tcItemOf(items, numItems, t);
-        const TcItem& it = tcItem(items, ii);
-        const int p0 = it.pBegin + (t - it.tileBegin) * kTileP;
+      while (!aborted() && nextTile(src, unit, unitEnd, tile)) {
+        const TcItem& it = src.item(tile.item);
+        const CUtensorMap* mr = src.mapR(tile.item);
+        const CUtensorMap* mw = src.mapW(tile.item);
+        const uint32_t bytes = (uint32_t)(3 * tile.units * kAUnitBytes + kWTileBytes);
+        bool ok = true;
         for (int kc = 0; kc < it.numChunks; ++kc) {
-          if (!mbarWait(&emptyBar[s], phase ^ 1)) { fail(); break; }
+          if (!mbarWait(&emptyBar[s], phase ^ 1)) { fail(); ok = false; break; }
           pending[s] = false;
           uint8_t* st = smem + (size_t)s * kStageBytes;
-          mbarExpectTx(&fullBar[s], kStageBytes);
+          mbarExpectTx(&fullBar[s], bytes);
           for (int c = 0; c < 3; ++c)
-            tmaLoad2d(st + c * kATileBytes, &maps.r[ii], &fullBar[s], kc * kChunkK, c * it.pTotal + p0);
-          tmaLoad2d(st + 3 * kATileBytes, &maps.w[ii], &fullBar[s], kc * kChunkK, 0);
+            for (int u = 0; u < tile.units; ++u)
+              tmaLoad2d(st + c * kATileBytes + u * kAUnitBytes, mr, &fullBar[s], kc * kChunkK,
+                        c * it.pTotal + tile.p0 + u * kUnitP);
+          if (!weightsReady) {  // the weights come from the kernel launched just before this one
+            gridDependencyWait();
+            weightsReady = true;
+          }
+          tmaLoad2d(st + 3 * kATileBytes, mw, &fullBar[s], kc * kChunkK, 0);
           pending[s] = true;
           pendingParity[s] = phase;
           if (++s == kStages) { s = 0; phase ^= 1; }
         }
+        if (!ok) break;
       }
       if (aborted()) {  // let loads in flight land before the CTA exits
         for (int k = 0; k < kStages; ++k)
@@ -246,8 +315,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       uint32_t phase = 0;
       int local = 0;
       bool issued = false;
-      for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
-        const int numChunks = tcItem(items, tcItemOf(items, numItems, t)).numChunks;
+      for (; !aborted() && nextTile(src, unit, unitEnd, tile); ++local) {
+        const int numChunks = src.item(tile.item).numChunks;
         int b = local & 1;
         uint32_t accPhase = (local >> 1) & 1;
         if (!mbarWait(&accEmpty[b], accPhase ^ 1)) { fail(); break; }
@@ -285,34 +354,47 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     // split the four blocks of 16 texels between them. Per block (two texel rows)
     // it reads its rows' accumulators (thread = probe), stages them in shared memory and then walks the
     // atlas coalesced: per step its lanes cover 4 probes x the 8 texels of one row (4 runs of 128 bytes).
-    // The old texels do not depend on the MMA, so their loads are issued before the accumulator wait.
+    // The old texels do not depend on the MMA, so their loads are issued before the accumulator wait. A warp
+    // whose rows lie past the tile's probes still waits for the accumulators before it releases them, so its
+    // arrivals on accEmpty stay in the phase of their tile.
+    gridDependencyWait();  // the weight sums come from the kernel launched just before this one
     const int quarter = warp & 3;  // TMEM lane quarter this warp may access
     const int half = (warp - 2) >> 2;  // which two texel blocks
     float* stage = reinterpret_cast<float*>(smem + (size_t)kStages * kStageBytes) + (warp - 2) * kStageWarpFloats;
     const int tx = lane & 7, pp = lane >> 3;
     int local = 0;
-    for (int t = blockIdx.x; t < tiles && !aborted(); t += gridDim.x, ++local) {
-      const TcItem& it = tcItem(items, tcItemOf(items, numItems, t));
+    for (; !aborted() && nextTile(src, unit, unitEnd, tile); ++local) {
+      const TcItem& it = src.item(tile.item);
       const bool bake = (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
       const float h = it.hysteresis, a = 1.0f - h;
       const int b = local & 1;
       const uint32_t accPhase = (local >> 1) & 1;
+      const int tileEnd = min(it.pEnd, tile.p0 + tile.units * kUnitP);
       // atlas offsets of the 8 probes this lane visits (probe 4g + pp of the warp's 32), texel (tx, 0)
-      const int warpProbe0 = it.pBegin + (t - it.tileBegin) * kTileP + quarter * 32;
+      const int warpProbe0 = tile.p0 + quarter * 32;
       size_t base[8];
       uint32_t liveMask = 0;
 #pragma unroll
       for (int g = 0; g < 8; ++g) {
         const int probe = warpProbe0 + 4 * g + pp;
-        const bool live = probe < it.pEnd;
+        const bool live = probe < tileEnd;
         const int px = live ? probe % it.X : 0, pzAll = live ? probe / it.X : 0;  // pzAll = layer * Z + z
         base[g] = (size_t)(kProbePix * pzAll + 1) * it.atlasW + (kProbePix * px + 1 + tx);
         liveMask |= (live ? 1u : 0u) << g;
       }
+      const bool rowsLive = warpProbe0 < tileEnd;  // warp-uniform
       const uint32_t laneAddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 3 * kOctTexels);
       bool ok = true;
+      if (!rowsLive) {
+        // warp-uniform outcome
+        if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase))) {
+          if (lane == 0) fail();
+          break;
+        }
+        tcFenceAfter();
+      }
 #pragma unroll 1
-      for (int blk = 2 * half; blk < 2 * half + 2; ++blk) {
+      for (int blk = 2 * half; rowsLive && blk < 2 * half + 2; ++blk) {
         // step k: probe group k >> 1, texel row ty = 2 blk + (k & 1)
         float4 olds[16];
 #pragma unroll
@@ -378,13 +460,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   if (warp == 1) tmemDealloc(tmem, kTmemCols);
 }
 
-// W[t][j] in 16-bit (rows = texels, K-major), the sums of the rounded weights and of the FP32 weights.
 // W[t][j] in 16-bit (rows = texels, K-major), the sums of the rounded weights and of the FP32 weights;
-// one block per (texel, item), threads over the rays.
+// one block per (texel, item), threads over the rays. Records from `items` in device memory, or `one` when
+// items is null.
 template <int kFmt>
-__global__ void __launch_bounds__(256) k_tc_weights(const unsigned char* __restrict__ items) {
+__global__ void __launch_bounds__(256) k_tc_weights(const unsigned char* __restrict__ items,
+                                                    const __grid_constant__ TcItem one) {
   __shared__ float r16[256], r32[256];
-  const TcItem& it = tcItem(items, blockIdx.y);
+  gridDependentsMayLaunch();
+  const TcItem& it = items ? tcItem(items, blockIdx.y) : one;
   const int n = it.n;
   int t = blockIdx.x;
   float3 omega = texelDirection(t % kOct, t / kOct);
@@ -489,7 +573,7 @@ int tcMaxItems() { return kMaxTcItems; }
 
 // Fills the item record and its two tensor maps for one grid; scratch = tcScratchBytes(N) bytes.
 bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs, void* scratch,
-                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int tileBegin,
+                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int unitBegin,
                    TcItemHost* out) {
   if (g.N % kChunkK) return false;
   TcItem& it = *reinterpret_cast<TcItem*>(out->item);
@@ -501,7 +585,7 @@ bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal,
   it.pEnd = layerEnd * g.X * g.Z;
   it.pTotal = pTotal;
   it.numChunks = g.N / kChunkK;
-  it.tileBegin = tileBegin;
+  it.unitBegin = unitBegin;
   it.hysteresis = hysteresis;
   it.flags = flags;
   it.atlas = atlas;
@@ -510,57 +594,86 @@ bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal,
   it.wsum16 = (float*)((uint8_t*)scratch + (size_t)kOctTexels * g.N * 2);
   it.wsum32 = it.wsum16 + kOctTexels;
   it.n = g.N;
-  out->tiles = (it.pEnd - it.pBegin + kTileP - 1) / kTileP;
-  if (!makeMap(reinterpret_cast<CUtensorMap*>(out->mapR), elemFmt, rad16, (uint64_t)3 * pTotal, (uint64_t)g.N, kTileP))
+  out->units = tcUnits(it);
+  if (!makeMap(reinterpret_cast<CUtensorMap*>(out->mapR), elemFmt, rad16, (uint64_t)3 * pTotal, (uint64_t)g.N, kUnitP))
     return false;
   if (!makeMap(reinterpret_cast<CUtensorMap*>(out->mapW), elemFmt, it.w16, kOctTexels, (uint64_t)g.N, kOctTexels))
     return false;
   return true;
 }
 
-// Weights of every item, then the tensor-core convolution of all items' tiles in one launch.
-// dItems: numItems TcItem records in device memory (copied from the TcItemHost.item bytes).
-cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
-                              int totalTiles, uint32_t* err, cudaStream_t stream) {
-  if (numItems <= 0 || totalTiles <= 0) return cudaSuccess;
-  if (numItems > kMaxTcItems) return cudaErrorInvalidValue;
-  const unsigned char* items = (const unsigned char*)dItems;
-  dim3 wg(kOctTexels, numItems);
-  if (elemFmt == 0) k_tc_weights<0><<<wg, 256, 0, stream>>>(items);
-  else k_tc_weights<1><<<wg, 256, 0, stream>>>(items);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  static TcMaps maps;  // host staging of the kernel parameter (copied at launch)
-  static std::mutex mapsMu;
-  std::lock_guard<std::mutex> lk(mapsMu);
-  for (int i = 0; i < numItems; ++i) {
-    memcpy(&maps.r[i], hostItems[i].mapR, sizeof(CUtensorMap));
-    memcpy(&maps.w[i], hostItems[i].mapW, sizeof(CUtensorMap));
-  }
-  size_t smem = kSmemTc;
-  auto kern = elemFmt == 0 ? k_conv_tc<0> : k_conv_tc<1>;
-  // per-process, per-device launch setup (the attribute is a property of the function on each device)
+namespace {
+
+// Per-process, per-device launch set-up of a k_conv_tc instance (the shared-memory attribute is a property
+// of the function on each device); returns the device's SM count in *sms.
+template <class Kern>
+cudaError_t tcLaunchSetup(Kern kern, int slot, int* sms) {
   static std::mutex mu;
-  static int sms[64] = {};
-  static bool attrSet[64][2] = {};
+  static int smCount[64] = {};
+  static bool attrSet[64][4] = {};
   int dev = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  {
-    std::lock_guard<std::mutex> lk2(mu);
-    if (!attrSet[dev][elemFmt]) {
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-      attrSet[dev][elemFmt] = true;
-    }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!attrSet[dev][slot]) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&smCount[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    attrSet[dev][slot] = true;
   }
-  int grid = totalTiles < sms[dev] ? totalTiles : sms[dev];
-  kern<<<grid, kThreadsTc, smem, stream>>>(maps, items, numItems, totalTiles, err);
-  return cudaGetLastError();
+  *sms = smCount[dev];
+  return cudaSuccess;
 }
 
-// One grid: the item record lives at the end of the scratch buffer.
+template <int kFmt, class Src>
+cudaError_t launchTc(const Src& src, int slot, int totalUnits, uint32_t* err, cudaStream_t stream) {
+  int sms = 0;
+  cudaError_t e = tcLaunchSetup(k_conv_tc<kFmt, Src>, slot, &sms);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(totalUnits < sms ? totalUnits : sms);
+  cfg.blockDim = dim3(kThreadsTc);
+  cfg.dynamicSmemBytes = kSmemTc;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_conv_tc<kFmt, Src>, src, totalUnits, err);
+}
+
+}  // namespace
+
+// Weights of every item, then the tensor-core convolution of all items' units in one launch.
+// dItems: numItems TcItem records in device memory (copied from the TcItemHost.item bytes).
+cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
+                              int totalUnits, uint32_t* err, cudaStream_t stream) {
+  if (numItems <= 0 || totalUnits <= 0) return cudaSuccess;
+  if (numItems > kMaxTcItems) return cudaErrorInvalidValue;
+  const unsigned char* items = (const unsigned char*)dItems;
+  TcItem none;
+  memset(&none, 0, sizeof none);
+  dim3 wg(kOctTexels, numItems);
+  if (elemFmt == 0) k_tc_weights<0><<<wg, 256, 0, stream>>>(items, none);
+  else k_tc_weights<1><<<wg, 256, 0, stream>>>(items, none);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  static TcMany src;  // host staging of the kernel parameter (copied at launch)
+  static std::mutex srcMu;
+  std::lock_guard<std::mutex> lk(srcMu);
+  for (int i = 0; i < numItems; ++i) {
+    memcpy(&src.maps.r[i], hostItems[i].mapR, sizeof(CUtensorMap));
+    memcpy(&src.maps.w[i], hostItems[i].mapW, sizeof(CUtensorMap));
+  }
+  src.items = items;
+  src.n = numItems;
+  return elemFmt == 0 ? launchTc<0>(src, 0, totalUnits, err, stream) : launchTc<1>(src, 1, totalUnits, err, stream);
+}
+
+// One grid: the record and the tensor maps travel in the kernel parameters (no copy to the device).
 cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
                          void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                          uint32_t* err, cudaStream_t stream) {
@@ -568,10 +681,16 @@ cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int p
   TcItemHost h;
   if (!tcPrepareItem(g, elemFmt, rad16, pTotal, dirs, scratch, atlas, layerBegin, layerEnd, hysteresis, flags, 0, &h))
     return cudaErrorInvalidValue;
-  void* dItem = (uint8_t*)scratch + tcScratchBytes(g.N) - 256;
-  cudaError_t e = cudaMemcpyAsync(dItem, h.item, sizeof(h.item), cudaMemcpyHostToDevice, stream);
+  TcOne one;
+  memcpy(&one.r, h.mapR, sizeof(CUtensorMap));
+  memcpy(&one.w, h.mapW, sizeof(CUtensorMap));
+  memcpy(&one.it, h.item, sizeof(TcItem));
+  dim3 wg(kOctTexels, 1);
+  if (elemFmt == 0) k_tc_weights<0><<<wg, 256, 0, stream>>>(nullptr, one.it);
+  else k_tc_weights<1><<<wg, 256, 0, stream>>>(nullptr, one.it);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return launchConvTcItems(elemFmt, &h, dItem, 1, h.tiles, err, stream);
+  return elemFmt == 0 ? launchTc<0>(one, 2, h.units, err, stream) : launchTc<1>(one, 3, h.units, err, stream);
 }
 
 }  // namespace ddgi

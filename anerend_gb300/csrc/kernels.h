@@ -91,13 +91,13 @@ struct TcItemHost {
   alignas(64) unsigned char mapR[128];
   alignas(64) unsigned char mapW[128];
   alignas(16) unsigned char item[128];
-  int tiles;
+  int units;  // 64-probe work units of the item
 };
 bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs, void* scratch,
-                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int tileBegin,
+                   void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int unitBegin,
                    TcItemHost* out);
 cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
-                              int totalTiles, uint32_t* err, cudaStream_t stream);
+                              int totalUnits, uint32_t* err, cudaStream_t stream);
 cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
                          void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                          uint32_t* err, cudaStream_t stream);

@@ -61,9 +61,14 @@ def ray_image(g: oracle.GridGeom, R: np.ndarray) -> np.ndarray:
 
 
 @pytest.mark.parametrize("fmt", [L.DDGI_ELEM_F16, L.DDGI_ELEM_BF16])
-@pytest.mark.parametrize("n,dims", [(64, (5, 3, 3)), (256, (8, 2, 9)), (512, (16, 2, 8))])
+@pytest.mark.parametrize("n,dims,layers", [
+    (64, (5, 3, 3), None), (256, (8, 2, 9), None), (512, (16, 2, 8), None),
+    # more 64-probe units than SMs, so CTAs take two-unit tiles; a layer range starting mid-unit and a
+    # last unit cut short by the grid's end
+    (64, (61, 9, 37), (2, 9)),
+])
 @pytest.mark.parametrize("bake", [False, True])
-def test_tc_convolve_matches_fp64(ctx, fmt, n, dims, bake):
+def test_tc_convolve_matches_fp64(ctx, fmt, n, dims, layers, bake):
     lib = L.load()
     d = desc(dims, n)
     g = oracle.GridGeom(*dims, n)
@@ -81,7 +86,7 @@ def test_tc_convolve_matches_fp64(ctx, fmt, n, dims, bake):
     r16, r16d = planar16(R, fmt)
     a_dev = torch.from_numpy(atlas).cuda()
     flags = L.DDGI_UBO_BAKE_MODE_ON_FLAG if bake else 0
-    b, e = 0, dims[1]
+    b, e = layers or (0, dims[1])
     ctx.check(lib.ddgi_convolve_tc_raw(ctx.handle, C.byref(d), r16.data_ptr(), fmt, dirs.data_ptr(),
                                        a_dev.data_ptr(), b, e, flags, stream))
     ctx.sync(stream)
