@@ -297,6 +297,13 @@ SERVING = ServingWorkload("ddgi_serving_32scenes_2000rps", 32, (10_000, 1_000_00
                           (64, 128, 256, 512), 150 << 30)
 
 
+def serving_scene_tris(sw: ServingWorkload) -> list:
+    """Triangle count of each resident scene of a serving workload (log-uniform over its range, from its seed)."""
+    u = uniform(sw.seed, 9105, sw.num_scenes)
+    lo, hi = np.log(sw.tri_range[0]), np.log(sw.tri_range[1])
+    return [int(round(np.exp(lo + (hi - lo) * x))) for x in u]
+
+
 def serving_requests(sw: ServingWorkload, count: int, rate: float | None = None):
     """`count` requests: (arrival time s, scene index, dims, rays, camera, rotation frame)."""
     rate = rate or sw.rate
