@@ -379,8 +379,14 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
   const uint4 hd = ldRo(reinterpret_cast<const uint4*>(nd + 1));
   const uint4 w0 = ldRo(reinterpret_cast<const uint4*>(nd + 2)), w1 = ldRo(reinterpret_cast<const uint4*>(nd + 3)),
               w2 = ldRo(reinterpret_cast<const uint4*>(nd + 4));
-  // byte words: lo.x 0-1, lo.y 2-3, lo.z 4-5, hi.x 6-7, hi.y 8-9, hi.z 10-11
-  const uint32_t qw[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+  // byte words: lo.x in w0.x/y, lo.y in w0.z/w, lo.z in w1.x/y, hi.x in w1.z/w, hi.y in w2.x/y, hi.z in w2.z/w
+  // (first word: slots 0-3, second: slots 4-7). Near / far words of each axis picked by the ray's direction
+  // signs with selects on named words: an array indexed by the octant would be placed in local memory.
+  const bool sx = (oct & 1u) != 0, sy = (oct & 2u) != 0, sz = (oct & 4u) != 0;
+  const uint32_t qn[6] = {sx ? w1.z : w0.x, sx ? w1.w : w0.y, sy ? w2.x : w0.z, sy ? w2.y : w0.w,
+                          sz ? w2.z : w1.x, sz ? w2.w : w1.y};
+  const uint32_t qf[6] = {sx ? w0.x : w1.z, sx ? w0.y : w1.w, sy ? w0.z : w2.x, sy ? w0.w : w2.y,
+                          sz ? w1.x : w2.z, sz ? w1.y : w2.w};
   const uint32_t eb = asUint(h0.w);
   const float p[3] = {h0.x, h0.y, h0.z};
   const float o[3] = {r.o.x, r.o.y, r.o.z};
@@ -407,21 +413,17 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
       Rv[a] = fmaf(o[a] - p[a], asFloatHd((254u - e) << 23) * 3.0517578125e-05f, 1.0f);
     }
   }
-  // near / far word pairs for the ray's direction signs
-  const int nxw = (oct & 1) ? 6 : 0, fxw = 6 - nxw;
-  const int nyw = (oct & 2) ? 8 : 2, fyw = 10 - nyw;
-  const int nzw = (oct & 4) ? 10 : 4, fzw = 14 - nzw;
   uint32_t hm = 0;  // slots whose box the ray meets
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int h = c >> 2, k = c & 3;
     const uint32_t sel = 0x7604u | ((uint32_t)k << 4);
-    const float vnx = asFloatHd(bytePerm(qw[nxw + h], 0x3F800000u, sel));
-    const float vfx = asFloatHd(bytePerm(qw[fxw + h], 0x3F800000u, sel));
-    const float vny = asFloatHd(bytePerm(qw[nyw + h], 0x3F800000u, sel));
-    const float vfy = asFloatHd(bytePerm(qw[fyw + h], 0x3F800000u, sel));
-    const float vnz = asFloatHd(bytePerm(qw[nzw + h], 0x3F800000u, sel));
-    const float vfz = asFloatHd(bytePerm(qw[fzw + h], 0x3F800000u, sel));
+    const float vnx = asFloatHd(bytePerm(qn[0 + h], 0x3F800000u, sel));
+    const float vfx = asFloatHd(bytePerm(qf[0 + h], 0x3F800000u, sel));
+    const float vny = asFloatHd(bytePerm(qn[2 + h], 0x3F800000u, sel));
+    const float vfy = asFloatHd(bytePerm(qf[2 + h], 0x3F800000u, sel));
+    const float vnz = asFloatHd(bytePerm(qn[4 + h], 0x3F800000u, sel));
+    const float vfz = asFloatHd(bytePerm(qf[4 + h], 0x3F800000u, sel));
     bool in;
     if (kPlusZ) {  // oct == 0: near words are the lo words
       in = vnx <= Rv[0] + 4.76837158203125e-7f && vfx >= Rv[0] - 4.76837158203125e-7f &&
