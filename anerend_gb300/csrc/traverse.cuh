@@ -253,20 +253,21 @@ DDGI_HD bool traverse(const BvhRef& b, const WRay& r, float tmin, float tmax, Hi
 // Two node layouts, chosen at compile time by DDGI_WIDE_QUANT (default 1, the quantized one: 80 B per node
 // against 208 B; the box tests read 2.6x fewer L1 lines per node for a byte-permute and an FMA per plane).
 // FP32 node (DDGI_WIDE_QUANT=0) = 13 float4 (208 B):
-//   [0]      uint4 {childBase, triBase, meta of slots 0-3, meta of slots 4-7} (meta: one byte per slot)
+//   [0]      uint4 header {childBase, triBase, slot masks, 0}
 //   [1],[2]  lo.x of slots 0-7      [3],[4]   hi.x      [5],[6]  lo.y   [7],[8]  hi.y
 //   [9],[10] lo.z                    [11],[12] hi.z
-// meta byte: 0 = empty slot; (7 << 5) | k = internal child, wide node childBase + k (k = rank of the slot
-// among the node's internal slots); (c << 5) | o with c in 1..kWideLeafMax = leaf of c triangle records
-// starting at triBase + o. Slot s holds the child that lies most toward the corner with sign bits s (bit a
-// set = +axis a), so visiting keys s ^ octant(ray) in increasing order is roughly front to back.
+// Slot masks = internal-slot mask | leaf-slot mask << 8 (bit s: slot s); a slot in neither is empty. The
+// internal slot s is wide node childBase + (internal slots below s); the leaf slot s is the single triangle
+// record triBase + (leaf slots below s): a node's leaf records are laid out in slot order. Slot s holds the
+// child that lies most toward the corner with sign bits s (bit a set = +axis a), so visiting keys
+// s ^ octant(ray) in increasing order is roughly front to back.
 #ifndef DDGI_WIDE_QUANT
 #define DDGI_WIDE_QUANT 1
 #endif
 #if DDGI_WIDE_QUANT
 // Quantized node = 5 float4 (80 B):
 //   [0]  float origin p.x, p.y, p.z; uint biased exponents e_x | e_y << 8 | e_z << 16 (scale s_a = 2^(e_a-127))
-//   [1]  uint4 {childBase, triBase, meta of slots 0-3, meta of slots 4-7}
+//   [1]  uint4 header {childBase, triBase, slot masks, 0} as in the FP32 node
 //   [2]  q lo.x of slots 0-7 (one byte each) | q lo.y   [3] q lo.z | q hi.x   [4] q hi.y | q hi.z
 // Slot boxes are [p + q_lo s, p + q_hi s] in exact arithmetic and contain the child (quantizeSlots rounds
 // outward). The traversal reads a byte q as v = 1 + q 2^-15 (one byte permute builds the float) and gets
@@ -275,19 +276,10 @@ constexpr int kWideNodeF4 = 5;
 #else
 constexpr int kWideNodeF4 = 13;
 #endif
-constexpr int kWideLeafMax = 1;
+constexpr int kWideLeafMax = 1;  // triangles per leaf slot: the header's leaf-slot mask locates one record each
 constexpr int kWideStack = 64;
 
-static_assert(8 * kWideLeafMax <= 32, "a wide node's triangles must fit the 32-bit pending mask");
-
-// Internal-slot mask (bit s set when slot s holds a wide node: meta byte (7 << 5) | rank) of the two meta
-// words. Per byte the top three bits ANDed into bit 7, then the four bits 7, 15, 23, 31 gathered into the
-// low nibble by one multiply (the partial products land on distinct bits, so nothing carries).
-DDGI_HD uint32_t internalSlots(uint32_t m03, uint32_t m47) {
-  const uint32_t a = (m03 & (m03 << 1) & (m03 << 2) & 0x80808080u) >> 7;
-  const uint32_t b = (m47 & (m47 << 1) & (m47 << 2) & 0x80808080u) >> 7;
-  return ((a * 0x01020408u) >> 24 & 0xfu) | ((b * 0x01020408u) >> 20 & 0xf0u);
-}
+static_assert(kWideLeafMax == 1, "leaf records are located by the leaf-slot mask, one per leaf slot");
 
 // Slot bits to key bits (key = slot ^ oct): swap bit pairs, pairs of pairs and nibbles per octant bit.
 DDGI_HD uint32_t slotsToKeys(uint32_t x, uint32_t oct) {
@@ -297,8 +289,9 @@ DDGI_HD uint32_t slotsToKeys(uint32_t x, uint32_t oct) {
   return x;
 }
 
-// node: the next wide node to test, -1 when the stack is exhausted. tMask: triangles of the last tested
-// node's hit leaves still to test, as bits of offsets from tBase; a step tests one of them.
+// node: the next wide node to test, -1 when the stack is exhausted. tMask: the last tested node's hit leaf
+// slots still to test (bits 0-7) and that node's leaf-slot mask (bits 8-15), or 0 when none is left; the
+// record of leaf slot k is tBase + (leaf slots below k). A step tests one of them.
 struct WideTrav {
   int node, sp;
   uint32_t oct;
@@ -353,9 +346,12 @@ template <bool kAnyHit, bool kPlusZ = false>
 DDGI_HD bool wideStep(const BvhRef& b, const WRay& r, float tmin, WideTrav& s, HitInfo& hit, uint32_t* err) {
   if (s.tMask == 0) wideNodeTest<kAnyHit, kPlusZ>(b, r, tmin, s, hit, err);
   if (s.tMask != 0) {
-    const int k = lowestBit(s.tMask);
-    s.tMask &= s.tMask - 1u;
-    if (testTri<kAnyHit>(b, r, (int)s.tBase + k, tmin, hit) && kAnyHit) return true;
+    const uint32_t tm = s.tMask;
+    const int k = lowestBit(tm);  // a pending slot: the low byte is not empty
+    const int rec = (int)s.tBase + popc((tm >> 8) & ((1u << k) - 1u));
+    const uint32_t rest = tm & (tm - 1u);
+    s.tMask = (rest & 0xffu) ? rest : 0u;
+    if (testTri<kAnyHit>(b, r, rec, tmin, hit) && kAnyHit) return true;
   }
   return s.tMask == 0 && s.node < 0;
 }
@@ -469,27 +465,19 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
     }
   }
 #endif
-  // internal hits in key order; the rest are leaves (an empty slot, meta 0, adds no triangle)
-  const uint32_t imask = internalSlots(hd.z, hd.w);
+  // internal hits in key order; hit leaf slots become the pending triangles (empty slots are in neither mask)
+  const uint32_t imask = hd.z & 0xffu, lmask = (hd.z >> 8) & 0xffu;
   uint32_t ihits = slotsToKeys(hm & imask, oct);
-  uint32_t lhits = hm & ~imask;
-  // the hit leaves' triangles: offsets (m & 31) .. + count from triBase
-  uint32_t tm = 0;
-  while (lhits) {
-    const int c = lowestBit(lhits);
-    lhits &= lhits - 1u;
-    const uint32_t m = ((c < 4 ? hd.z : hd.w) >> (8 * (c & 3))) & 0xffu;
-    tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-  }
-  if (tm != 0u) {
-    if (hd.y + (uint32_t)bitEnd(tm) > (uint32_t)b.numTris) {
+  const uint32_t lhits = hm & lmask;
+  if (lhits != 0u) {
+    if (hd.y + (uint32_t)popc(lmask) > (uint32_t)b.numTris) {
       flagError(err, DDGI_DEVERR_BOUNDS);
       s.node = -1;
       s.sp = 0;
       return;
     }
     s.tBase = hd.y;
-    s.tMask = tm;
+    s.tMask = lhits | (lmask << 8);
   }
   if (ihits) {
     // descend into the nearest-keyed internal child, keep the rest of this node's hits on the stack

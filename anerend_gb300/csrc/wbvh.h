@@ -3,9 +3,10 @@
 //
 // Each wide node starts from one binary subtree and repeatedly opens the open child (subtree of more
 // than kWideLeafMax triangles) with the largest surface area until it has 8 children or none is left to
-// open. Children of at most kWideLeafMax triangles become leaves; their triangle records are laid out
-// contiguously per wide node (triBase + offset); larger children become wide nodes, numbered in
-// breadth-first order so the internal children of a node are consecutive (childBase + rank). Children are
+// open. Children of kWideLeafMax (one) triangle become leaf slots; their records are laid out contiguously
+// per wide node in slot order (triBase + leaf slots below); larger children become wide nodes, numbered in
+// breadth-first order so the internal children of a node are consecutive (childBase + internal slots below);
+// the header holds the internal- and leaf-slot masks. Children are
 // placed in slots by a greedy octant assignment (slot s = the child lying most toward the corner with
 // sign bits s). The method follows the greedy variant of Ylitie, Karras, Laine 2017 ("Efficient
 // incoherent ray traversal on GPUs through compressed wide BVHs"); child boxes are stored as FP32 planes
@@ -238,22 +239,21 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
       slotOf[bi] = bs;
       kidOf[bs] = bi;
     }
-    // leaves: records laid out per node in slot order; internal children: consecutive wide nodes
+    // leaves: one record each, laid out per node in slot order; internal children: consecutive wide nodes
     const uint32_t triBase = (uint32_t)order.size();
     const int childBase = numWide;
-    uint8_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t imask = 0, lmask = 0;
     int rank = 0;
     for (int s = 0; s < 8; ++s) {
       const int i = kidOf[s];
       if (i < 0) continue;
       if (kids[i].count <= kWideLeafMax) {
-        const uint32_t off = (uint32_t)order.size() - triBase;
         std::vector<int> recs;
         gather(kids[i], recs);
         for (int rec : recs) order.push_back(rec);
-        meta[s] = (uint8_t)(((uint32_t)recs.size() << 5) | off);
+        lmask |= 1u << s;
       } else {
-        meta[s] = (uint8_t)((7u << 5) | (uint32_t)rank);
+        imask |= 1u << s;
         Job j;
         j.index = childBase + rank;
         j.kids.push_back(cand(kids[i].ref, 0));
@@ -269,9 +269,7 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
       for (int sl = 0; sl < 8; ++sl) (*slotRef)[(size_t)index * 8 + sl] = kidOf[sl] >= 0 ? kids[kidOf[sl]].ref : kEmptySlot;
     }
     float4* nd = out.data() + (size_t)index * kWideNodeF4;
-    uint32_t m0 = 0, m1 = 0;
-    for (int s = 0; s < 4; ++s) m0 |= (uint32_t)meta[s] << (8 * s);
-    for (int s = 0; s < 4; ++s) m1 |= (uint32_t)meta[4 + s] << (8 * s);
+    const uint32_t masks = imask | (lmask << 8);
 #if DDGI_WIDE_QUANT
     float slo[8][3], shi[8][3];
     uint32_t used = 0;
@@ -284,9 +282,9 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
       if (i >= 0) used |= 1u << sl;
     }
     quantizeSlots(slo, shi, used, nd);
-    nd[1] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
+    nd[1] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(masks), 0.0f);
 #else
-    nd[0] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(m0), asFloatH(m1));
+    nd[0] = make_float4(asFloatH((uint32_t)childBase), asFloatH(triBase), asFloatH(masks), 0.0f);
     float pl[6][8];
     for (int s = 0; s < 8; ++s) {
       const int i = kidOf[s];
@@ -304,13 +302,14 @@ inline bool collapse(const float4* nodes2, const float4* tris, int numTris, std:
   return (int)order.size() == numTris;
 }
 
-// Header words and the exact box of slot `sl` of a wide node (host checks).
-inline void nodeHeader(const float4* nd, uint32_t& childBase, uint32_t& triBase, uint32_t meta[2]) {
+// Header words (child base, record base, internal-slot mask, leaf-slot mask) and the exact box of slot `sl`
+// of a wide node (host checks).
+inline void nodeHeader(const float4* nd, uint32_t& childBase, uint32_t& triBase, uint32_t& imask, uint32_t& lmask) {
   const float4 h = nd[DDGI_WIDE_QUANT ? 1 : 0];
   childBase = (uint32_t)asIntH(h.x);
   triBase = (uint32_t)asIntH(h.y);
-  meta[0] = (uint32_t)asIntH(h.z);
-  meta[1] = (uint32_t)asIntH(h.w);
+  imask = (uint32_t)asIntH(h.z) & 0xffu;
+  lmask = ((uint32_t)asIntH(h.z) >> 8) & 0xffu;
 }
 inline void slotBox(const float4* nd, int sl, double lo[3], double hi[3]) {
 #if DDGI_WIDE_QUANT

@@ -166,12 +166,13 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
       if (n < 0 || n >= numWide) { stats[5]++; continue; }
       ++visited;
       const float4* nd = wide.data() + (size_t)n * kWideNodeF4;
-      uint32_t childBase, triBase, mm[2];
-      wbvh::nodeHeader(nd, childBase, triBase, mm);
-      int rank = 0;
+      uint32_t childBase, triBase, imask, lmask;
+      wbvh::nodeHeader(nd, childBase, triBase, imask, lmask);
+      if (imask & lmask) stats[5]++;
+      int rank = 0, leafRank = 0;
       for (int s = 0; s < 8; ++s) {
-        uint32_t m = (mm[s / 4] >> (8 * (s % 4))) & 0xff;
-        if (!m) continue;
+        const bool internal = (imask >> s) & 1u, leaf = (lmask >> s) & 1u;
+        if (!internal && !leaf) continue;
         double blo[3], bhi[3];
         wbvh::slotBox(nd, s, blo, bhi);
         Box64 b{{blo[0], blo[1], blo[2]}, {bhi[0], bhi[1], bhi[2]}};
@@ -181,21 +182,18 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
           b.lo[a] = std::max(b.lo[a], pb.lo[a]);
           b.hi[a] = std::min(b.hi[a], pb.hi[a]);
         }
-        if ((m >> 5) == 7) {
-          if ((int)(m & 31) != rank) stats[5]++;
+        if (internal) {
           st.push_back({(int)(childBase + rank), b});
           ++rank;
         } else {
-          int c = m >> 5, first = triBase + (m & 31);
-          if (c < 1 || c > kWideLeafMax || first + c > numTris) { stats[5]++; continue; }
-          for (int k = first; k < first + c; ++k) {
-            seen[k]++;
-            for (int v = 0; v < 3; ++v) {
-              float4 p = recs2[3 * k + v];
-              float q[3] = {p.x, p.y, p.z};
-              for (int a = 0; a < 3; ++a)
-                if (q[a] < b.lo[a] || q[a] > b.hi[a]) stats[5]++;
-            }
+          const int k = (int)triBase + leafRank++;  // one record per leaf slot, in slot order
+          if (k >= numTris) { stats[5]++; continue; }
+          seen[k]++;
+          for (int v = 0; v < 3; ++v) {
+            float4 p = recs2[3 * k + v];
+            float q[3] = {p.x, p.y, p.z};
+            for (int a = 0; a < 3; ++a)
+              if (q[a] < b.lo[a] || q[a] > b.hi[a]) stats[5]++;
           }
         }
       }
