@@ -2,6 +2,8 @@
 // the probe-update path restated for CUDA, and the internal launch records.
 #pragma once
 
+#include <stddef.h>
+
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -195,6 +197,13 @@ struct InstanceGPU {
   float w2oLin[9];
   uint32_t mesh, material, triOffset;
 };
+// hit shading reads an instance record as six float4 (o2w, w2oLin, then mesh and material in the last one)
+static_assert(sizeof(InstanceGPU) == 96 && offsetof(InstanceGPU, w2oLin) == 48 && offsetof(InstanceGPU, mesh) == 84 &&
+                  offsetof(InstanceGPU, material) == 88,
+              "instance record layout read by reconstructHit");
+static_assert(offsetof(DdgiMeshInfo, indexOffset) == offsetof(DdgiMeshInfo, vertexOffset) + 4 &&
+                  offsetof(DdgiMeshInfo, vertexOffset) % 8 == 0 && sizeof(DdgiMeshInfo) % 8 == 0,
+              "vertexOffset and indexOffset of a mesh record are read as one 8-byte load");
 
 // BVH2 node in the Aila-Laine layout: child bounds packed so one node is four float4 loads.
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)

@@ -314,10 +314,17 @@ template <bool kMirrorNormal>
 DDGI_D HitSurface reconstructHit(const SceneGPU& s, int leaf, float b1, float b2) {
   const int inst = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 1].w));
   const int prim = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 2].w));
-  const InstanceGPU& in = s.instances[inst];
-  const DdgiMeshInfo& mesh = s.meshes[in.mesh];
-  const uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
-  const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
+  // the 96-byte instance record as six 16-byte loads (its buffer is 256-byte aligned): o2w in q0..q2,
+  // w2oLin in q3, q4, q5.x, then mesh and material
+  const float4* iq = reinterpret_cast<const float4*>(s.instances + inst);
+  const float4 q0 = __ldg(iq), q1 = __ldg(iq + 1), q2 = __ldg(iq + 2), q3 = __ldg(iq + 3), q4 = __ldg(iq + 4),
+               q5 = __ldg(iq + 5);
+  const float m[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+  const uint32_t meshId = __float_as_uint(q5.y), materialId = __float_as_uint(q5.z);
+  // vertexOffset and indexOffset of the mesh record, one 8-byte load
+  const uint2 offs = __ldg(reinterpret_cast<const uint2*>(&s.meshes[meshId].vertexOffset));
+  const uint32_t ib = offs.y + 3u * (uint32_t)prim;
+  const DdgiPackedVertex* vb = s.vertices + offs.x;
   const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
   const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
   const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
@@ -327,18 +334,17 @@ DDGI_D HitSurface reconstructHit(const SceneGPU& s, int leaf, float b1, float b2
   const float4 e0 = __ldg((const float4*)v0.d2), e1 = __ldg((const float4*)v1.d2), e2 = __ldg((const float4*)v2.d2);
   HitSurface h;
   const float3 posObj = xyz(a0) * b0 + xyz(a1) * b1 + xyz(a2) * b2;
-  const float* m = in.o2w;
   h.pos = f3(m[0] * posObj.x + m[1] * posObj.y + m[2] * posObj.z + m[3],
              m[4] * posObj.x + m[5] * posObj.y + m[6] * posObj.z + m[7],
              m[8] * posObj.x + m[9] * posObj.y + m[10] * posObj.z + m[11]);
-  const DdgiMaterialInfo& mat = s.materials[in.material];
+  const DdgiMaterialInfo& mat = s.materials[materialId];
   float3 nObj = f3(c0.z, c0.w, e0.x) * b0 + f3(c1.z, c1.w, e1.x) * b1 + f3(c2.z, c2.w, e2.x) * b2;
   nObj = normalize3(nObj);
   if (kMirrorNormal) {
     h.normal = normalize3(f3(m[0] * nObj.x + m[1] * nObj.y + m[2] * nObj.z, m[4] * nObj.x + m[5] * nObj.y + m[6] * nObj.z,
                              m[8] * nObj.x + m[9] * nObj.y + m[10] * nObj.z));
   } else {
-    const float* wi = in.w2oLin;  // normal * WorldToObject (row vector times the inverse 3x3)
+    const float wi[9] = {q3.x, q3.y, q3.z, q3.w, q4.x, q4.y, q4.z, q4.w, q5.x};  // normal * WorldToObject
     h.normal = normalize3(f3(nObj.x * wi[0] + nObj.y * wi[3] + nObj.z * wi[6], nObj.x * wi[1] + nObj.y * wi[4] + nObj.z * wi[7],
                              nObj.x * wi[2] + nObj.y * wi[5] + nObj.z * wi[8]));
   }
