@@ -287,7 +287,7 @@ int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_
 // Ray slots of a whole-grid trace for any warpProbes: ceil(XZ / wp) * wp <= XZ + 31 probes per layer.
 long long maxRaySlots(const GridGPU& g) { return ((long long)g.X * g.Z + 31) * g.Y * g.N; }
 
-uint64_t gridFootprint(const DdgiGridDesc* d, int convMode) {
+uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds) {
   GridGPU g = makeGridGPU(*d);
   uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rays = (uint64_t)g.rayW * g.bh * g.Z * g.Y;
@@ -297,6 +297,7 @@ uint64_t gridFootprint(const DdgiGridDesc* d, int convMode) {
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
   if (convMode != 0) bytes += 6 * rays + tcScratchBytes(g.N);
   bytes += kTraceScratchPerRay * (uint64_t)maxRaySlots(g);  // the launch's trace scratch for this grid
+  if (hitSeeds) bytes += 20ull * g.N + 4ull * g.X * g.Y * g.Z * g.N;  // previous lattice, seed map, hit memo
   return bytes;
 }
 
@@ -326,6 +327,12 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, sizeof(int) * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wt, 4 * (size_t)g->g.N * kOctTexels);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wsum, 4 * kOctTexels);
+  if (!asyncAlloc) {  // closest-hit seeding for grids traced frame after frame
+    if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->latticePrev, 16 * (size_t)g->g.N);
+    if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->seedDir, sizeof(int) * (size_t)g->g.N);
+    if (e == cudaSuccess)
+      e = gridAlloc(g, (void**)&g->hitMemo, sizeof(int) * (size_t)g->g.X * g->g.Y * g->g.Z * g->g.N);
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(g->rayRad, 0, 16 * rayTexels, st);
   if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], st);
   if (e == cudaSuccess && !asyncAlloc) e = cudaStreamSynchronize(st);
@@ -356,6 +363,9 @@ void gridDestroy(DdgiGrid* g) {
   gridFree(g, g->rayHit);
   gridFree(g, g->lattice);
   gridFree(g, g->order);
+  gridFree(g, g->latticePrev);
+  gridFree(g, g->seedDir);
+  gridFree(g, g->hitMemo);
   gridFree(g, g->rad16);
   gridFree(g, g->tcScratch);
   gridFree(g, g->wt);
@@ -636,7 +646,7 @@ void ddgi_grid_destroy(DdgiGrid* g) { gridDestroy(g); }
 
 uint64_t ddgi_grid_footprint(const DdgiGridDesc* desc, int convMode) {
   if (validateGridDesc(nullptr, desc) != DDGI_OK) return 0;
-  return gridFootprint(desc, convMode);
+  return gridFootprint(desc, convMode, true);
 }
 
 int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
@@ -725,6 +735,10 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   ti.rayDir = g->rayDir;
   ti.rayHit = g->rayHit;
   ti.warpBegin = 0;
+  ti.latticePrev = g->latticePrev;
+  ti.seedDir = g->seedDir;
+  ti.hitMemo = g->hitMemo;
+  ti.seedOn = g->memoValid ? 1 : 0;
   Mat3& rot = *reinterpret_cast<Mat3*>(h + sizeof(TraceItem));
   memcpy(rot.m, frame->rotation, sizeof(rot.m));
   CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
@@ -735,6 +749,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   g->tracedBegin = b;
   g->tracedEnd = e;
   g->latticeValid = true;
+  g->memoValid = g->hitMemo != nullptr;
   g->rad16Written = gg.rad16 != nullptr;
   return DDGI_OK;
 }

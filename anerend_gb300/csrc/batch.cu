@@ -194,6 +194,10 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.rayDir = g->rayDir;
     ti.rayHit = g->rayHit;
     ti.warpBegin = warps;
+    ti.latticePrev = g->latticePrev;
+    ti.seedDir = g->seedDir;
+    ti.hitMemo = g->hitMemo;
+    ti.seedOn = g->memoValid ? 1 : 0;
     warps += traceWarps(gg, f);
     rays += (long long)(le - lb) * g->g.X * g->g.Z * g->g.N;
     memcpy(hRots[i].m, fr.rotation, sizeof(float) * 9);
@@ -223,6 +227,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     g->tracedBegin = lb;
     g->tracedEnd = le;
     g->latticeValid = true;
+    g->memoValid = g->hitMemo != nullptr;
     g->rad16Written = tc;
   }
   rc = S->reserveRays(32 * warps);

@@ -23,6 +23,14 @@ struct TraceItem {
   float4* rayDir;
   int* rayHit;
   long long warpBegin;    // first warp of this item (its ray slots start at 32 * warpBegin)
+  // Closest-hit seeding. A ray first tests a candidate triangle: the closest hit of its probe's ray in the
+  // nearest direction of the last traced lattice. A candidate that is hit bounds the search from the start;
+  // any candidate leaves the result unchanged (the closest hit, ties to the lowest id, whatever was tested
+  // first). hitMemo == nullptr: no seeding and no memo; seedOn == 0: memo written but not read (first trace).
+  float4* latticePrev;    // the lattice kernel saves the previous lattice here before writing the new one
+  int* seedDir;           // per direction: the nearest direction of latticePrev
+  int* hitMemo;           // per (probe, direction): the closest-hit record of the last trace, -1 for a miss
+  int seedOn;
 };
 
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);

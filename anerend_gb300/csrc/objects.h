@@ -86,6 +86,13 @@ struct DdgiGrid {
   int* rayHit = nullptr;
   float4* lattice = nullptr;
   int* order = nullptr;   // trace-kernel direction order (N ints)
+  // closest-hit seeding (grids made by ddgi_grid_create; served grids trace once and keep none): the last
+  // traced lattice, per direction the nearest direction of that lattice, and per (probe, direction) the
+  // closest-hit record of the last trace (-1 for a miss)
+  float4* latticePrev = nullptr;
+  int* seedDir = nullptr;
+  int* hitMemo = nullptr;
+  bool memoValid = false;  // hitMemo holds a trace's records
   DdgiTuning tuning{};
   void* rad16 = nullptr;  // planar 16-bit radiance for the tensor-core convolution (3 x P x N)
   void* tcScratch = nullptr;
@@ -132,7 +139,8 @@ void gridDestroy(DdgiGrid* g);
 // Device bytes a grid of this description holds (atlas pair, ray images, lattice and weight tables and, for
 // a tensor-core convolution, the 16-bit radiance and its weight scratch).
 long long maxRaySlots(const GridGPU& g);
-uint64_t gridFootprint(const DdgiGridDesc* d, int convMode);
+// hitSeeds: the grid keeps the closest-hit seeding buffers (grids of ddgi_grid_create; served grids do not)
+uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds);
 // Batched launch of n (grid, scene, frame) items through a reusable launch state (records, staging, graph).
 struct LaunchState;
 LaunchState* launchStateCreate(DdgiContext* ctx);

@@ -252,7 +252,7 @@ int ddgi_server_submit(DdgiServer* s, const DdgiRequest* req, uint64_t* id) {
   Req* r = new (std::nothrow) Req();
   if (!r) return fail(ctx, DDGI_ENOMEM, "host allocation");
   r->r = *req;
-  r->bytes = gridFootprint(&req->grid, s->tuning.convMode);
+  r->bytes = gridFootprint(&req->grid, s->tuning.convMode, false);  // served grids keep no hit memo
   r->rays = (uint64_t)req->grid.dims[0] * req->grid.dims[1] * req->grid.dims[2] * (uint64_t)req->grid.raysPerProbe;
   std::lock_guard<std::mutex> lk(s->mu);
   r->id = s->nextId++;

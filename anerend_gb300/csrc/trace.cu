@@ -286,10 +286,16 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
         } else {
           ray = makeRay(probeOrigin(T.g, T.f, rs), xyz(__ldg(&T.lattice[rs.j])));
           bvh = T.s.bvh;
-          if (travInit<kWide, false>(bvh, ray, st, hit))
+          if (travInit<kWide, false>(bvh, ray, st, hit)) {
             hits[cand] = make_float4(__int_as_float(hit.leaf), hit.t, hit.b1, hit.b2);
-          else
+          } else {
             id = cand;
+            if (T.seedOn) {  // the seed candidate: the last trace's hit in the nearest direction
+              const size_t p = ((size_t)rs.layer * T.g.Z + rs.pz) * T.g.X + rs.px;
+              const int c = __ldg(&T.hitMemo[p * T.g.N + __ldg(&T.seedDir[rs.j])]);
+              if ((unsigned)c < (unsigned)bvh.numTris) testTri<false>(bvh, ray, c, kTMin, hit);
+            }
+          }
         }
       }
     }
@@ -389,6 +395,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
       const RaySlot rs = raySlot(g, f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
       const float3 origin = probeOrigin(g, f, rs);
       const float3 dir = xyz(__ldg(&T.lattice[rs.j]));
+      if (T.hitMemo)  // this trace's closest-hit record, the next trace's seed candidate
+        T.hitMemo[(((size_t)rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N + rs.j] = leaf >= 0 ? leaf : -1;
       float3 L;
       int hitCode = -1;
       if (leaf < 0) {
@@ -788,7 +796,29 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
   double r[3];
   for (int row = 0; row < 3; ++row)
     r[row] = (double)m[row] * v[0] + (double)m[3 + row] * v[1] + (double)m[6 + row] * v[2];
+  if (it.latticePrev) it.latticePrev[i] = it.lattice[i];  // the last traced lattice, for the seed map
   const_cast<float4*>(it.lattice)[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
+}
+
+// Seed map of the items that seed their closest hits: for each direction of the new lattice the nearest
+// direction of the last traced one (largest dot product, the lowest index on ties). Any choice is exact; a
+// near direction makes the candidate likely to be hit.
+__global__ void k_seed_dirs(const TraceItem* __restrict__ items) {
+  const TraceItem& it = items[blockIdx.y];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!it.seedOn || j >= it.g.N) return;
+  const float4 d = it.lattice[j];
+  float best = -3.0f;
+  int bi = 0;
+  for (int i = 0; i < it.g.N; ++i) {
+    const float4 q = __ldg(&it.latticePrev[i]);
+    const float c = d.x * q.x + d.y * q.y + d.z * q.z;
+    if (c > best) {
+      best = c;
+      bi = i;
+    }
+  }
+  it.seedDir[j] = bi;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -835,6 +865,7 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   if (e != cudaSuccess) return e;
   dim3 lg((maxN + 127) / 128, numItems);
   k_lattice_batch<<<lg, 128, 0, stream>>>(dItems, dRots);
+  k_seed_dirs<<<lg, 128, 0, stream>>>(dItems);
   if (totalWarps <= 0) return cudaGetLastError();
   const long long rays = totalWarps * 32;
   if (rays > 0x7fffffffll) return cudaErrorInvalidValue;  // shadow records carry 31-bit slot ids + a flag

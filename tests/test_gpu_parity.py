@@ -435,3 +435,35 @@ def test_skipped_shadow_rays_leave_radiance_unchanged(ctx, shadow_mode):
         for g in grids:
             g.close()
         scene.close()
+
+
+@pytest.mark.parametrize("bvh_width", [8, 2])
+def test_seeded_closest_hits_equal_unseeded(ctx, bvh_width):
+    """A grid traced frame after frame first tests, for each ray, the closest hit its probe's ray in the
+    nearest direction of the previous lattice had; a fresh grid has no such candidate. Hit ids and shadow
+    bits of every ray must be the same either way, across frames 8-11 of the 262,144-triangle workload
+    (the camera moves between frames 9 and 10)."""
+    w = scenes.SINGLE_GRID
+    scene = ddgi.Scene(ctx, scenes.build_scene(w))
+    opts = L.DDGI_GRID_RECORD_HITS
+    seeded = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=opts)
+    try:
+        seeded.set_tuning(bvh_width=bvh_width)
+        for f in range(8, 12):
+            fp = ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f), layer=3)
+            seeded.update(scene, fp)
+            fresh = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=opts)
+            try:
+                fresh.set_tuning(bvh_width=bvh_width)
+                fresh.update(scene, fp)
+                ctx.sync()
+                _, want, _ = fresh.download_rays(hits=True)
+                _, got, _ = seeded.download_rays(hits=True)
+            finally:
+                fresh.close()
+            rows = slice(3 * w.dims[2] * 16, 4 * w.dims[2] * 16)
+            assert np.array_equal(got[rows], want[rows]), f
+            assert (got[rows] >= 0).mean() > 0.5
+    finally:
+        seeded.close()
+        scene.close()
