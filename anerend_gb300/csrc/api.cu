@@ -297,7 +297,7 @@ uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds) {
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
   if (convMode != 0) bytes += 6 * rays + tcScratchBytes(g.N);
   bytes += kTraceScratchPerRay * (uint64_t)maxRaySlots(g);  // the launch's trace scratch for this grid
-  if (hitSeeds) bytes += 20ull * g.N + 4ull * g.X * g.Y * g.Z * g.N;  // previous lattice, seed map, hit memo
+  if (hitSeeds) bytes += 20ull * g.N + 8ull * g.X * g.Y * g.Z * g.N;  // previous lattice, seed map, two memos
   return bytes;
 }
 
@@ -332,6 +332,8 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
     if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->seedDir, sizeof(int) * (size_t)g->g.N);
     if (e == cudaSuccess)
       e = gridAlloc(g, (void**)&g->hitMemo, sizeof(int) * (size_t)g->g.X * g->g.Y * g->g.Z * g->g.N);
+    if (e == cudaSuccess)
+      e = gridAlloc(g, (void**)&g->occMemo, sizeof(int) * (size_t)g->g.X * g->g.Y * g->g.Z * g->g.N);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(g->rayRad, 0, 16 * rayTexels, st);
   if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], st);
@@ -366,6 +368,7 @@ void gridDestroy(DdgiGrid* g) {
   gridFree(g, g->latticePrev);
   gridFree(g, g->seedDir);
   gridFree(g, g->hitMemo);
+  gridFree(g, g->occMemo);
   gridFree(g, g->rad16);
   gridFree(g, g->tcScratch);
   gridFree(g, g->wt);
@@ -738,6 +741,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   ti.latticePrev = g->latticePrev;
   ti.seedDir = g->seedDir;
   ti.hitMemo = g->hitMemo;
+  ti.occMemo = g->occMemo;
   ti.seedOn = g->memoValid ? 1 : 0;
   Mat3& rot = *reinterpret_cast<Mat3*>(h + sizeof(TraceItem));
   memcpy(rot.m, frame->rotation, sizeof(rot.m));

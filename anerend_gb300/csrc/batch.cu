@@ -197,6 +197,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.latticePrev = g->latticePrev;
     ti.seedDir = g->seedDir;
     ti.hitMemo = g->hitMemo;
+    ti.occMemo = g->occMemo;
     ti.seedOn = g->memoValid ? 1 : 0;
     warps += traceWarps(gg, f);
     rays += (long long)(le - lb) * g->g.X * g->g.Z * g->g.N;

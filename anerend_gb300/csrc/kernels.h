@@ -30,6 +30,9 @@ struct TraceItem {
   float4* latticePrev;    // the lattice kernel saves the previous lattice here before writing the new one
   int* seedDir;           // per direction: the nearest direction of latticePrev
   int* hitMemo;           // per (probe, direction): the closest-hit record of the last trace, -1 for a miss
+  // Shadow rays likewise first test the occluder of the shadow ray in the nearest previous direction (a
+  // record of the BVH the shadow rays traverse); a shadowed ray that hits it needs no traversal.
+  int* occMemo;           // per (probe, direction): the last shadow ray's occluder record, -1 if unshadowed
   int seedOn;
 };
 

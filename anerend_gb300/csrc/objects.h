@@ -92,7 +92,8 @@ struct DdgiGrid {
   float4* latticePrev = nullptr;
   int* seedDir = nullptr;
   int* hitMemo = nullptr;
-  bool memoValid = false;  // hitMemo holds a trace's records
+  int* occMemo = nullptr;  // per (probe, direction): the shadow ray's occluder record of a trace, -1 if unshadowed
+  bool memoValid = false;  // hitMemo and occMemo hold a trace's records
   DdgiTuning tuning{};
   void* rad16 = nullptr;  // planar 16-bit radiance for the tensor-core convolution (3 x P x N)
   void* tcScratch = nullptr;

@@ -428,7 +428,14 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         // is cast only when the values differ or the caller records per-ray hit codes (their shadow bit).
         cast = T.rayHit != nullptr || __float_as_uint(L.x) != __float_as_uint(Ls.x) ||
                __float_as_uint(L.y) != __float_as_uint(Ls.y) || __float_as_uint(L.z) != __float_as_uint(Ls.z);
-        hits[id] = make_float4(Ls.x, Ls.y, Ls.z, 0.f);
+        // the shadowed value, and in .w the shadow ray's candidate occluder (the last trace's occluder in the
+        // nearest previous direction, -1 for none)
+        int occ = -1;
+        if (cast && T.seedOn) {
+          const size_t pj = (((size_t)rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N;
+          occ = __ldg(&T.occMemo[pj + __ldg(&T.seedDir[rs.j])]);
+        }
+        hits[id] = make_float4(Ls.x, Ls.y, Ls.z, __int_as_float(occ));
         hitCode = __float_as_int(r0.w) * 2;
       }
       // stores (rgen:108-109)
@@ -457,7 +464,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
 // kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
 template <bool kWide, bool kLightSpace, class Src>
 __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlocks : DDGI_TRACE_MIN_BLOCKS)
-    k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList,
+    k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList, float4* __restrict__ hits,
                    unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -488,11 +495,18 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
         bvh = kLightSpace ? T.s.shadow : T.s.bvh;
         ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
+        if (!finished) {  // the candidate occluder k_shade parked: if it is hit, the ray is shadowed
+          const int c = __float_as_int(hits[slot].w);
+          if ((unsigned)c < (unsigned)bvh.numTris) finished = testTri<true>(bvh, ray, c, kTMin, hit);
+        }
       }
     }
     if (id >= 0 && !finished) finished = travStep<kWide, true, kLightSpace>(bvh, ray, st, hit, err);
     if (id >= 0 && finished) {
-      if (hit.leaf >= 0) reinterpret_cast<uint32_t*>(shadowList + id)[3] = slot | 0x80000000u;
+      if (hit.leaf >= 0) {
+        reinterpret_cast<uint32_t*>(shadowList + id)[3] = slot | 0x80000000u;
+        reinterpret_cast<int*>(hits + slot)[3] = hit.leaf;  // the occluder, for the memo
+      }
       id = -1;
     }
   }
@@ -510,12 +524,18 @@ __global__ void __launch_bounds__(256) k_shadow_resolve(const __grid_constant__ 
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
        k += (long long)gridDim.x * blockDim.x) {
     const uint32_t u = __float_as_uint(shadowList[k].w);
-    if (!(u & 0x80000000u)) continue;
     const uint32_t id = u & 0x7fffffffu;
     const long long warp = id >> 5;
     const TraceItem& T = src.at(warp);
+    const bool shadowed = (u & 0x80000000u) != 0;
+    if (!shadowed && !T.occMemo) continue;
     const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
-    const float3 Ls = xyz(hits[id]);
+    const float4 hr = hits[id];
+    if (T.occMemo)  // the occluder of this shadow ray (-1: unshadowed), the next trace's candidate
+      T.occMemo[(((size_t)rs.layer * T.g.Z + rs.pz) * T.g.X + rs.px) * T.g.N + rs.j] =
+          shadowed ? __float_as_int(hr.w) : -1;
+    if (!shadowed) continue;
+    const float3 Ls = xyz(hr);
     const size_t idx = rayIndex(T.g, rs);
     T.rayRad[idx] = make_float4(Ls.x, Ls.y, Ls.z, 1.0f);
     if (T.rayHit) T.rayHit[idx] |= 1;
@@ -851,7 +871,7 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
   auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, Src> : k_trace_shadow<true, false, Src>)
                      : (lightSpace ? k_trace_shadow<false, true, Src> : k_trace_shadow<false, false, Src>);
   const int shadowBlocks = lightSpace ? blocks * kShadowLightBlocks / DDGI_TRACE_MIN_BLOCKS : blocks;
-  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
+  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dHits, dCounters, refill, err);
   k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters, dHits);
 }
 

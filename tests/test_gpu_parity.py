@@ -440,9 +440,9 @@ def test_skipped_shadow_rays_leave_radiance_unchanged(ctx, shadow_mode):
 @pytest.mark.parametrize("bvh_width", [8, 2])
 def test_seeded_closest_hits_equal_unseeded(ctx, bvh_width):
     """A grid traced frame after frame first tests, for each ray, the closest hit its probe's ray in the
-    nearest direction of the previous lattice had; a fresh grid has no such candidate. Hit ids and shadow
-    bits of every ray must be the same either way, across frames 8-11 of the 262,144-triangle workload
-    (the camera moves between frames 9 and 10)."""
+    nearest direction of the previous lattice had, and for each shadow ray that ray's occluder; a fresh grid
+    has no such candidates. Hit ids and shadow bits of every ray must be the same either way, across frames
+    8-11 of the 262,144-triangle workload (the camera moves between frames 9 and 10)."""
     w = scenes.SINGLE_GRID
     scene = ddgi.Scene(ctx, scenes.build_scene(w))
     opts = L.DDGI_GRID_RECORD_HITS
