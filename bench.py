@@ -575,7 +575,8 @@ def run_ours(args, rank, local, world):
         e[2].record()
         grid.convolve(fp, stream)
         e[3].record()
-        launches += 7 + (1 if moved else 0)  # lattice, closest hit, shade, shadow, shadow resolve, weights, convolve (+ translate)
+        # lattice, seed map, closest hit, shade, shadow, shadow resolve, weights, convolve (+ translate)
+        launches += 8 + (1 if moved else 0)
         f += 1
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0

@@ -213,7 +213,10 @@ void ddgi_grid_destroy(DdgiGrid* grid);
 int  ddgi_grid_buffers(const DdgiGrid* grid, DdgiGridBuffers* out);
 /* Clears the atlas to (0,0,0,1) and the translation state to (0,0). */
 int  ddgi_grid_reset(DdgiGrid* grid, void* stream);
-/* Device bytes a grid of this description holds with the given DdgiTuning.convMode (0 for an invalid desc). */
+/* Device bytes a grid of this description made by ddgi_grid_create holds with the given DdgiTuning.convMode
+ * (0 for an invalid desc). It includes 8 bytes per probe ray for the hit and occluder records of the grid's
+ * last trace, which seed its next trace (each ray first tests the triangle its probe's ray in the nearest
+ * direction hit); grids of the serving loop are traced once and keep none. */
 uint64_t ddgi_grid_footprint(const DdgiGridDesc* desc, int convMode);
 /* Reads / sets the grid's launch shape (results do not depend on it). */
 int  ddgi_grid_get_tuning(const DdgiGrid* grid, DdgiTuning* out);
@@ -390,7 +393,7 @@ int  ddgi_batch_update(DdgiBatch* batch, const DdgiFrame* frames, void* stream);
 typedef struct DdgiServer DdgiServer;
 
 typedef struct DdgiServerConfig {
-  uint64_t memoryBudget;  /* device bytes of request grids admitted at once (ddgi_grid_footprint) */
+  uint64_t memoryBudget;  /* device bytes of request grids admitted at once (ddgi_grid_footprint less the seeding records) */
   int32_t  maxBatch;      /* requests per launch (1..64) */
   int32_t  inFlight;      /* launches running at once, each on its own stream (1..4) */
   int32_t  convMode;      /* DdgiTuning.convMode of the served grids */
