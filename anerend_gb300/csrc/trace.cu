@@ -137,12 +137,17 @@ DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const voi
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Wavefront trace of one launch (every item of a batch, or one grid): four kernels in stream order.
-//   k_trace_closest   persistent closest-hit traversal; writes one hit record per ray slot
-//   k_shade           one thread per ray slot: hit reconstruction, shading, probe lookup, outputs; appends
-//                     a shadow ray (origin + slot id) to a list for each hit
-//   k_trace_shadow    persistent any-hit traversal over the list; flags the records of shadowed rays
-//   k_shadow_resolve  one thread per shadow record: the shadowed radiance of the flagged rays
+// Wavefront trace of one launch (every item of a batch, or one grid): four kernels in stream order, after
+// the lattice and seed-map kernels.
+//   k_trace_closest   persistent closest-hit traversal, seeded with a candidate hit; writes one hit record
+//                     per ray slot
+//   k_shade           one thread per ray slot: hit reconstruction, shading, probe lookup, outputs, hit memo;
+//                     appends a shadow ray (origin + slot id) to a list for each hit whose lit and shadowed
+//                     radiance differ
+//   k_trace_shadow    persistent any-hit traversal over the list, seeded with a candidate occluder; flags
+//                     the records of shadowed rays
+//   k_shadow_resolve  one thread per shadow record: the occluder memo and the shadowed radiance of the
+//                     flagged rays
 // Splitting keeps each kernel small (registers, instruction cache), lets the traversal kernels refill
 // idle lanes with new rays instead of waiting for a warp's longest ray, and keeps scattered per-ray output
 // writes out of the traversal loops.
