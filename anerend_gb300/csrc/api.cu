@@ -521,11 +521,23 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
   sc->view.meshes = sc->meshes;
   sc->view.instances = sc->instances;
   sc->view.materials = sc->materials;
+  if (tris > 0) {
+    e = cudaMalloc(&sc->shade, 48ull * tris);
+    if (e == cudaSuccess) {
+      sc->view.shade = sc->shade;
+      e = launchShadingRecords(sc->view, d->numIndices, d->numVertices, sc->shade, ctx->dErr, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      ddgi_scene_destroy(sc);
+      return cudaFail(ctx, e, "scene shading records");
+    }
+  }
   sc->info.numTriangles = tris;
   sc->info.numNodes = (uint64_t)sc->bvh.numNodes;
   sc->info.deviceBytes = sizeof(DdgiPackedVertex) * d->numVertices + 4ull * d->numIndices +
                          sizeof(DdgiMeshInfo) * d->numMeshes + sizeof(InstanceGPU) * inst.size() +
-                         sizeof(DdgiMaterialInfo) * d->numMaterials + 48ull * tris +
+                         sizeof(DdgiMaterialInfo) * d->numMaterials + 48ull * tris + 48ull * tris +
                          64ull * (tris > 1 ? tris - 1 : 1) + 208ull * (uint64_t)sc->bvh.numWNodes;
   for (int k = 0; k < 3; ++k) {
     sc->info.boundsMin[k] = sc->bvh.centroidLo[k];
@@ -564,6 +576,9 @@ int updateBvhs(DdgiScene* sc, int mode, cudaStream_t st) {
   cudaError_t e = refresh(sc->bvh, sc->instances);
   if (e != cudaSuccess) return cudaFail(ctx, e, "scene BVH update");
   sc->view.bvh = BvhRef{sc->bvh.nodes, sc->bvh.wnodes, sc->bvh.tris, tris, sc->bvh.numNodes, sc->bvh.numWNodes};
+  e = launchShadingRecords(sc->view, sc->numIndices, sc->numVertices, sc->shade, ctx->dErr, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "scene shading records");
   if (sc->shadowValid) {
     int k[3];
     double S[3];
@@ -628,6 +643,7 @@ void ddgi_scene_destroy(DdgiScene* s) {
   cudaFree(s->meshes);
   cudaFree(s->instances);
   cudaFree(s->materials);
+  cudaFree(s->shade);
   lbvhFree(&s->bvh);
   lbvhFree(&s->shadowBvh);
   delete s;

@@ -229,6 +229,11 @@ struct SceneGPU {
   const DdgiMeshInfo* meshes;
   const InstanceGPU* instances;
   const DdgiMaterialInfo* materials;
+  // Shading records, 3 float4 per record of `bvh` (its order): vertex k's normal times the instance's
+  // WorldToObject (normal * WorldToObject, rchit:72, applied per vertex: the product is linear, so
+  // interpolating afterwards gives the same direction) in .xyz, and the instance's material in .w of the
+  // first. The probe-update shading reads these instead of the index / vertex / instance records.
+  const float4* shade;
   // Shadow BVH in the sheared ray space of the light direction (Woop et al.'s per-ray shear, fixed for
   // every shadow ray of a frame): a shadow ray from p is the line through shear(p) along +z, so the same
   // watertight test and traversal run on it with direction (0, 0, 1). shadow.tris is null when not built.

@@ -37,6 +37,10 @@ struct TraceItem {
 };
 
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);
+// Shading records (SceneGPU::shade) of the scene BVH's records, from the scene's index, vertex, mesh and
+// instance records; `out` holds 3 * bvh.numTris float4.
+cudaError_t launchShadingRecords(const SceneGPU& s, uint64_t numIndices, uint64_t numVerts, float4* out,
+                                 uint32_t* err, cudaStream_t stream);
 // Warps of one grid's trace for frame f (32 ray slots each).
 long long traceWarps(const GridGPU& g, const FrameGPU& f);
 // Device counters of one trace launch: closest-hit queue, shadow-list length, shadow queue, spare.

@@ -65,6 +65,7 @@ struct DdgiScene {
   InstanceGPU* instances = nullptr;
   DdgiMaterialInfo* materials = nullptr;
   LbvhResult bvh;
+  float4* shade = nullptr;            // shading records of bvh's records (SceneGPU::shade)
   DdgiSceneInfo info{};
   SceneGPU view{};
   std::vector<InstanceGPU> hostInst;  // host copy (composed into the shadow BVH's transforms)

@@ -376,6 +376,79 @@ DDGI_D HitSurface reconstructHit(const SceneGPU& s, int leaf, float b1, float b2
   return h;
 }
 
+// Interpolated vertex colour in linear space at record `leaf` (rchit:183-184, bindless.glsl:199-203), through
+// the index and vertex records: the shading's fallback when the material's base colour factor is dark.
+DDGI_D float3 vertexColour(const SceneGPU& s, int leaf, float b0, float b1, float b2) {
+  const int inst = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 1].w));
+  const int prim = __float_as_int(__ldg(&s.bvh.tris[3 * leaf + 2].w));
+  const DdgiMeshInfo& mesh = s.meshes[s.instances[inst].mesh];
+  const uint32_t ib = mesh.indexOffset + 3u * (uint32_t)prim;
+  const DdgiPackedVertex* vb = s.vertices + mesh.vertexOffset;
+  const DdgiPackedVertex& v0 = vb[__ldg(&s.indices[ib])];
+  const DdgiPackedVertex& v1 = vb[__ldg(&s.indices[ib + 1])];
+  const DdgiPackedVertex& v2 = vb[__ldg(&s.indices[ib + 2])];
+  const float3 c = f3(v0.d0[3], v0.d1[0], v0.d1[1]) * b0 + f3(v1.d0[3], v1.d1[0], v1.d1[1]) * b1 +
+                   f3(v2.d0[3], v2.d1[0], v2.d1[1]) * b2;
+  return toLinear(c);
+}
+
+// Surface at a hit of the probe update from the BVH record (world vertices) and its shading record
+// (SceneGPU::shade): position = the interpolated world vertices, normal = normalize(interpolated
+// vertex normal * WorldToObject) - the reference's ObjectToWorld * interpolated object position and
+// normalize(normalize(interpolated normal) * WorldToObject) (rchit:137-187), in another order of the same
+// linear operations. Three dependent loads per hit (record, shading record, material) instead of five
+// levels through the instance, mesh, index and vertex records.
+DDGI_D HitSurface shadeSurface(const SceneGPU& s, int leaf, float b1, float b2, float4& r0) {
+  r0 = __ldg(&s.bvh.tris[3 * leaf]);
+  const float4 r1 = __ldg(&s.bvh.tris[3 * leaf + 1]), r2 = __ldg(&s.bvh.tris[3 * leaf + 2]);
+  const float4 m0 = __ldg(&s.shade[3 * leaf]), m1 = __ldg(&s.shade[3 * leaf + 1]), m2 = __ldg(&s.shade[3 * leaf + 2]);
+  const float b0 = 1.0f - b1 - b2;
+  HitSurface h;
+  h.pos = xyz(r0) * b0 + xyz(r1) * b1 + xyz(r2) * b2;
+  h.normal = normalize3(xyz(m0) * b0 + xyz(m1) * b1 + xyz(m2) * b2);
+  const DdgiMaterialInfo& mat = s.materials[__float_as_uint(m0.w)];
+  const float4 bcf = __ldg((const float4*)mat.baseColFac);
+  h.color = bcf.x + bcf.y + bcf.z > 0.1f ? xyz(bcf) : vertexColour(s, leaf, b0, b1, b2);
+  const float4 mr = __ldg((const float4*)mat.metRough);
+  const float4 em = __ldg((const float4*)mat.emissive);
+  h.metallic = mr.x;
+  h.roughness = mr.y;
+  h.emissive = xyz(em) * em.w;
+  return h;
+}
+
+// Shading records of the scene BVH's records (SceneGPU::shade), one thread per record.
+__global__ void k_shading_records(SceneGPU s, uint64_t numIndices, uint64_t numVerts, float4* __restrict__ out,
+                                  uint32_t* __restrict__ err) {
+  const int rec = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rec >= s.bvh.numTris) return;
+  const int inst = __float_as_int(s.bvh.tris[3 * rec + 1].w);
+  const int prim = __float_as_int(s.bvh.tris[3 * rec + 2].w);
+  const InstanceGPU& in = s.instances[inst];
+  const DdgiMeshInfo& mesh = s.meshes[in.mesh];
+  const float* wi = in.w2oLin;
+  for (int k = 0; k < 3; ++k) {
+    const uint64_t ii = (uint64_t)mesh.indexOffset + 3ull * (uint64_t)prim + k;
+    uint64_t vv = ii < numIndices ? (uint64_t)mesh.vertexOffset + s.indices[ii] : numVerts;
+    if (vv >= numVerts) {
+      atomicOr(err, DDGI_DEVERR_BOUNDS);
+      out[3 * rec + k] = make_float4(0.f, 0.f, 0.f, __uint_as_float(in.material));
+      continue;
+    }
+    const DdgiPackedVertex& v = s.vertices[vv];
+    const float nx = v.d1[2], ny = v.d1[3], nz = v.d2[0];
+    out[3 * rec + k] = make_float4(nx * wi[0] + ny * wi[3] + nz * wi[6], nx * wi[1] + ny * wi[4] + nz * wi[7],
+                                   nx * wi[2] + ny * wi[5] + nz * wi[8], __uint_as_float(in.material));
+  }
+}
+
+cudaError_t launchShadingRecords(const SceneGPU& s, uint64_t numIndices, uint64_t numVerts, float4* out,
+                                 uint32_t* err, cudaStream_t stream) {
+  if (s.bvh.numTris <= 0) return cudaSuccess;
+  k_shading_records<<<(s.bvh.numTris + 255) / 256, 256, 0, stream>>>(s, numIndices, numVerts, out, err);
+  return cudaGetLastError();
+}
+
 // Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
 // computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
 // shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
@@ -407,9 +480,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
       if (leaf < 0) {
         L = toLinear(f.skyColor * f.skyIntensity);  // rmiss:20
       } else {
-        const HitSurface h = reconstructHit<false>(s, leaf, hr.z, hr.w);
+        float4 r0;
+        const HitSurface h = shadeSurface(s, leaf, hr.z, hr.w, r0);
         const float3 pos = h.pos;
-        const float4 r0 = __ldg(&s.bvh.tris[3 * leaf]);
         // shadow ray origin toward the sun (rchit:155-176): the light's sheared space when built
         if (s.shadow.tris != nullptr) {
           const float pk[3] = {pos.x, pos.y, pos.z};
