@@ -59,17 +59,22 @@ __global__ void __launch_bounds__(256) k_conv_weights_batch(const ConvItem* __re
   if (threadIdx.x == 0) it.wsum[t] = part[0];
 }
 
-// Many grids in one launch. The unit of work is a tile of 32 probes of one item (kTileProbes); a block of
-// 128 threads computes the 32 x 64 (probe, texel) block of a tile with a 4-probe x 4-texel register tile per
-// thread, so one shared-memory float4 of weights and four float4s of radiance feed 48 FMAs. The rays are
-// walked in chunks of 16: the next chunk's radiance and weights are fetched into registers while the current
-// chunk is consumed from shared memory. Every (probe, texel) sum runs over j in order with fmaf, as the
-// single-grid kernel does.
-constexpr int kTileProbes = 32;
+// Many grids in one launch. The unit of work is a tile of 8 kPT probes of one item (kTileProbes); a block of
+// 128 threads computes the kTileProbes x 64 (probe, texel) block of a tile with a kPT-probe x 4-texel
+// register tile per thread, so one shared-memory float4 of weights and kPT float4s of radiance feed 12 kPT
+// FMAs. The rays are walked in chunks of 16: the next chunk's radiance and weights are fetched into registers
+// while the current chunk is consumed from shared memory. Every (probe, texel) sum runs over j in order with
+// fmaf, whatever the tile shape. kPT = 2 keeps twice the warps of kPT = 4 resident on a single grid (an
+// 8192-probe grid is 512 tiles), which the latency of the shared-memory loads needs.
+#ifndef DDGI_CONV_PT
+#define DDGI_CONV_PT 2
+#endif
+constexpr int kPT = DDGI_CONV_PT;  // probes per thread
+constexpr int kTileProbes = 8 * kPT;
 constexpr int kTileThreads = 128;
 constexpr int kChunk = 16;  // rays per chunk (the smallest raysPerProbe)
 constexpr int kRStride = kChunk + 1;  // padded probe stride of the radiance chunk (bank spread)
-constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;          // 4 float4 per thread
+constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;          // kPT float4 per thread
 constexpr int kWLoads = kChunk * kOctTexels / 4 / kTileThreads;       // 2 float4 per thread
 
 // kSingle: one item, passed by value in `single` (the raw entry points, which own no device records).
@@ -80,7 +85,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
   __shared__ float4 sR[kTileProbes * kRStride];
   __shared__ float4 sW[kChunk * kOctTexels / 4];
   const int tg = threadIdx.x & 15;  // texels 4tg .. 4tg+3
-  const int pg = threadIdx.x >> 4;  // probes 4pg .. 4pg+3 of the tile
+  const int pg = threadIdx.x >> 4;  // probes kPT pg .. kPT pg + kPT - 1 of the tile
   for (long long tile = blockIdx.x; tile < totalTiles; tile += gridDim.x) {
     int lo = 0, hi = kSingle ? 0 : numItems - 1;
     while (lo < hi) {
@@ -116,9 +121,9 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
 #pragma unroll
       for (int k = 0; k < kWLoads; ++k) wn[k] = __ldg(W4 + (size_t)j0 * (kOctTexels / 4) + threadIdx.x + k * kTileThreads);
     };
-    float acc[4][4][3];
+    float acc[kPT][4][3];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < kPT; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = acc[a][b][2] = 0.0f;
     fetch(0);
@@ -135,8 +140,8 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
         float4 w = sW[jj * (kOctTexels / 4) + tg];
         float wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          float4 L = sR[(4 * pg + a) * kRStride + jj];
+        for (int a = 0; a < kPT; ++a) {
+          float4 L = sR[(kPT * pg + a) * kRStride + jj];
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             acc[a][b][0] = fmaf(wv[b], L.x, acc[a][b][0]);
@@ -149,8 +154,8 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
     const bool bake = (it.flags & DDGI_UBO_BAKE_MODE_ON_FLAG) != 0;
     const float h = it.hysteresis, ha = 1.0f - h;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      long long pl = base + 4 * pg + a;
+    for (int a = 0; a < kPT; ++a) {
+      long long pl = base + kPT * pg + a;
       if (pl >= total) break;
       int layer = it.layerBegin + (int)(pl / probesPerLayer);
       int p = (int)(pl % probesPerLayer);
