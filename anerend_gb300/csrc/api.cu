@@ -813,7 +813,8 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
   ci.flags = frame->flags;
   ci.groupBegin = 0;
   CK(g->ring.copy(slot, g->dConv, sizeof(ConvItem), st), "convolve record");
-  CK(launchConvFp32Batch(g->dConv, 1, convGroups(g->g, b, e), st), "convolve");
+  const int tp = convTileProbes((long long)(e - b) * g->g.X * g->g.Z);
+  CK(launchConvFp32Batch(g->dConv, 1, convGroups(g->g, b, e, tp), st, tp), "convolve");
   return DDGI_OK;
 }
 
@@ -970,13 +971,22 @@ int ddgi_mirror_reflections(DdgiGrid* g, DdgiScene* sc, const DdgiFrame* frame, 
   int rc = frameToGPU(ctx, frame, f);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  // shadow rays in the light-space BVH of this frame's light when the grid traces its shadows there
+  SceneGPU view = sc->view;
+  if (g->tuning.shadowMode == 1) {
+    rc = ensureShadowBvh(sc, frame->lightDir, st);
+    if (rc) return rc;
+    view = sc->view;
+  } else {
+    view.shadow = BvhRef{};
+  }
   // rays, hits, shadow points, shadowed radiance, visibility; released once the stream has consumed them
   void* scratch = nullptr;
   unsigned long long* counter = nullptr;
   CK(cudaMallocAsync(&scratch, mirrorScratchBytes((long long)count), st), "mirror scratch");
   cudaError_t e = cudaMallocAsync(&counter, sizeof(unsigned long long), st);
   if (e == cudaSuccess)
-    e = launchMirror(sc->view, g->g, f, g->atlas[g->cur], points, (long long)count, (float4*)out, scratch, counter,
+    e = launchMirror(view, g->g, f, g->atlas[g->cur], points, (long long)count, (float4*)out, scratch, counter,
                      ctx->dErr, st);
   cudaFreeAsync(scratch, st);
   if (counter) cudaFreeAsync(counter, st);

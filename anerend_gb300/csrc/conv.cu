@@ -59,29 +59,27 @@ __global__ void __launch_bounds__(256) k_conv_weights_batch(const ConvItem* __re
   if (threadIdx.x == 0) it.wsum[t] = part[0];
 }
 
-// Many grids in one launch. The unit of work is a tile of 8 kPT probes of one item (kTileProbes); a block of
-// 128 threads computes the kTileProbes x 64 (probe, texel) block of a tile with a kPT-probe x 4-texel
-// register tile per thread, so one shared-memory float4 of weights and kPT float4s of radiance feed 12 kPT
-// FMAs. The rays are walked in chunks of 16: the next chunk's radiance and weights are fetched into registers
-// while the current chunk is consumed from shared memory. Every (probe, texel) sum runs over j in order with
-// fmaf, whatever the tile shape. kPT = 2 keeps twice the warps of kPT = 4 resident on a single grid (an
-// 8192-probe grid is 512 tiles), which the latency of the shared-memory loads needs.
-#ifndef DDGI_CONV_PT
-#define DDGI_CONV_PT 2
-#endif
-constexpr int kPT = DDGI_CONV_PT;  // probes per thread
-constexpr int kTileProbes = 8 * kPT;
+// Many grids in one launch. The unit of work is a tile of 8 kPT probes of one item; a block of 128 threads
+// computes the 8 kPT x 64 (probe, texel) block of a tile with a kPT-probe x 4-texel register tile per thread,
+// so one shared-memory float4 of weights and kPT float4s of radiance feed 12 kPT FMAs. The rays are walked
+// in chunks of 16: the next chunk's radiance and weights are fetched into registers while the current chunk
+// is consumed from shared memory. Every (probe, texel) sum runs over j in order with fmaf, whatever the tile
+// shape. kPT = 4 reads shared memory least per FMA; kPT = 2 keeps twice the warps resident when a launch has
+// few tiles (an 8192-probe grid: 512 tiles of 16 probes instead of 256 of 32), which the latency of the
+// shared-memory loads needs. convTileProbes picks one per launch.
 constexpr int kTileThreads = 128;
 constexpr int kChunk = 16;  // rays per chunk (the smallest raysPerProbe)
 constexpr int kRStride = kChunk + 1;  // padded probe stride of the radiance chunk (bank spread)
-constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;          // kPT float4 per thread
 constexpr int kWLoads = kChunk * kOctTexels / 4 / kTileThreads;       // 2 float4 per thread
 
 // kSingle: one item, passed by value in `single` (the raw entry points, which own no device records).
-template <bool kSingle>
+// kPT: probes per thread (tiles of 8 kPT probes).
+template <bool kSingle, int kPT>
 __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvItem* __restrict__ items, int numItems,
                                                                      long long totalTiles,
                                                                      const __grid_constant__ ConvItem single) {
+  constexpr int kTileProbes = 8 * kPT;
+  constexpr int kRLoads = kTileProbes * kChunk / kTileThreads;  // kPT float4 per thread
   __shared__ float4 sR[kTileProbes * kRStride];
   __shared__ float4 sW[kChunk * kOctTexels / 4];
   const int tg = threadIdx.x & 15;  // texels 4tg .. 4tg+3
@@ -189,20 +187,38 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
 
 }  // namespace
 
-long long convGroups(const GridGPU& g, int layerBegin, int layerEnd) {
-  return ((long long)(layerEnd - layerBegin) * g.X * g.Z + kTileProbes - 1) / kTileProbes;
+long long convGroups(const GridGPU& g, int layerBegin, int layerEnd, int tileProbes) {
+  return ((long long)(layerEnd - layerBegin) * g.X * g.Z + tileProbes - 1) / tileProbes;
 }
 
-cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream) {
-  if (numItems <= 0 || totalGroups <= 0) return cudaSuccess;
-  k_conv_weights_batch<<<dim3(kOctTexels, numItems), 256, 0, stream>>>(dItems);
+int convTileProbes(long long probes) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // 32-probe tiles once they fill two waves of 4 blocks per SM, else 16-probe tiles
+  return probes >= 2LL * 4 * sms * 32 ? 32 : 16;
+}
+
+namespace {
+template <bool kSingle, int kPT>
+void launchTiles(const ConvItem* dItems, int numItems, long long tiles, const ConvItem& single, cudaStream_t stream) {
   int dev = 0, sms = 0, perSm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch<false>, kTileThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch<kSingle, kPT>, kTileThreads, 0);
   long long grid = (long long)sms * (perSm > 0 ? perSm : 1);
-  if (grid > totalGroups) grid = totalGroups;
-  k_conv_fp32_batch<false><<<(unsigned)grid, kTileThreads, 0, stream>>>(dItems, numItems, totalGroups, ConvItem{});
+  if (grid > tiles) grid = tiles;
+  k_conv_fp32_batch<kSingle, kPT><<<(unsigned)grid, kTileThreads, 0, stream>>>(dItems, numItems, tiles, single);
+}
+}  // namespace
+
+cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream,
+                                int tileProbes) {
+  if (numItems <= 0 || totalGroups <= 0) return cudaSuccess;
+  if (tileProbes != 16 && tileProbes != 32) return cudaErrorInvalidValue;
+  k_conv_weights_batch<<<dim3(kOctTexels, numItems), 256, 0, stream>>>(dItems);
+  if (tileProbes == 32) launchTiles<false, 4>(dItems, numItems, totalGroups, ConvItem{}, stream);
+  else launchTiles<false, 2>(dItems, numItems, totalGroups, ConvItem{}, stream);
   return cudaGetLastError();
 }
 
@@ -226,14 +242,10 @@ cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* 
   it.hysteresis = hysteresis;
   it.flags = flags;
   it.groupBegin = 0;
-  const long long tiles = convGroups(g, layerBegin, layerEnd);
-  int dev = 0, sms = 0, perSm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_conv_fp32_batch<true>, kTileThreads, 0);
-  long long grid = (long long)sms * (perSm > 0 ? perSm : 1);
-  if (grid > tiles) grid = tiles;
-  k_conv_fp32_batch<true><<<(unsigned)grid, kTileThreads, 0, stream>>>(nullptr, 1, tiles, it);
+  const int tp = convTileProbes((long long)(layerEnd - layerBegin) * g.X * g.Z);
+  const long long tiles = convGroups(g, layerBegin, layerEnd, tp);
+  if (tp == 32) launchTiles<true, 4>(nullptr, 1, tiles, it, stream);
+  else launchTiles<true, 2>(nullptr, 1, tiles, it, stream);
   return cudaGetLastError();
 }
 

@@ -60,9 +60,12 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
 // Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's
 // visibility mask along shadowDir. counter: one device word of scratch. recordIds: DdgiHit.triangle holds the
 // hit's triangle record (BVH order) instead of its global id.
+// light: with `points`, run them in light's light-space shadow BVH (light->shadow, sheared by light->shear*) along
+// +z instead of `bvh`; shadowDir must be the normalised direction toward the light it was built for.
 cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
                             DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
-                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds = false);
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds = false,
+                            const SceneGPU* light = nullptr);
 // Ambient term of G-buffer points from an atlas (deferred_tiled.comp:263-299), CLAMP_TO_EDGE sampling.
 cudaError_t launchQueryIrradiance(const GridGPU& g, const FrameGPU& f, const void* atlas, const DdgiSurfacePoint* pts,
                                   long long count, float4* out, cudaStream_t stream);
@@ -94,8 +97,12 @@ struct ConvItem {
   uint32_t flags;
   long long groupBegin;  // first 32-probe tile of this item
 };
-long long convGroups(const GridGPU& g, int layerBegin, int layerEnd);
-cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream);
+// Tiles of tileProbes (16 or 32) probes of one grid's layer range; convTileProbes: the tile size for a launch
+// over `probes` probes (32 when they fill the GPU twice over, else 16).
+long long convGroups(const GridGPU& g, int layerBegin, int layerEnd, int tileProbes = 16);
+int convTileProbes(long long probes);
+cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream,
+                                int tileProbes = 16);
 
 // Tensor-core convolution (conv_tc.cu). rad16: planar 16-bit radiance (elemFmt 0 FP16, 1 BF16), row
 // c * pTotal + p; N a multiple of 64. scratch: tcScratchBytes(N) bytes (16-bit weights + two sum rows).

@@ -624,11 +624,14 @@ __global__ void __launch_bounds__(256) k_shadow_resolve(const __grid_constant__ 
 // Ray queries (DdgiRay -> DdgiHit) on the persistent refill loop of the probe traversal. kShadowMask:
 // the rays are shadow.rgen's (origin = the point, direction = -lightDir, [0.1, 50], any hit) and the output
 // is its visibility mask; points with w != 0 are sky pixels (visibility 1, no ray).
-template <bool kWide, bool kAnyHit, bool kShadowMask>
+// kLightSpace (with kShadowMask): the points' rays run in the light-space BVH `bvh` along +z, each point
+// sheared by (shK, shS) as the probe update's shadow rays are; shadowDir must then be the normalised
+// direction toward the light that the BVH was sheared for.
+template <bool kWide, bool kAnyHit, bool kShadowMask, bool kLightSpace = false>
 __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
     k_trace_rays(BvhRef bvh, const DdgiRay* __restrict__ rays, const float4* __restrict__ points, float3 shadowDir,
                  long long count, unsigned long long* __restrict__ counter, int refillLanes, DdgiHit* __restrict__ hits,
-                 float* __restrict__ vis, bool recordIds, uint32_t* __restrict__ err) {
+                 float* __restrict__ vis, bool recordIds, uint32_t* __restrict__ err, int3 shK, float3 shS) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   long long id = -1;
@@ -664,6 +667,12 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
           const float4 p = points[cand];
           o = xyz(p);
           d = shadowDir;
+          if (kLightSpace) {
+            const float pk[3] = {p.x, p.y, p.z};
+            const float pz = pk[shK.z];
+            o = f3(pk[shK.x] - shS.x * pz, pk[shK.y] - shS.y * pz, shS.z * pz);
+            d = f3(0.f, 0.f, 1.f);
+          }
           tmin = kTMin;
           t1 = kTMax;
           sky = p.w != 0.0f;
@@ -688,7 +697,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
     }
     if (id >= 0) {
       bool done;
-      if constexpr (kWide) done = wideStep<kAnyHit>(bvh, ray, tmin, st, hit, err);
+      if constexpr (kWide) done = wideStep<kAnyHit, kLightSpace>(bvh, ray, tmin, st, hit, err);
       else done = binStep<kAnyHit>(bvh, ray, tmin, st, hit, err);
       if (done) {
         finish(id);
@@ -700,8 +709,11 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
 
 cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, long long count, bool anyHit,
                             DdgiHit* hits, const float4* points, float3 shadowDir, float* vis,
-                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds) {
+                            unsigned long long* counter, uint32_t* err, cudaStream_t stream, bool recordIds,
+                            const SceneGPU* light) {
   if (count <= 0) return cudaSuccess;
+  const int3 shK = light ? make_int3(light->shearK[0], light->shearK[1], light->shearK[2]) : make_int3(0, 1, 2);
+  const float3 shS = light ? f3(light->shearS[0], light->shearS[1], light->shearS[2]) : f3(0.f, 0.f, 1.f);
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
@@ -709,15 +721,19 @@ cudaError_t launchTraceRays(const BvhRef& bvh, bool wide, const DdgiRay* rays, l
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = sms * 8;
   const int refill = 8;
-  if (points) {  // shadow mask: any hit
-    if (wide) k_trace_rays<true, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err);
-    else k_trace_rays<false, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err);
+  if (points && light) {  // shadow mask in the light-space BVH
+    const BvhRef& lb = light->shadow;
+    if (wide) k_trace_rays<true, true, true, true><<<blocks, kTraceThreads, 0, stream>>>(lb, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err, shK, shS);
+    else k_trace_rays<false, true, true, true><<<blocks, kTraceThreads, 0, stream>>>(lb, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err, shK, shS);
+  } else if (points) {  // shadow mask: any hit
+    if (wide) k_trace_rays<true, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err, shK, shS);
+    else k_trace_rays<false, true, true><<<blocks, kTraceThreads, 0, stream>>>(bvh, nullptr, points, shadowDir, count, counter, refill, nullptr, vis, recordIds, err, shK, shS);
   } else if (anyHit) {
-    if (wide) k_trace_rays<true, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
-    else k_trace_rays<false, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
+    if (wide) k_trace_rays<true, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err, shK, shS);
+    else k_trace_rays<false, true, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err, shK, shS);
   } else {
-    if (wide) k_trace_rays<true, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
-    else k_trace_rays<false, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err);
+    if (wide) k_trace_rays<true, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err, shK, shS);
+    else k_trace_rays<false, false, false><<<blocks, kTraceThreads, 0, stream>>>(bvh, rays, nullptr, shadowDir, count, counter, refill, hits, nullptr, recordIds, err, shK, shS);
   }
   return cudaGetLastError();
 }
@@ -870,10 +886,13 @@ cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f,
                                   err, stream, true);
   if (e != cudaSuccess) return e;
   k_mirror_shade<<<(unsigned)blocks, 256, 0, stream>>>(s, g, f, atlas, pts, hits, count, out, dark, spts);
-  // the shadow ray of rchit:45-66: normalize(-lightDir) over [0.1, 50], terminating on the first hit
+  // the shadow ray of rchit:45-66: normalize(-lightDir) over [0.1, 50], terminating on the first hit; in the
+  // light-space BVH when the scene carries one for this light (the caller makes sure it matches)
   const float3 ld = f.lightDir * -1.0f;
   const float3 sdir = ld * (1.0f / sqrtf(ld.x * ld.x + ld.y * ld.y + ld.z * ld.z));
-  e = launchTraceRays(s.bvh, wide, nullptr, count, true, nullptr, spts, sdir, vis, counter, err, stream, false);
+  const bool lightSpace = s.shadow.tris != nullptr;
+  e = launchTraceRays(s.bvh, lightSpace ? s.shadow.wnodes != nullptr : wide, nullptr, count, true, nullptr, spts,
+                      sdir, vis, counter, err, stream, false, lightSpace ? &s : nullptr);
   if (e != cudaSuccess) return e;
   k_mirror_resolve<<<(unsigned)blocks, 256, 0, stream>>>(vis, dark, out, count);
   return cudaGetLastError();

@@ -51,11 +51,13 @@ def _points_on_triangles(arrays, n, seed):
 
 @pytest.mark.parametrize("options", [0, L.DDGI_GRID_EDGE_CLAMP])
 @pytest.mark.parametrize("flags", [L.DDGI_UBO_DDGI_FLAG, 0])
-def test_mirror_matches_oracle(ctx, options, flags):
+@pytest.mark.parametrize("shadow_mode", [1, 0])  # shadow rays in the light-space BVH, or the scene BVH
+def test_mirror_matches_oracle(ctx, options, flags, shadow_mode):
     w = scenes.CPU_REFERENCE
     arrays = scenes.build_scene(w)
     scene = ddgi.Scene(ctx, arrays)
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=options)
+    grid.set_tuning(shadow_mode=shadow_mode)
     osc = oracle.OracleScene(arrays, L.SceneDesc)
     try:
         b = grid.buffers

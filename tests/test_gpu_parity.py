@@ -114,8 +114,9 @@ def test_convolve_fp32(ctx, n, bake):
 
 # ---- full update: trace + shade + convolve against the oracle ---------------------------------------
 
-def _run_lockstep(ctx, w, frames, options=0, layer=-1, fmt=L.DDGI_FORMAT_RGBA32F, check_rays=True, tuning=None):
-    arrays = scenes.build_scene(w)
+def _run_lockstep(ctx, w, frames, options=0, layer=-1, fmt=L.DDGI_FORMAT_RGBA32F, check_rays=True, tuning=None,
+                  arrays=None):
+    arrays = arrays if arrays is not None else scenes.build_scene(w)
     scene = ddgi.Scene(ctx, arrays)
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, atlas_format=fmt,
                           options=options | L.DDGI_GRID_RECORD_HITS)
@@ -467,3 +468,18 @@ def test_seeded_closest_hits_equal_unseeded(ctx, bvh_width):
     finally:
         seeded.close()
         scene.close()
+
+
+def test_dark_materials_take_the_vertex_colour(ctx):
+    """Materials whose base colour factor sums to <= 0.1 are shaded with the interpolated vertex colour in
+    linear space (getSurfaceDataFromMat, bindless.glsl:199-203): half the materials of the 4096-triangle
+    workload set to a black base colour, the traced rays and the atlas against the oracle."""
+    w = scenes.CPU_REFERENCE
+    arrays = scenes.build_scene(w)
+    arrays.materials["baseColFac"][::2, :3] = 0.0
+    atlas, want, stats = _run_lockstep(ctx, w, 3, arrays=arrays)
+    for s in stats:
+        assert s["hit_mismatch"] == 0, s
+        assert s["ray_err_max"] <= (1e-4 if s["prev_equal"] else 1e-2), s
+    err = rel_err(atlas, want, 1e-3)
+    assert np.percentile(err, 99.9) <= 1e-3, np.percentile(err, [50, 99, 99.9, 100])
