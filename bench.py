@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -66,8 +67,7 @@ class ClockSampler:
 
     def start(self):
         try:
-            self.out = open(ROOT / "gpurun_out" / f".clocks_{os.getpid()}.csv", "w") if (ROOT / "gpurun_out").exists() \
-                else open(f"/tmp/.clocks_{os.getpid()}.csv", "w")
+            self.out = open(Path(tempfile.gettempdir()) / f".ddgi_clocks_{os.getpid()}.csv", "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
                                          stderr=subprocess.DEVNULL)
