@@ -43,7 +43,7 @@ extern "C" {
 #define DDGI_ENOMEM       -2   /* device or host allocation failed                                   */
 #define DDGI_ETIMEDOUT    -3   /* a bounded device wait gave up                                       */
 #define DDGI_EDEVICE      -4   /* CUDA runtime error                                                  */
-#define DDGI_EUNSUPPORTED -5   /* feature not available in this build (e.g. textured materials)      */
+#define DDGI_EUNSUPPORTED -5   /* feature this library does not support (e.g. textured materials)     */
 #define DDGI_EOVERFLOW    -6   /* a device-side bound was hit (traversal stack); work was skipped     */
 #define DDGI_EBUSY        -7   /* admission refused (serving: memory budget / slots)                  */
 

@@ -1,7 +1,7 @@
 // ORACLE — test infrastructure only, never part of the product path.
 //
-// FP64 CPU restatement of AneRend's DDGI probe update, used by the tests as the checker and by the
-// benchmark as the timed CPU baseline. Each function names the reference lines it follows:
+// FP64 CPU restatement of AneRend's DDGI probe update, the parity reference of the tests and the
+// benchmark's timed CPU baseline. Each function names the reference lines it follows:
 //   ray generation      assets/shaders/irradiance_probe_update.rgen:35-111
 //   hit shading         assets/shaders/irradiance_probe_update.rchit:134-221, .rmiss:17-21
 //   lighting / lookup   assets/shaders/pbr_light.glsl:10-43, 88-166, 168-388
