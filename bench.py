@@ -542,7 +542,7 @@ def run_ours(args, rank, local, world):
     probe_grid.close()
 
     grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
-    grid.set_tuning(warp_probes=2, ray_order=1, shadow_mode=1, conv_mode=0, bvh_width=args.bvh_width,
+    grid.set_tuning(warp_probes=args.warp_probes, ray_order=1, shadow_mode=1, conv_mode=0, bvh_width=args.bvh_width,
                     refill_lanes=args.refill_lanes)  # FP32 throughout
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     rays_per_step = w.probes * w.rays
@@ -674,6 +674,7 @@ def main():
     ap.add_argument("--form", choices=["precision", "batched"], help="run only this form and print its measurements")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal tree (8-wide or binary)")
     ap.add_argument("--refill-lanes", type=int, default=8, help="idle lanes before a traversal warp refills (1..32)")
+    ap.add_argument("--warp-probes", type=int, default=2, help="probes per traversal warp (1, 2, 4, ... 32)")
     args = ap.parse_args()
     rank, local, world = dist_init()
     if args.impl == "reference":
