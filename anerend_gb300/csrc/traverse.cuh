@@ -37,6 +37,18 @@ DDGI_D float min3f(float a, float b, float c) {
   asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
 }
+// Two round-to-nearest FMAs in one packed FP32 instruction: (a.x b.x + c.x, a.y b.y + c.y), each the same
+// value fmaf gives.
+DDGI_D float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long A, B, C, D;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(B) : "f"(b.x), "f"(b.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(C) : "f"(c.x), "f"(c.y));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(D) : "l"(A), "l"(B), "l"(C));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(D));
+  return d;
+}
 #else
 // host builds must compile with -ffp-contract=off so products and differences round separately
 inline float mulRn(float a, float b) { return a * b; }
@@ -58,6 +70,7 @@ inline uint32_t bytePerm(uint32_t x, uint32_t y, uint32_t sel) {
 inline void flagError(uint32_t* err, uint32_t bits) { if (err) *err |= bits; }
 inline float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
 inline float min3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
+inline float2 fma2(float2 a, float2 b, float2 c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
 #endif
 
 struct WRay {
@@ -425,9 +438,11 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
       in = vnx <= Rv[0] + 4.76837158203125e-7f && vfx >= Rv[0] - 4.76837158203125e-7f &&
            vny <= Rv[1] + 4.76837158203125e-7f && vfy >= Rv[1] - 4.76837158203125e-7f &&
            fmaxf(fmaf(vnz, A[2], Bn[2]), tmin) <= fminf(fmaf(vfz, A[2], Bf[2]), hit.t) * 1.0000004f;
-    } else {
-      const float tn = max3f(fmaf(vnx, A[0], Bn[0]), fmaf(vny, A[1], Bn[1]), fmaxf(fmaf(vnz, A[2], Bn[2]), tmin));
-      const float tf = min3f(fmaf(vfx, A[0], Bf[0]), fmaf(vfy, A[1], Bf[1]), fminf(fmaf(vfz, A[2], Bf[2]), hit.t));
+    } else {  // x and y planes as one packed FMA each for the near and far sides
+      const float2 tnxy = fma2(make_float2(vnx, vny), make_float2(A[0], A[1]), make_float2(Bn[0], Bn[1]));
+      const float2 tfxy = fma2(make_float2(vfx, vfy), make_float2(A[0], A[1]), make_float2(Bf[0], Bf[1]));
+      const float tn = max3f(tnxy.x, tnxy.y, fmaxf(fmaf(vnz, A[2], Bn[2]), tmin));
+      const float tf = min3f(tfxy.x, tfxy.y, fminf(fmaf(vfz, A[2], Bf[2]), hit.t));
       in = tn <= tf * 1.0000004f;
     }
     hm |= (in ? 1u : 0u) << c;
