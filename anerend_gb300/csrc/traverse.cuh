@@ -49,6 +49,25 @@ DDGI_D float2 fma2(float2 a, float2 b, float2 c) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(D));
   return d;
 }
+// Two round-to-nearest products / differences in one packed FP32 instruction (never contracted).
+DDGI_D float2 mul2(float2 a, float2 b) {
+  unsigned long long A, B, D;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(B) : "f"(b.x), "f"(b.y));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(D) : "l"(A), "l"(B));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(D));
+  return d;
+}
+DDGI_D float2 sub2(float2 a, float2 b) {
+  unsigned long long A, B, D;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(B) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(D) : "l"(A), "l"(B));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(D));
+  return d;
+}
 #else
 // host builds must compile with -ffp-contract=off so products and differences round separately
 inline float mulRn(float a, float b) { return a * b; }
@@ -71,6 +90,8 @@ inline void flagError(uint32_t* err, uint32_t bits) { if (err) *err |= bits; }
 inline float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
 inline float min3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
 inline float2 fma2(float2 a, float2 b, float2 c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
+inline float2 mul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+inline float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 #endif
 
 struct WRay {
@@ -120,14 +141,15 @@ DDGI_HD bool intersectTri(const WRay& r, float3 v0, float3 v1, float3 v2, float 
                           float& b1, float& b2) {
   float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
   float Akz = get(A, r.kz), Bkz = get(B, r.kz), Ckz = get(C, r.kz);
-  float Ax = subRn(get(A, r.kx), mulRn(r.Sx, Akz));
-  float Ay = subRn(get(A, r.ky), mulRn(r.Sy, Akz));
-  float Bx = subRn(get(B, r.kx), mulRn(r.Sx, Bkz));
-  float By = subRn(get(B, r.ky), mulRn(r.Sy, Bkz));
-  float Cx = subRn(get(C, r.kx), mulRn(r.Sx, Ckz));
-  float Cy = subRn(get(C, r.ky), mulRn(r.Sy, Ckz));
-  float U = subRn(mulRn(Cx, By), mulRn(Cy, Bx));
-  float V = subRn(mulRn(Ax, Cy), mulRn(Ay, Cx));
+  // the sheared x and y of each vertex, and two of the three edge functions, as packed pairs: the same
+  // separately rounded products and differences
+  const float2 S = make_float2(r.Sx, r.Sy);
+  const float2 Axy = sub2(make_float2(get(A, r.kx), get(A, r.ky)), mul2(S, make_float2(Akz, Akz)));
+  const float2 Bxy = sub2(make_float2(get(B, r.kx), get(B, r.ky)), mul2(S, make_float2(Bkz, Bkz)));
+  const float2 Cxy = sub2(make_float2(get(C, r.kx), get(C, r.ky)), mul2(S, make_float2(Ckz, Ckz)));
+  const float Ax = Axy.x, Ay = Axy.y, Bx = Bxy.x, By = Bxy.y, Cx = Cxy.x, Cy = Cxy.y;
+  const float2 UV = sub2(mul2(make_float2(Cx, Ax), make_float2(By, Cy)), mul2(make_float2(Cy, Ay), make_float2(Bx, Cx)));
+  float U = UV.x, V = UV.y;
   float W = subRn(mulRn(Bx, Ay), mulRn(By, Ax));
   if (U == 0.0f || V == 0.0f || W == 0.0f) {  // exact fallback of the paper
     U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
