@@ -209,9 +209,14 @@ def rotation(seed: int, frame: int) -> np.ndarray:
 
 
 def camera(w: Workload, frame: int) -> tuple:
-    if w.move_every:
-        return (float(frame // w.move_every), 0.0, 0.0)
-    return (0.0, 0.0, 0.0)
+    """Camera position of a frame: +1 in x every `move_every` frames over the workload's `frames`, then back
+    (-1 every `move_every` frames) over as many, and so on. Frames past the first run keep the camera within
+    the first run's positions, so a run of any length sees the same scene coverage and only ±1 translations."""
+    if not w.move_every:
+        return (0.0, 0.0, 0.0)
+    legs = max(1, w.frames // w.move_every)  # positions 0 .. legs - 1 on the way out
+    p = (frame // w.move_every) % (2 * legs)
+    return (float(p if p < legs else 2 * legs - 1 - p), 0.0, 0.0)
 
 
 @dataclass

@@ -2,7 +2,8 @@
 
 One step = one probe update of the whole grid: translation (when the camera's probe index changes), the
 rotated golden-angle lattice, trace + shade of all 2,097,152 rays, and the convolution + hysteresis of all
-8192 probes. The camera moves +1 in x every 10 frames, as in the workload definition.
+8192 probes. The camera moves +1 in x every 10 frames over the workload's 60 frames, as in the workload
+definition, then back and forth over the same positions, so a long run stays within the same scene.
 
   value      probe rays/s, device-timed (CUDA events on the launching stream), inputs resident in HBM
   e2e        the same metric through the C ABI from the host: ddgi_update + ddgi_atlas_download into pinned
@@ -21,6 +22,7 @@ reported."""
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -54,9 +56,12 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples (every 200 ms) during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Each sample carries nvidia-smi's timestamp; stop(t0, t1) keeps the samples taken between the wall-clock
+    times t0 and t1 (time.time()) of the timed region, or all samples if none fell inside it."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -71,10 +76,35 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
                                          stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # nvidia-smi start-up, so its samples cover the whole timed region
         except (OSError, FileNotFoundError):
             self.proc = None
 
-    def stop(self):
+    @staticmethod
+    def parse(lines, t0=None, t1=None):
+        """Summary of sample lines: median SM clock, max clock, active slowdown reasons, sample counts."""
+        rows = []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                sm, smax = float(f[2]), float(f[3])
+            except ValueError:
+                continue
+            rows.append((ts, sm, smax, {nm for nm, v in zip(names, f[6:10]) if v.lower() == "active"}))
+        inside = [r for r in rows if t0 is not None and t0 <= r[0] <= t1]
+        use = inside or rows
+        if not use:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0,
+                    "samples_in_region": 0}
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": use[-1][2],
+                "reasons": sorted(set().union(*(r[3] for r in use))), "samples": len(use),
+                "samples_in_region": len(inside)}
+
+    def stop(self, t0=None, t1=None):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         self.proc.terminate()
@@ -82,22 +112,7 @@ class ClockSampler:
         self.out.close()
         lines = Path(self.out.name).read_text().strip().splitlines()
         Path(self.out.name).unlink(missing_ok=True)
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                smax = float(f[2])
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return self.parse(lines, t0, t1)
 
 
 def dist_init():
@@ -563,6 +578,7 @@ def run_ours(args, rank, local, world):
     barrier(world)
     torch.cuda.synchronize()
     sampler.start()
+    t_region0 = time.time()
     t_wall0 = time.perf_counter()
     for s in range(args.steps):
         flush.zero_()
@@ -580,8 +596,9 @@ def run_ours(args, rank, local, world):
         f += 1
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
+    t_region1 = time.time()
     barrier(world)
-    clocks = sampler.stop()
+    clocks = sampler.stop(t_region0, t_region1)
     ctx.sync(stream)
     step_ms = [e[0].elapsed_time(e[3]) for e in ev]
     trace_ms = [e[1].elapsed_time(e[2]) for e in ev]
@@ -666,7 +683,8 @@ def run_ours(args, rank, local, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    # 600 updates are about 1 s of device time: enough 200 ms clock samples inside the timed region
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
