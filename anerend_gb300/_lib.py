@@ -164,6 +164,8 @@ SIGNATURES = {
     "ddgi_convolve": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p]),
     "ddgi_update": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Frame), C.c_void_p]),
     "ddgi_atlas_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "ddgi_atlas_download_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "ddgi_atlas_download_wait": (C.c_int, [C.c_void_p]),
     "ddgi_atlas_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ddgi_rays_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ddgi_atlas_export_rgba16f": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),

@@ -377,6 +377,11 @@ void gridDestroy(DdgiGrid* g) {
   cudaFree(g->dQueue);
   cudaFree(g->dHits);
   cudaFree(g->dConv);
+  if (g->dlDone) cudaEventSynchronize(g->dlDone);  // no copy to the host still reads the staging buffer
+  cudaFree(g->dlStage);
+  if (g->dlSnap) cudaEventDestroy(g->dlSnap);
+  if (g->dlDone) cudaEventDestroy(g->dlDone);
+  if (g->dlStream) cudaStreamDestroy(g->dlStream);
   g->ring.release();
   delete g;
 }
@@ -839,6 +844,39 @@ int ddgi_atlas_download(DdgiGrid* g, void* host, uint64_t bytes, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   CK(cudaMemcpyAsync(host, g->atlas[g->cur], bytes, cudaMemcpyDeviceToHost, st), "atlas download");
   CK(cudaStreamSynchronize(st), "atlas download sync");
+  return DDGI_OK;
+}
+
+int ddgi_atlas_download_async(DdgiGrid* g, void* host, uint64_t bytes, void* stream) {
+  if (!g || !host) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_download_async");
+  DdgiContext* ctx = g->ctx;
+  if (bytes != g->atlasBytes) return fail(ctx, DDGI_EINVAL, "atlas is %llu bytes, got %llu",
+                                          (unsigned long long)g->atlasBytes, (unsigned long long)bytes);
+  if (!g->dlStage) {
+    CK(cudaMalloc(&g->dlStage, g->atlasBytes), "atlas download staging");
+    CK(cudaStreamCreateWithFlags(&g->dlStream, cudaStreamNonBlocking), "atlas download stream");
+    CK(cudaEventCreateWithFlags(&g->dlSnap, cudaEventDisableTiming), "atlas download event");
+    CK(cudaEventCreateWithFlags(&g->dlDone, cudaEventDisableTiming), "atlas download event");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  // the staging buffer is free once the previous copy to the host has ended
+  if (g->dlPending) CK(cudaStreamWaitEvent(st, g->dlDone, 0), "atlas download order");
+  CK(cudaMemcpyAsync(g->dlStage, g->atlas[g->cur], bytes, cudaMemcpyDeviceToDevice, st), "atlas snapshot");
+  CK(cudaEventRecord(g->dlSnap, st), "atlas snapshot event");
+  CK(cudaStreamWaitEvent(g->dlStream, g->dlSnap, 0), "atlas download order");
+  CK(cudaMemcpyAsync(host, g->dlStage, bytes, cudaMemcpyDeviceToHost, g->dlStream), "atlas download");
+  CK(cudaEventRecord(g->dlDone, g->dlStream), "atlas download event");
+  g->dlPending = true;
+  return DDGI_OK;
+}
+
+int ddgi_atlas_download_wait(DdgiGrid* g) {
+  if (!g) return fail(nullptr, DDGI_EINVAL, "NULL argument to ddgi_atlas_download_wait");
+  DdgiContext* ctx = g->ctx;
+  if (g->dlPending) {
+    CK(cudaEventSynchronize(g->dlDone), "atlas download wait");
+    g->dlPending = false;
+  }
   return DDGI_OK;
 }
 

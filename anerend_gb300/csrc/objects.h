@@ -120,6 +120,12 @@ struct DdgiGrid {
   float4* dShadow = nullptr;             // then the shadow list)
   ConvItem* dConv = nullptr;
   StagingRing ring;
+  // asynchronous atlas download (allocated on first use): a stream-ordered device snapshot of the atlas,
+  // copied to the host on dlStream after dlSnap; dlDone marks the end of the last copy to the host
+  void* dlStage = nullptr;
+  cudaStream_t dlStream = nullptr;
+  cudaEvent_t dlSnap = nullptr, dlDone = nullptr;
+  bool dlPending = false;
 };
 
 namespace ddgi {

@@ -209,6 +209,17 @@ class ProbeGrid:
         self.ctx.check(self.ctx.lib.ddgi_atlas_download(self.handle, _ptr(out), out.nbytes, stream))
         return out
 
+    def download_atlas_async(self, out, stream: int = 0) -> None:
+        """Start a readback of the atlas into `out` (a contiguous host array or pinned torch tensor of
+        atlasBytes, kept alive by the caller); it is complete once wait_download() returns."""
+        ptr = out.data_ptr() if hasattr(out, "data_ptr") else _ptr(out)
+        nbytes = out.numel() * out.element_size() if hasattr(out, "element_size") else out.nbytes
+        self.ctx.check(self.ctx.lib.ddgi_atlas_download_async(self.handle, ptr, nbytes, stream))
+
+    def wait_download(self) -> None:
+        """Block until every readback started with download_atlas_async has reached the host."""
+        self.ctx.check(self.ctx.lib.ddgi_atlas_download_wait(self.handle))
+
     def upload_atlas(self, arr: np.ndarray, stream: int = 0) -> None:
         arr = np.ascontiguousarray(arr)
         self.ctx.check(self.ctx.lib.ddgi_atlas_upload(self.handle, _ptr(arr), arr.nbytes, stream))

@@ -247,6 +247,16 @@ int  ddgi_update(DdgiGrid* grid, const DdgiScene* scene, const DdgiFrame* frame,
 int  ddgi_atlas_download(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
 int  ddgi_atlas_upload(DdgiGrid* grid, const void* host, uint64_t bytes, void* stream);
 
+/* The same readback without waiting (a per-frame readback that overlaps the next update): the atlas as it
+ * stands in `stream`'s order is copied into a device staging buffer, then to `host` on the grid's own copy
+ * stream, so later work on `stream` (the next ddgi_update) runs during the copy to the host. The staging
+ * buffer (atlasBytes of device memory, outside ddgi_grid_footprint) is allocated on the first call. A
+ * further call's snapshot waits on the device until the previous copy to the host has ended. `host` should
+ * be pinned memory; it must stay valid, and is complete, once ddgi_atlas_download_wait returns, which
+ * blocks until every download issued on the grid has reached the host. */
+int  ddgi_atlas_download_async(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
+int  ddgi_atlas_download_wait(DdgiGrid* grid);
+
 /* Baked-atlas persistence in the reference's layout: the atlas as RGBA16F texels, 8 bytes each, width 10 X,
  * height 10 Z Y - the data of the asset::Texture that downloadDDGIAtlas returns (VulkanRenderer.cpp:2706-2771,
  * format RGBA16F_SFLOAT, one mip) - converted from / to the grid's atlas format (round to nearest even).
