@@ -376,7 +376,6 @@ void gridDestroy(DdgiGrid* g) {
   cudaFree(g->dTrace);
   cudaFree(g->dQueue);
   cudaFree(g->dHits);
-  cudaFree(g->dConv);
   if (g->dlDone) cudaEventSynchronize(g->dlDone);  // no copy to the host still reads the staging buffer
   cudaFree(g->dlStage);
   if (g->dlSnap) cudaEventDestroy(g->dlSnap);
@@ -386,7 +385,7 @@ void gridDestroy(DdgiGrid* g) {
   delete g;
 }
 
-// Records of the single-grid launches (ddgi_trace / ddgi_convolve), allocated on first use.
+// Record and scratch of the single-grid trace (ddgi_trace), allocated on first use.
 int ensureSoloRecords(DdgiGrid* g) {
   if (g->dTrace) return DDGI_OK;
   DdgiContext* ctx = g->ctx;
@@ -397,7 +396,6 @@ int ensureSoloRecords(DdgiGrid* g) {
   const long long slots = maxRaySlots(g->g);
   CK(cudaMalloc(&g->dHits, kTraceScratchPerRay * (size_t)slots), "trace scratch");
   g->dShadow = g->dHits + slots;
-  CK(cudaMalloc(&g->dConv, sizeof(ConvItem)), "convolve record");
   CK(g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem))), "record staging");
   return DDGI_OK;
 }
@@ -802,24 +800,11 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
        "tensor-core convolve");
     return DDGI_OK;
   }
-  int rc = ensureSoloRecords(g);
-  if (rc) return rc;
-  int slot = 0;
-  ConvItem& ci = *reinterpret_cast<ConvItem*>(g->ring.acquire(&slot));
-  ci.g = g->g;
-  ci.rayRad = g->rayRad;
-  ci.dirs = g->lattice;
-  ci.wt = g->wt;
-  ci.wsum = g->wsum;
-  ci.atlas = g->atlas[g->cur];
-  ci.layerBegin = b;
-  ci.layerEnd = e;
-  ci.hysteresis = g->desc.hysteresis;
-  ci.flags = frame->flags;
-  ci.groupBegin = 0;
-  CK(g->ring.copy(slot, g->dConv, sizeof(ConvItem), st), "convolve record");
-  const int tp = convTileProbes((long long)(e - b) * g->g.X * g->g.Z);
-  CK(launchConvFp32Batch(g->dConv, 1, convGroups(g->g, b, e, tp), st, tp), "convolve");
+  // the record travels in the kernel parameters (no copy to the device ahead of the launch); the weights
+  // and tile kernels are those of the batched form
+  CK(launchConvWeights(g->g.N, g->lattice, g->wt, g->wsum, st), "convolve weights");
+  CK(launchConvFp32(g->g, g->rayRad, g->wt, g->wsum, g->atlas[g->cur], b, e, g->desc.hysteresis, frame->flags, st),
+     "convolve");
   return DDGI_OK;
 }
 

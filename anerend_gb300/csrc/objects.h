@@ -111,14 +111,13 @@ struct DdgiGrid {
   // allocStream), so creating and freeing them never synchronizes the device
   bool asyncAlloc = false;
   cudaStream_t allocStream = nullptr;
-  // single-item records of the trace and FP32 convolution (the grid runs the batched kernels with one item),
-  // allocated on first use
+  // single-item record of the trace (the grid runs the batched trace kernels with one item), allocated on
+  // first use
   TraceItem* dTrace = nullptr;
   Mat3* dRot = nullptr;
   unsigned long long* dQueue = nullptr;  // kTraceCounters trace counters
   float4* dHits = nullptr;               // trace scratch for every ray slot of the grid (hit records,
   float4* dShadow = nullptr;             // then the shadow list)
-  ConvItem* dConv = nullptr;
   StagingRing ring;
   // asynchronous atlas download (allocated on first use): a stream-ordered device snapshot of the atlas,
   // copied to the host on dlStream after dlSnap; dlDone marks the end of the last copy to the host
