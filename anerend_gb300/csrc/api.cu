@@ -373,7 +373,6 @@ void gridDestroy(DdgiGrid* g) {
   gridFree(g, g->tcScratch);
   gridFree(g, g->wt);
   gridFree(g, g->wsum);
-  cudaFree(g->dTrace);
   cudaFree(g->dQueue);
   cudaFree(g->dHits);
   if (g->dlDone) cudaEventSynchronize(g->dlDone);  // no copy to the host still reads the staging buffer
@@ -381,22 +380,17 @@ void gridDestroy(DdgiGrid* g) {
   if (g->dlSnap) cudaEventDestroy(g->dlSnap);
   if (g->dlDone) cudaEventDestroy(g->dlDone);
   if (g->dlStream) cudaStreamDestroy(g->dlStream);
-  g->ring.release();
   delete g;
 }
 
-// Record and scratch of the single-grid trace (ddgi_trace), allocated on first use.
+// Counters and scratch of the single-grid trace (ddgi_trace), allocated on first use.
 int ensureSoloRecords(DdgiGrid* g) {
-  if (g->dTrace) return DDGI_OK;
+  if (g->dQueue) return DDGI_OK;
   DdgiContext* ctx = g->ctx;
-  // dTrace is followed by the rotation: one staging copy carries both
-  CK(cudaMalloc(&g->dTrace, sizeof(TraceItem) + sizeof(Mat3)), "trace record");
-  g->dRot = reinterpret_cast<Mat3*>(reinterpret_cast<unsigned char*>(g->dTrace) + sizeof(TraceItem));
   CK(cudaMalloc(&g->dQueue, kTraceCounters * sizeof(unsigned long long)), "trace counters");
   const long long slots = maxRaySlots(g->g);
   CK(cudaMalloc(&g->dHits, kTraceScratchPerRay * (size_t)slots), "trace scratch");
   g->dShadow = g->dHits + slots;
-  CK(g->ring.init(std::max(sizeof(TraceItem) + sizeof(Mat3), sizeof(ConvItem))), "record staging");
   return DDGI_OK;
 }
 
@@ -744,9 +738,8 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   // the persistent batched kernels with one item (the same code the batched form runs)
   rc = ensureSoloRecords(g);
   if (rc) return rc;
-  int slot = 0;
-  unsigned char* h = g->ring.acquire(&slot);
-  TraceItem& ti = *reinterpret_cast<TraceItem*>(h);
+  // the record and rotation travel in the kernel parameters: nothing is copied ahead of the launches
+  TraceItem ti{};
   ti.s = view;
   ti.g = gg;
   ti.f = f;
@@ -762,12 +755,11 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   ti.hitMemo = g->hitMemo;
   ti.occMemo = g->occMemo;
   ti.seedOn = g->memoValid ? 1 : 0;
-  Mat3& rot = *reinterpret_cast<Mat3*>(h + sizeof(TraceItem));
+  Mat3 rot;
   memcpy(rot.m, frame->rotation, sizeof(rot.m));
-  CK(g->ring.copy(slot, g->dTrace, sizeof(TraceItem) + sizeof(Mat3), st), "trace record");
-  CK(launchTraceBatch(g->dTrace, g->dRot, 1, g->g.N, traceWarps(gg, f), g->dQueue, g->dHits, g->dShadow,
+  CK(launchTraceBatch(nullptr, nullptr, 1, g->g.N, traceWarps(gg, f), g->dQueue, g->dHits, g->dShadow,
                       ctx->numSms * 8, g->tuning.refillLanes, g->tuning.bvhWidth != 2, g->tuning.shadowMode == 1,
-                      ctx->dErr, st, &ti),
+                      ctx->dErr, st, &ti, &rot),
      "trace");
   g->tracedBegin = b;
   g->tracedEnd = e;

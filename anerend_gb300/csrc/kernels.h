@@ -49,12 +49,13 @@ constexpr int kTraceCounters = 4;
 constexpr size_t kTraceScratchPerRay = 32;
 // Lattices of every item (rotation per item), then the wavefront trace of all items' ray slots:
 // closest-hit traversal, shading, shadow traversal, shadowed-ray resolve. dHits and dShadow hold
-// 32 * totalWarps float4 each. hItems: the host copy of the records; a single record is passed to the
-// wavefront kernels by value (constant-bank reads), otherwise they read dItems.
+// 32 * totalWarps float4 each. hItems / hRot: a single record and its rotation on the host, passed to every
+// kernel by value (constant-bank reads; dItems and dRots are not read), otherwise the kernels read dItems and
+// dRots. The lattice kernel zeroes dCounters, so no copy or memset runs ahead of the launches.
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
-                             const TraceItem* hItems = nullptr);
+                             const TraceItem* hItems = nullptr, const Mat3* hRot = nullptr);
 
 
 // Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's

@@ -111,14 +111,11 @@ struct DdgiGrid {
   // allocStream), so creating and freeing them never synchronizes the device
   bool asyncAlloc = false;
   cudaStream_t allocStream = nullptr;
-  // single-item record of the trace (the grid runs the batched trace kernels with one item), allocated on
-  // first use
-  TraceItem* dTrace = nullptr;
-  Mat3* dRot = nullptr;
+  // counters and scratch of the single-grid trace (the batched trace kernels with one item, its record in
+  // the kernel parameters), allocated on first use
   unsigned long long* dQueue = nullptr;  // kTraceCounters trace counters
   float4* dHits = nullptr;               // trace scratch for every ray slot of the grid (hit records,
   float4* dShadow = nullptr;             // then the shadow list)
-  StagingRing ring;
   // asynchronous atlas download (allocated on first use): a stream-ordered device snapshot of the atlas,
   // copied to the host on dlStream after dlSnap; dlDone marks the end of the last copy to the host
   void* dlStage = nullptr;

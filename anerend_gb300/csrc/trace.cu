@@ -899,8 +899,13 @@ cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f,
 }
 
 // Rotated lattices of many grids: one block row per item.
-__global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3* __restrict__ rots) {
-  const TraceItem& it = items[blockIdx.y];
+// Records from `items` and `rots` in device memory, or `one` and `rotOne` when items is null. Block (0, 0)
+// also zeroes the trace counters, which the wavefront kernels launched after this one use.
+__global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3* __restrict__ rots,
+                                const __grid_constant__ TraceItem one, const __grid_constant__ Mat3 rotOne,
+                                unsigned long long* __restrict__ counters) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < kTraceCounters) counters[threadIdx.x] = 0ull;
+  const TraceItem& it = items ? items[blockIdx.y] : one;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= it.g.N) return;
   double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
@@ -909,7 +914,7 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
   double v[3] = {cos(theta) * sp, sin(theta) * sp, cos(phi)};
   double len = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
   v[0] /= len; v[1] /= len; v[2] /= len;
-  const float* m = rots[blockIdx.y].m;
+  const float* m = items ? rots[blockIdx.y].m : rotOne.m;
   double r[3];
   for (int row = 0; row < 3; ++row)
     r[row] = (double)m[row] * v[0] + (double)m[3 + row] * v[1] + (double)m[6 + row] * v[2];
@@ -920,15 +925,18 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
 // Seed map of the items that seed their closest hits: for each direction of the new lattice the nearest
 // direction of the last traced one (largest dot product, the lowest index on ties). Any choice is exact; a
 // near direction makes the candidate likely to be hit.
-__global__ void k_seed_dirs(const TraceItem* __restrict__ items) {
-  const TraceItem& it = items[blockIdx.y];
+__global__ void k_seed_dirs(const TraceItem* __restrict__ items, const __grid_constant__ TraceItem one) {
+  const TraceItem& it = items ? items[blockIdx.y] : one;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (!it.seedOn || j >= it.g.N) return;
+  // the fields in registers: `it` may be a parameter, read through a generic reference
+  const int n = it.g.N;
+  const float4* __restrict__ prev = it.latticePrev;
   const float4 d = it.lattice[j];
   float best = -3.0f;
   int bi = 0;
-  for (int i = 0; i < it.g.N; ++i) {
-    const float4 q = __ldg(&it.latticePrev[i]);
+  for (int i = 0; i < n; ++i) {
+    const float4 q = __ldg(&prev[i]);
     const float c = d.x * q.x + d.y * q.y + d.z * q.z;
     if (c > best) {
       best = c;
@@ -977,12 +985,15 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
-                             const TraceItem* hItems) {
-  cudaError_t e = cudaMemsetAsync(dCounters, 0, kTraceCounters * sizeof(unsigned long long), stream);
-  if (e != cudaSuccess) return e;
+                             const TraceItem* hItems, const Mat3* hRot) {
+  // one item given on the host with its rotation: every kernel takes it in its parameters, and dItems /
+  // dRots are not read
+  const bool byValue = hItems && hRot && numItems == 1;
+  const TraceItem one = byValue ? hItems[0] : TraceItem{};
+  const Mat3 rotOne = byValue ? *hRot : Mat3{};
   dim3 lg((maxN + 127) / 128, numItems);
-  k_lattice_batch<<<lg, 128, 0, stream>>>(dItems, dRots);
-  k_seed_dirs<<<lg, 128, 0, stream>>>(dItems);
+  k_lattice_batch<<<lg, 128, 0, stream>>>(byValue ? nullptr : dItems, dRots, one, rotOne, dCounters);
+  k_seed_dirs<<<lg, 128, 0, stream>>>(byValue ? nullptr : dItems, one);
   if (totalWarps <= 0) return cudaGetLastError();
   const long long rays = totalWarps * 32;
   if (rays > 0x7fffffffll) return cudaErrorInvalidValue;  // shadow records carry 31-bit slot ids + a flag
@@ -992,7 +1003,7 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long shadeBlocks = (rays + 255) / 256;
   if (shadeBlocks > (long long)sms * 16) shadeBlocks = (long long)sms * 16;
-  if (hItems && numItems == 1) {
+  if (byValue) {
     launchWavefront(ItemsOne{hItems[0]}, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide, lightSpace,
                     err, stream);
   } else {
