@@ -925,18 +925,26 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
 // Seed map of the items that seed their closest hits: for each direction of the new lattice the nearest
 // direction of the last traced one (largest dot product, the lowest index on ties). Any choice is exact; a
 // near direction makes the candidate likely to be hit.
+constexpr int kSeedStageMax = 1024;  // raysPerProbe is at most 1024 (validated when a grid is created)
 __global__ void k_seed_dirs(const TraceItem* __restrict__ items, const __grid_constant__ TraceItem one) {
+  __shared__ float4 sPrev[kSeedStageMax];
   const TraceItem& it = items ? items[blockIdx.y] : one;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!it.seedOn || j >= it.g.N) return;
+  if (!it.seedOn) return;  // the same for the whole block
   // the fields in registers: `it` may be a parameter, read through a generic reference
   const int n = it.g.N;
   const float4* __restrict__ prev = it.latticePrev;
+  // the last traced lattice staged once per block; the scan below reads it from shared memory
+  const bool staged = n <= kSeedStageMax;
+  if (staged)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sPrev[i] = __ldg(&prev[i]);
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
   const float4 d = it.lattice[j];
   float best = -3.0f;
   int bi = 0;
   for (int i = 0; i < n; ++i) {
-    const float4 q = __ldg(&prev[i]);
+    const float4 q = staged ? sPrev[i] : __ldg(&prev[i]);
     const float c = d.x * q.x + d.y * q.y + d.z * q.z;
     if (c > best) {
       best = c;
