@@ -1,7 +1,8 @@
 """ORACLE — test infrastructure only. The reference's DDGI shader stages compiled as FP64 C++ (build_ref.py,
 ref_harness.cpp): ray generation + closest-hit + miss on chosen pixels of one layer's ray image, and the
 convolution on chosen invocations, at the reference's compile-time grid (64 x 8 x 64 probes, 256 rays,
-hysteresis 0.96). Used to pin the oracle restatement (tests/test_oracle_vs_reference_shaders.py) and to
+hysteresis 0.96); and, per G-buffer point, the specular GI mirror pass, the RT shadow pass and the deferred
+pass's DDGI block. Used to pin the oracle restatement (tests/test_oracle_vs_reference_shaders.py) and to
 make the golden fixtures in tests/golden/. Available only where the reference sources are present."""
 from __future__ import annotations
 
@@ -39,6 +40,12 @@ class RefShaders:
         self.lib.ref_convolve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                           C.c_int, C.c_int]
         self.lib.ref_convolve.restype = C.c_int
+        for name in ("ref_mirror", "ref_query_irradiance"):
+            fn = getattr(self.lib, name)
+            fn.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_void_p]
+            fn.restype = C.c_int
+        self.lib.ref_shadow_mask.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        self.lib.ref_shadow_mask.restype = C.c_int
         self._keep = None
 
     def set_scene(self, scene_desc) -> None:
@@ -65,6 +72,35 @@ class RefShaders:
         assert irr.shape == RAY_IMAGE + (4,) and dirs.shape == RAY_IMAGE + (4,)
         assert atlas.dtype == np.float64 and atlas.flags.c_contiguous and atlas.shape == ATLAS + (4,)
         assert self.lib.ref_convolve(C.addressof(frame), layer, _p(irr), _p(dirs), _p(atlas), x0, y0, x1, y1) == 0
+
+
+    def mirror(self, frame, atlas: np.ndarray, points: np.ndarray) -> np.ndarray:
+        """mirror_reflections.rgen on MIRROR_POINT records with `atlas` (FP64, the reference's atlas size) as
+        probeTex: (count, 4) (radiance, hit distance)."""
+        a = np.ascontiguousarray(atlas, np.float64)
+        assert a.shape == ATLAS + (4,)
+        pts = np.ascontiguousarray(points)
+        out = np.zeros((len(pts), 4))
+        assert self.lib.ref_mirror(C.addressof(frame), _p(a), ATLAS[1], ATLAS[0], _p(pts), len(pts), _p(out)) == 0
+        return out
+
+    def shadow_mask(self, frame, points: np.ndarray) -> np.ndarray:
+        """shadow.rgen on float32 (x, y, z, sky) points: the stored visibility per point."""
+        pts = np.ascontiguousarray(points, np.float32)
+        out = np.zeros(len(pts))
+        assert self.lib.ref_shadow_mask(C.addressof(frame), _p(pts), len(pts), _p(out)) == 0
+        return out
+
+    def query_irradiance(self, frame, atlas: np.ndarray, points: np.ndarray) -> np.ndarray:
+        """The deferred pass's DDGI block (doLight with the direct light off) on SURFACE_POINT records with
+        `atlas` as probeTex (CLAMP_TO_EDGE): (count, 3) ambient terms."""
+        a = np.ascontiguousarray(atlas, np.float64)
+        assert a.shape == ATLAS + (4,)
+        pts = np.ascontiguousarray(points)
+        out = np.zeros((len(pts), 3))
+        assert self.lib.ref_query_irradiance(C.addressof(frame), _p(a), ATLAS[1], ATLAS[0], _p(pts), len(pts),
+                                             _p(out)) == 0
+        return out
 
 
 __all__ = ["RefShaders", "build_if_available", "LIB", "DIMS", "STEP", "RAYS", "HYSTERESIS", "RAY_IMAGE", "ATLAS"]

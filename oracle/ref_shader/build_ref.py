@@ -2,35 +2,42 @@
 oracle restatement can be checked against the reference's own shader code.
 
 It reads the stage sources where they lie under the reference tree (assets/shaders/irradiance_probe_update
-.rgen / .rchit / .rmiss and probe_conv.comp, with their includes), rewrites the GLSL declarations into
-C++ over glsl_shim.hpp (every float becomes a double), keeps only the functions each stage's main reaches,
-and writes the result to oracle/_ref/gen/stages.inc. ref_harness.cpp includes it, supplies traceRayEXT
-(the oracle's exact FP64 closest hit decides which triangle a ray hits; the closest-hit or miss stage then
-runs on the payload, as the ray-tracing pipeline would) and exports a small C API. Everything it writes
-goes to oracle/_ref/, which is not committed. Machines without the reference sources build nothing.
+.rgen / .rchit / .rmiss and probe_conv.comp; the specular GI pass mirror_reflections.rgen / .rchit / .rmiss;
+the RT shadow pass shadow.rgen / .rchit / .rmiss; the deferred pass deferred_tiled.comp from its doLight
+function, which holds the DDGI consumer block; with their includes), rewrites the GLSL declarations into
+C++ over glsl_shim.hpp (every float becomes a double), keeps only the functions each stage's entry reaches,
+and writes the result to oracle/_ref/gen/stages.inc. ref_harness.cpp includes it, supplies traceRayEXT per
+pipeline (the oracle's exact FP64 closest hit decides which triangle a ray hits; that pipeline's closest-hit
+or miss stage then runs on the payload, as the ray-tracing pipeline would) and exports a small C API.
+Everything it writes goes to oracle/_ref/, which is not committed. Machines without the reference sources
+build nothing.
 
 The rewrite is mechanical; what it changes, construct by construct:
   #version / #extension                 dropped; #include inlined once per stage
   layout(...) qualifiers                 dropped
   uniform / buffer blocks                a struct type plus one instance; unsized arrays become pointers
   uniform sampler2D / image2D / ...      plain globals of the shim's types (the harness binds them)
-  rayPayloadEXT T p (location L)         a global T p; traceRayEXT(..., L) passes its address
+  shared (compute shaders)               plain globals
+  rayPayloadEXT T p (location L)         a global T p; traceRayEXT(..., L) passes its address to the
+                                         pipeline's dispatcher (traceRay_<pipeline> in the harness)
   rayPayloadInEXT T p                    a pointer set by the harness; uses of p read through it
   hitAttributeEXT vec2 bary              a global the harness sets before the closest-hit stage runs
   out / inout parameters                 references
   T x[n] = T[](a, b, ...)                brace initialisers
   floating literals                      read at their decimal value in FP64 (the shader rounds them to
                                          float32; the comparison isolates arithmetic, see the pin test)
-  main                                   <stage>::stage_main
+  main                                   <stage>::stage_main (a stage entered elsewhere keeps its name)
 """
 from __future__ import annotations
 
+import os
 import re
 import subprocess
 import sys
 from pathlib import Path
 
-REFERENCE = Path("/root/reference")
+# the reference source tree: ANEREND_REFERENCE when set, else where this build environment mounts it
+REFERENCE = Path(os.environ.get("ANEREND_REFERENCE", "/root/reference"))
 SHADERS = REFERENCE / "assets" / "shaders"
 HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
@@ -43,11 +50,19 @@ USING = " ".join(f"using glsl::{f};" for f in (
     "abs", "floor", "fract", "sqrt", "sin", "cos", "acos", "exp", "log", "pow", "max", "min", "mod", "clamp",
     "mix", "dot", "length", "distance", "normalize", "cross", "reflect"))
 
+# stage -> (source, ray-tracing pipeline whose traceRayEXT dispatcher it calls, entry function)
 STAGES = {
-    "rgen": "irradiance_probe_update.rgen",
-    "rchit": "irradiance_probe_update.rchit",
-    "rmiss": "irradiance_probe_update.rmiss",
-    "conv": "probe_conv.comp",
+    "rgen": ("irradiance_probe_update.rgen", "probe", "main"),
+    "rchit": ("irradiance_probe_update.rchit", "probe", "main"),
+    "rmiss": ("irradiance_probe_update.rmiss", "probe", "main"),
+    "conv": ("probe_conv.comp", None, "main"),
+    "mrgen": ("mirror_reflections.rgen", "mirror", "main"),
+    "mrchit": ("mirror_reflections.rchit", "mirror", "main"),
+    "mrmiss": ("mirror_reflections.rmiss", "mirror", "main"),
+    "srgen": ("shadow.rgen", "shadow", "main"),
+    "srchit": ("shadow.rchit", "shadow", "main"),
+    "srmiss": ("shadow.rmiss", "shadow", "main"),
+    "deferred": ("deferred_tiled.comp", None, "doLight"),
 }
 
 
@@ -135,6 +150,7 @@ def _params(head: str) -> str:
 def _decl(text: str, stage: str, payloads: dict, inpayload: list) -> str:
     t = re.sub(r"layout\s*\([^)]*\)\s*", "", text).strip()
     t = re.sub(r"\b(readonly|writeonly|restrict|coherent|volatile)\b\s*", "", t)
+    t = re.sub(r"^shared\s+", "", t)
     if re.match(r"in\s*;$", t):  # local_size declaration of a compute shader
         return ""
     m = re.match(r"(uniform|buffer)\s+(\w+)\s*(\{.*\})\s*(\w+)\s*;$", t, re.S)
@@ -144,6 +160,9 @@ def _decl(text: str, stage: str, payloads: dict, inpayload: list) -> str:
     m = re.match(r"uniform\s+(\w+)\s+(\w+)\s*\[\s*\]\s*;$", t)
     if m:
         return f"{m.group(1)}* {m.group(2)} = nullptr;"
+    m = re.match(r"uniform\s+(\w+)\s+(\w+)\s*\[\s*(\d+)\s*\]\s*;$", t)
+    if m:
+        return f"{m.group(1)} {m.group(2)}[{m.group(3)}];"
     m = re.match(r"uniform\s+(\w+)\s+(\w+)\s*;$", t)
     if m:
         return f"{m.group(1)} {m.group(2)};"
@@ -163,7 +182,7 @@ def _decl(text: str, stage: str, payloads: dict, inpayload: list) -> str:
     return re.sub(r"=\s*\w+\s*\[\s*\d*\s*\]\s*\((.*)\)\s*;$", r"= {\1};", t, flags=re.S)
 
 
-def translate_stage(stage: str, fname: str) -> str:
+def translate_stage(stage: str, fname: str, pipeline: str | None = None, entry: str = "main") -> str:
     src = _strip_comments(_inline(SHADERS / fname, {fname}))
     items = _items(src)
     funcs = {}
@@ -174,8 +193,8 @@ def translate_stage(stage: str, fname: str) -> str:
             funcs.setdefault(name, []).append(it)
             if name not in order:
                 order.append(name)
-    # functions reachable from main
-    need, todo = set(), ["main"]
+    # functions reachable from the entry
+    need, todo = set(), [entry]
     while todo:
         f = todo.pop()
         if f in need or f not in funcs:
@@ -214,7 +233,7 @@ def translate_stage(stage: str, fname: str) -> str:
         cases = " ".join(f"if (loc == {k}) return &{v};" for k, v in sorted(payloads.items()))
         text = text.replace("using namespace glsl;", "using namespace glsl;\nvoid* payloadAt(int loc);", 1)
         text += f"\nvoid* payloadAt(int loc) {{ {cases} return nullptr; }}"
-        text = re.sub(r"\btraceRayEXT\s*\(", "traceRayStage(payloadAt, ", text)
+        text = re.sub(r"\btraceRayEXT\s*\(", f"traceRay_{pipeline}(payloadAt, ", text)
     return text + f"\n}}  // namespace {stage}\n"
 
 
@@ -222,8 +241,8 @@ def generate() -> Path:
     GEN.mkdir(parents=True, exist_ok=True)
     parts = ["// Generated by oracle/ref_shader/build_ref.py from the reference's shader sources. Do not commit.",
              "#define float double"]
-    for stage, fname in STAGES.items():
-        parts.append(translate_stage(stage, fname))
+    for stage, (fname, pipeline, entry) in STAGES.items():
+        parts.append(translate_stage(stage, fname, pipeline, entry))
     parts.append("#undef float")
     out = GEN / "stages.inc"
     out.write_text("\n".join(parts))
@@ -233,7 +252,7 @@ def generate() -> Path:
 def build_if_available(force: bool = False) -> Path | None:
     """Builds oracle/_ref/libddgi_refshader.so when the reference sources are present; returns its path
     or None."""
-    if not (SHADERS / STAGES["rgen"]).is_file():
+    if not (SHADERS / STAGES["rgen"][0]).is_file():
         return None
     deps = [HERE / "build_ref.py", HERE / "glsl_shim.hpp", HERE / "ref_harness.cpp", ORACLE / "ddgi_oracle.cpp"]
     if LIB.exists() and not force and all(p.stat().st_mtime <= LIB.stat().st_mtime for p in deps):

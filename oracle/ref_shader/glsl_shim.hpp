@@ -191,6 +191,12 @@ GLSL_BINOPS(uvec3, uint, 3)
 
 // ---- matrices (column-major, GLSL conventions) --------------------------------------------------------
 struct mat3;
+// mat4x3: 4 columns of 3 rows (gl_ObjectToWorldEXT / gl_WorldToObjectEXT)
+struct mat4x3 {
+  dvec3 c[4];
+  dvec3& operator[](int i) { return c[i]; }
+  const dvec3& operator[](int i) const { return c[i]; }
+};
 struct mat4 {
   dvec4 c[4];
   mat4() {}
@@ -207,17 +213,17 @@ struct mat3 {
   }
   mat3(const dvec3& a, const dvec3& b, const dvec3& d) { c[0] = a; c[1] = b; c[2] = d; }
   explicit mat3(const mat4& m) { for (int i = 0; i < 3; ++i) c[i] = dvec3(m.c[i].x, m.c[i].y, m.c[i].z); }
-  dvec3& operator[](int i) { return c[i]; }
-  const dvec3& operator[](int i) const { return c[i]; }
-};
-// mat4x3: 4 columns of 3 rows (gl_ObjectToWorldEXT / gl_WorldToObjectEXT)
-struct mat4x3 {
-  dvec3 c[4];
+  explicit mat3(const mat4x3& m) { for (int i = 0; i < 3; ++i) c[i] = m.c[i]; }
   dvec3& operator[](int i) { return c[i]; }
   const dvec3& operator[](int i) const { return c[i]; }
 };
 inline dvec3 operator*(const mat3& m, const dvec3& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
 inline dvec4 operator*(const mat4& m, const dvec4& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z + m.c[3] * v.w; }
+inline mat4 operator*(const mat4& a, const mat4& b) {
+  mat4 r;
+  for (int i = 0; i < 4; ++i) r.c[i] = a * b.c[i];
+  return r;
+}
 inline dvec3 operator*(const mat4x3& m, const dvec4& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z + m.c[3] * v.w; }
 inline double dot(const dvec3& a, const dvec3& b);
 inline dvec4 operator*(const dvec3& v, const mat4x3& m) {  // row vector times matrix
@@ -325,7 +331,11 @@ struct image2D {
 struct sampler2D {
   const double* data = nullptr;  // RGBA doubles, row-major
   int w = 0, h = 0;
+  bool clampToEdge = false;      // CLAMP_TO_EDGE addressing instead of REPEAT
 };
+// cube maps appear only in code the compared stages never execute (the deferred pass's point-light shadows)
+struct samplerCube {};
+inline dvec4 texture(const samplerCube&, const dvec3&) { return dvec4(0.0); }
 struct accelerationStructureEXT {};
 
 inline dvec4 imageLoad(const image2D& im, const ivec2& p) {
@@ -339,14 +349,19 @@ inline void imageStore(image2D& im, const ivec2& p, const dvec4& v) {
   t[0] = v.x; t[1] = v.y; t[2] = v.z; t[3] = v.w;
 }
 inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }
-// LINEAR filter, REPEAT addressing, texel centres at (i + 0.5) / size
+// LINEAR filter, REPEAT (or CLAMP_TO_EDGE) addressing, texel centres at (i + 0.5) / size
 inline dvec4 texture(const sampler2D& s, const dvec2& uv) {
   if (!s.data) return dvec4(0.0);
   double tx = uv.x * s.w - 0.5, ty = uv.y * s.h - 0.5;
   double fx0 = std::floor(tx), fy0 = std::floor(ty);
   double fx = tx - fx0, fy = ty - fy0;
   long long x0 = (long long)fx0, y0 = (long long)fy0;
-  auto wrap = [](long long v, int m) { long long r = v % m; return (int)(r < 0 ? r + m : r); };
+  const bool clampEdge = s.clampToEdge;
+  auto wrap = [clampEdge](long long v, int m) {
+    if (clampEdge) return (int)(v < 0 ? 0 : (v >= m ? m - 1 : v));
+    long long r = v % m;
+    return (int)(r < 0 ? r + m : r);
+  };
   int xs[2] = {wrap(x0, s.w), wrap(x0 + 1, s.w)}, ys[2] = {wrap(y0, s.h), wrap(y0 + 1, s.h)};
   double wx[2] = {1.0 - fx, fx}, wy[2] = {1.0 - fy, fy};
   dvec4 r(0.0);

@@ -82,3 +82,61 @@ def conv_inputs(rotation):
     block = np.concatenate([dirs, np.ones((RAYS, 1))], 1).reshape(16, 16, 4)
     dir_img = np.tile(block, (64, 64, 1))
     return np.ascontiguousarray(irr), np.ascontiguousarray(dir_img), dirs
+
+
+def _points_on_triangles(arrays, n: int, stream: int) -> np.ndarray:
+    """n seeded points on the scene's triangles (FP64)."""
+    v = arrays.vertices["d0"][:, :3].astype(np.float64)
+    tri = arrays.indices.reshape(-1, 3)
+    u = [scenes.uniform(SEED, stream + k, n) for k in range(3)]
+    k = (u[0] * len(tri)).astype(np.int64) % len(tri)
+    a, b = u[1].copy(), u[2].copy()
+    flip = a + b > 1
+    a[flip], b[flip] = 1 - a[flip], 1 - b[flip]
+    return v[tri[k, 0]] * (1 - a - b)[:, None] + v[tri[k, 1]] * a[:, None] + v[tri[k, 2]] * b[:, None]
+
+
+def _unit(n: int, stream: int) -> np.ndarray:
+    z = 2.0 * scenes.uniform(SEED, stream, n) - 1.0
+    phi = 2.0 * np.pi * scenes.uniform(SEED, stream + 1, n)
+    r = np.sqrt(1.0 - z * z)
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], 1)
+
+
+def mirror_points(arrays, n: int = 400) -> np.ndarray:
+    """MIRROR_POINT records for the specular GI pass: points on the scene's triangles with seeded normals
+    (not unit length), every 13th a sky pixel."""
+    pts = np.zeros(n, dtype=L.MIRROR_POINT)
+    pts["position"] = _points_on_triangles(arrays, n, 500)
+    pts["normal"] = _unit(n, 510) * (0.5 + scenes.uniform(SEED, 512, n))[:, None]
+    pts["sky"][::13] = 1.0
+    return pts
+
+
+def shadow_points(arrays, n: int = 400) -> np.ndarray:
+    """float32 (x, y, z, sky) points for the RT shadow pass: on the scene's triangles, every 11th a sky pixel."""
+    pts = np.zeros((n, 4), np.float32)
+    pts[:, :3] = _points_on_triangles(arrays, n, 520)
+    pts[::11, 3] = 1.0
+    return pts
+
+
+def surface_points(n: int = 400) -> np.ndarray:
+    """SURFACE_POINT records for the deferred pass's DDGI block: positions in the scene's box (some beyond
+    NUM_PROBES_PER_PLANE * PROBE_STEP.x / 2 = 32 of the camera), seeded normals, materials and shadows."""
+    pts = np.zeros(n, dtype=L.SURFACE_POINT)
+    lo, hi = np.array([-30.0, 0.0, -30.0]), np.array([30.0, 15.0, 30.0])
+    pts["position"] = lo + (hi - lo) * np.stack([scenes.uniform(SEED, 530 + k, n) for k in range(3)], 1)
+    pts["normal"] = _unit(n, 540) * (0.5 + scenes.uniform(SEED, 542, n))[:, None]
+    pts["albedo"] = np.stack([scenes.uniform(SEED, 550 + k, n) for k in range(3)], 1)
+    pts["metallic"] = (scenes.uniform(SEED, 553, n) < 0.3).astype(np.float32)
+    pts["roughness"] = 0.1 + 0.9 * scenes.uniform(SEED, 554, n)
+    pts["shadow"] = np.floor(3.0 * scenes.uniform(SEED, 555, n)) / 2.0  # 0, 0.5 or 1
+    return pts
+
+
+def pass_frames():
+    """(name, FrameParams) of the G-buffer passes: the DDGI flag on and off."""
+    base = dict(camera_pos=(3.7, 1.3, -2.6), light_dir=(-0.3, -1.0, -0.2), sun_intensity=3.0,
+                sky_color=(0.4, 0.5, 0.7), sky_intensity=1.0)
+    return [("ddgi_on", FrameParams(flags=L.DDGI_UBO_DDGI_FLAG, **base)), ("ddgi_off", FrameParams(flags=0, **base))]

@@ -2,7 +2,12 @@
 // sources as FP64 C++ (build_ref.py writes them to oracle/_ref/gen/stages.inc), on the CPU:
 //   ray generation (irradiance_probe_update.rgen main) per ray-image pixel, with traceRayEXT dispatching
 //   to the closest-hit (.rchit) or miss (.rmiss) stage the way the ray-tracing pipeline does, and the
-//   convolution (probe_conv.comp main) per invocation.
+//   convolution (probe_conv.comp main) per invocation;
+//   the specular GI pass (mirror_reflections.rgen / .rchit / .rmiss) and the RT shadow pass (shadow.rgen /
+//   .rchit / .rmiss) per G-buffer point, and the deferred pass's doLight (deferred_tiled.comp) per point with
+//   the direct light switched off, which leaves the ambient term of its DDGI block.
+// A G-buffer point is given to a stage as a one-pixel G-buffer: ubo.invViewProj is the matrix whose only
+// non-zero column is the last one, (point, 1), so calcWorldPos returns the point exactly whatever the depth.
 // Which triangle a ray hits is decided by the oracle's exact FP64 closest hit (ddgi_oracle.cpp, compiled
 // into the same library); the reference's own hit comes from the closed driver BVH and RT hardware. The
 // harness binds the scene records (converted to FP64), the UBO fields, the push constants and the images.
@@ -25,8 +30,14 @@ thread_local mat4x3 gl_ObjectToWorldEXT;
 thread_local mat4x3 gl_WorldToObjectEXT;
 thread_local dvec3 gl_WorldRayOriginEXT;
 
-void traceRayStage(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint mask, uint sbt,
-                   uint stride, uint miss, const dvec3& origin, double tmin, const dvec3& dir, double tmax, int loc);
+// traceRayEXT of each ray-tracing pipeline: the probe update, the specular GI mirror pass, the RT shadow pass
+#define DDGI_TRACE_RAY_DECL(name)                                                                                  \
+  void name(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint mask, uint sbt, uint stride, \
+            uint miss, const dvec3& origin, double tmin, const dvec3& dir, double tmax, int loc);
+DDGI_TRACE_RAY_DECL(traceRay_probe)
+DDGI_TRACE_RAY_DECL(traceRay_mirror)
+DDGI_TRACE_RAY_DECL(traceRay_shadow)
+thread_local uvec3 gl_LocalInvocationID;
 }  // namespace glsl
 
 #include "stages.inc"
@@ -50,6 +61,17 @@ struct Scene {
   std::vector<uint32_t> triOffset;  // first global triangle id of each instance
 };
 Scene g_scene;
+
+// The scene records again for the specular GI and deferred stages (their record types are their own).
+template <class PV, class MI, class MA, class TI>
+struct SceneCopy {
+  std::vector<PV> verts;
+  std::vector<MI> meshes;
+  std::vector<MA> mats;
+  std::vector<TI> tiles;
+};
+SceneCopy<mrchit::PackedVertex, mrchit::MeshInfo, mrchit::MaterialInfo, mrchit::TileInfo> g_mirror;
+SceneCopy<deferred::PackedVertex, deferred::MeshInfo, deferred::MaterialInfo, deferred::TileInfo> g_deferred;
 
 glsl::dvec4 v4(const float* f) { return glsl::dvec4(f[0], f[1], f[2], f[3]); }
 
@@ -92,9 +114,67 @@ void setUbo(UBO& u, const DdgiFrame* f) {
 }  // namespace
 
 namespace glsl {
-// The pipeline's traceRayEXT: closest hit -> the closest-hit stage (unless skipped), miss -> the miss stage.
-void traceRayStage(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint, uint, uint, uint,
-                   const dvec3& origin, double tmin, const dvec3& dir, double tmax, int loc) {
+// The closest hit of the oracle for a traceRayEXT (the shaders' range [0.1, 50]); the instance it belongs to.
+int oracleHit(const dvec3& origin, const dvec3& dir, double b12[2], int* instOut) {
+  const double o[3] = {origin.x, origin.y, origin.z}, d[3] = {dir.x, dir.y, dir.z};
+  double t = 0;
+  int unc = 0;
+  const int gid = oracle_closest_hit(g_scene.oracle, o, d, &t, b12, &unc);
+  if (gid >= 0) {
+    int inst = 0;
+    while (inst + 1 < (int)g_scene.triOffset.size() && g_scene.triOffset[inst + 1] <= (uint32_t)gid) ++inst;
+    *instOut = inst;
+  }
+  return gid;
+}
+
+// The specular GI pipeline's traceRayEXT (mirror_reflections.rchit / .rmiss; its shadow rays skip the closest
+// hit, so a miss clears their shadow flag).
+void traceRay_mirror(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint, uint, uint, uint,
+                     const dvec3& origin, double, const dvec3& dir, double, int loc) {
+  void* payload = payloadAt(loc);
+  double b12[2] = {0, 0};
+  int inst = 0;
+  const int gid = oracleHit(origin, dir, b12, &inst);
+  if (gid < 0) {
+    mrmiss::hitPayload* saved = mrmiss::payload__in;
+    mrmiss::payload__in = static_cast<mrmiss::hitPayload*>(payload);
+    mrmiss::stage_main();
+    mrmiss::payload__in = saved;
+    return;
+  }
+  if (flags & gl_RayFlagsSkipClosestHitShaderEXT) return;
+  const DdgiInstance& in = g_scene.insts[inst];
+  gl_InstanceCustomIndexEXT = (int)(in.material | (in.mesh << 10));
+  gl_PrimitiveID = (int)(gid - g_scene.triOffset[inst]);
+  transforms(in.transform, gl_ObjectToWorldEXT, gl_WorldToObjectEXT);
+  gl_WorldRayOriginEXT = origin;
+  mrchit::bary = dvec2(b12[0], b12[1]);
+  mrchit::payload__in = static_cast<mrchit::hitPayload*>(payload);
+  mrchit::stage_main();  // its shadow ray skips the closest hit: nothing above is overwritten
+}
+
+// The RT shadow pipeline's traceRayEXT (shadow.rchit / .rmiss).
+void traceRay_shadow(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint, uint, uint, uint,
+                     const dvec3& origin, double, const dvec3& dir, double, int loc) {
+  void* payload = payloadAt(loc);
+  double b12[2] = {0, 0};
+  int inst = 0;
+  const int gid = oracleHit(origin, dir, b12, &inst);
+  if (gid < 0) {
+    srmiss::prd__in = static_cast<srmiss::hitPayload*>(payload);
+    srmiss::stage_main();
+    return;
+  }
+  if (flags & gl_RayFlagsSkipClosestHitShaderEXT) return;
+  srchit::prd__in = static_cast<srchit::hitPayload*>(payload);
+  srchit::stage_main();
+}
+
+// The probe update pipeline's traceRayEXT: closest hit -> the closest-hit stage (unless skipped), miss -> the
+// miss stage.
+void traceRay_probe(void* (*payloadAt)(int), const accelerationStructureEXT&, uint flags, uint, uint, uint, uint,
+                    const dvec3& origin, double tmin, const dvec3& dir, double tmax, int loc) {
   (void)tmin;
   (void)tmax;  // the oracle query uses the shaders' range [0.1, 50]
   void* payload = payloadAt(loc);
@@ -133,6 +213,54 @@ void traceRayStage(void* (*payloadAt)(int), const accelerationStructureEXT&, uin
   rchit::bary = savedBary;
 }
 }  // namespace glsl
+
+namespace {
+// g_scene's records in another stage's record types (the same members)
+template <class SC>
+void copyScene(SC& s) {
+  s.verts.resize(g_scene.verts.size());
+  for (size_t i = 0; i < g_scene.verts.size(); ++i) {
+    const auto& v = g_scene.verts[i];
+    s.verts[i].d0 = v.d0; s.verts[i].d1 = v.d1; s.verts[i].d2 = v.d2; s.verts[i].d3 = v.d3; s.verts[i].d4 = v.d4;
+    s.verts[i].d5 = v.d5;
+  }
+  s.meshes.resize(g_scene.meshes.size());
+  for (size_t i = 0; i < g_scene.meshes.size(); ++i) {
+    s.meshes[i].vertexOffset = g_scene.meshes[i].vertexOffset;
+    s.meshes[i].indexOffset = g_scene.meshes[i].indexOffset;
+  }
+  s.mats.resize(g_scene.mats.size());
+  for (size_t i = 0; i < g_scene.mats.size(); ++i) {
+    s.mats[i].baseColFac = g_scene.mats[i].baseColFac;
+    s.mats[i].emissive = g_scene.mats[i].emissive;
+    s.mats[i].bindlessIndices = g_scene.mats[i].bindlessIndices;
+    s.mats[i].metRough = g_scene.mats[i].metRough;
+  }
+  s.tiles.resize(g_scene.tiles.size());
+  for (auto& t : s.tiles) t.ddgiAtlasTex = -1;
+}
+
+// ubo.invViewProj that maps every clip-space point to `p` (its only non-zero column is the last).
+template <class UBO>
+void pointAt(UBO& u, const float p[3]) {
+  u.invViewProj = glsl::mat4(0.0);
+  u.invViewProj.c[3] = glsl::dvec4(p[0], p[1], p[2], 1.0);
+  u.screenWidth = 1;
+  u.screenHeight = 1;
+}
+
+// one-texel images
+struct Texel {
+  double v[4] = {0, 0, 0, 0};
+  void set(double a, double b, double c, double d) { v[0] = a; v[1] = b; v[2] = c; v[3] = d; }
+  glsl::sampler2D sampler() const {
+    glsl::sampler2D s;
+    s.data = v;
+    s.w = s.h = 1;
+    return s;
+  }
+};
+}  // namespace
 
 extern "C" {
 
@@ -177,6 +305,15 @@ int ref_scene_set(const DdgiSceneDesc* d) {
   rchit::meshBuffer.meshes = g_scene.meshes.data();
   rchit::materialBuffer.infos = g_scene.mats.data();
   rchit::tileInfoBuffer.tiles = g_scene.tiles.data();
+  copyScene(g_mirror);
+  mrchit::vertexBuffer.vertices = g_mirror.verts.data();
+  mrchit::indexBuffer.indices = g_scene.indices.data();
+  mrchit::meshBuffer.meshes = g_mirror.meshes.data();
+  mrchit::materialBuffer.infos = g_mirror.mats.data();
+  mrchit::tileInfoBuffer.tiles = g_mirror.tiles.data();
+  copyScene(g_deferred);
+  deferred::materialBuffer.infos = g_deferred.mats.data();
+  deferred::tileInfoBuffer.tiles = g_deferred.tiles.data();
   return 0;
 }
 
@@ -218,6 +355,108 @@ int ref_trace(const DdgiFrame* f, const float rot[9], int layer, const double* a
         irrOut[4 * ((size_t)y * w + x) + c] = irr[4 * ((size_t)(y0 + y) * 1024 + x0 + x) + c];
         dirOut[4 * ((size_t)y * w + x) + c] = dir[4 * ((size_t)(y0 + y) * 1024 + x0 + x) + c];
       }
+  return 0;
+}
+
+// The specular GI pass (mirror_reflections.rgen main) for each DdgiMirrorPoint, with atlas (RGBA FP64,
+// atlasW x atlasH) bound as probeTex with the default REPEAT sampler. out: per point (radiance, hit distance)
+// as the pass stores into ReflectTex.
+int ref_mirror(const DdgiFrame* f, const double* atlas, int atlasW, int atlasH, const DdgiMirrorPoint* pts,
+               int64_t count, double* out) {
+  if (!g_scene.oracle) return -1;
+  setUbo(mrgen::ubo, f);
+  setUbo(mrchit::ubo, f);
+  setUbo(mrmiss::ubo, f);
+  mrchit::probeTex.data = atlas;
+  mrchit::probeTex.w = atlasW;
+  mrchit::probeTex.h = atlasH;
+  mrchit::probeTex.clampToEdge = false;
+  Texel depth, g0, g1, lut, res;
+  glsl::image2D outIm;
+  outIm.data = res.v;
+  outIm.w = outIm.h = 1;
+  for (int64_t i = 0; i < count; ++i) {
+    const DdgiMirrorPoint& p = pts[i];
+    pointAt(mrgen::ubo, p.position);
+    depth.set(p.sky != 0.0f ? 1.0 : 0.5, 0, 0, 0);
+    g0.set(p.normal[0], p.normal[1], p.normal[2], 0.0);
+    g1.set(0, 0, 0, 0);
+    mrgen::depthIm = depth.sampler();
+    mrgen::geom0Im = g0.sampler();
+    mrgen::geom1Im = g1.sampler();
+    mrgen::lutTex = lut.sampler();
+    mrgen::outputIm = outIm;
+    res.set(0, 0, 0, 0);
+    glsl::gl_LaunchIDEXT = glsl::uvec3(0u, 0u, 0u);
+    mrgen::stage_main();
+    for (int c = 0; c < 4; ++c) out[4 * i + c] = res.v[c];
+  }
+  return 0;
+}
+
+// The RT shadow pass (shadow.rgen main, UBO_RT_SHADOWS_FLAG set) for each point: float4 (world position, w != 0
+// a sky pixel). vis: the value the pass stores into its r32f mask.
+int ref_shadow_mask(const DdgiFrame* f, const float* points, int64_t count, double* vis) {
+  if (!g_scene.oracle) return -1;
+  setUbo(srgen::ubo, f);
+  srgen::ubo.flags |= (1u << 3);  // UBO_RT_SHADOWS_FLAG: the pass runs
+  Texel depth, res;
+  glsl::image2D outIm;
+  outIm.data = res.v;
+  outIm.w = outIm.h = 1;
+  for (int64_t i = 0; i < count; ++i) {
+    const float* p = points + 4 * i;
+    pointAt(srgen::ubo, p);
+    depth.set(p[3] != 0.0f ? 1.0 : 0.5, 0, 0, 0);
+    srgen::depth = depth.sampler();
+    srgen::outputIm = outIm;
+    res.set(-1, 0, 0, 0);
+    glsl::gl_LaunchIDEXT = glsl::uvec3(0u, 0u, 0u);
+    srgen::stage_main();
+    vis[i] = res.v[0];
+  }
+  return 0;
+}
+
+// The deferred pass's doLight (deferred_tiled.comp) for each DdgiSurfacePoint with no point lights, no SSAO, no
+// specular GI, exposure 1 and sunIntensity 0, so the stored colour is the ambient term of its DDGI block
+// (deferred_tiled.comp:263-299) plus the zero emissive; the point's shadow comes through the RT shadow mask,
+// atlas (RGBA FP64) is bound as probeTex with the pass's CLAMP_TO_EDGE sampler. out: count x 3 doubles.
+int ref_query_irradiance(const DdgiFrame* f, const double* atlas, int atlasW, int atlasH, const DdgiSurfacePoint* pts,
+                         int64_t count, double* out) {
+  if (!g_scene.oracle) return -1;
+  DdgiFrame fr = *f;
+  fr.sunIntensity = 0.0f;
+  setUbo(deferred::ubo, &fr);
+  deferred::ubo.flags = (f->flags & (1u << 4)) | (1u << 3);  // UBO_DDGI_FLAG as given, UBO_RT_SHADOWS_FLAG
+  deferred::ubo.exposure = 1.0;
+  deferred::probeTex.data = atlas;
+  deferred::probeTex.w = atlasW;
+  deferred::probeTex.h = atlasH;
+  deferred::probeTex.clampToEdge = true;
+  deferred::groupLocalNumIndices = 0;
+  Texel i0, i1, i2, depth, mask, res;
+  glsl::image2D outIm;
+  outIm.data = res.v;
+  outIm.w = outIm.h = 1;
+  for (int64_t i = 0; i < count; ++i) {
+    const DdgiSurfacePoint& p = pts[i];
+    pointAt(deferred::ubo, p.position);
+    i0.set(p.normal[0], p.normal[1], p.normal[2], p.albedo[0]);
+    i1.set(p.albedo[1], p.albedo[2], p.metallic, p.roughness);
+    i2.set(0, 0, 0, 0);
+    depth.set(0.5, 0, 0, 0);
+    mask.set(p.shadow, 0, 0, 0);
+    deferred::im0 = i0.sampler();
+    deferred::im1 = i1.sampler();
+    deferred::im2 = i2.sampler();
+    deferred::depth = depth.sampler();
+    deferred::rtShadowMask = mask.sampler();
+    deferred::outputIm = outIm;
+    res.set(0, 0, 0, 0);
+    deferred::doLight(glsl::ivec2(0, 0));
+    for (int c = 0; c < 3; ++c) out[3 * i + c] = res.v[c];
+  }
   return 0;
 }
 

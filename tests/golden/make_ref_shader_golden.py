@@ -1,11 +1,14 @@
 """Writes tests/golden/ref_shader_pin.npz: outputs of the reference's own DDGI shader code (irradiance_probe
-_update.rgen / .rchit / .rmiss and probe_conv.comp, compiled as FP64 C++ by oracle/ref_shader/build_ref.py
-from the reference sources) on the seeded pin workload of oracle/ref_shader/pin_workload.py.
+_update.rgen / .rchit / .rmiss and probe_conv.comp; mirror_reflections.rgen / .rchit / .rmiss; shadow.rgen /
+.rchit / .rmiss; deferred_tiled.comp's doLight; compiled as FP64 C++ by oracle/ref_shader/build_ref.py from the
+reference sources) on the seeded pin workload of oracle/ref_shader/pin_workload.py.
 
 Run where the reference sources are present:  python tests/golden/make_ref_shader_golden.py
 Per frame (camera_relative, bake_tile) it stores, for every compared rectangle, the traced radiance and
 direction texels (RGB, FP64) and the convolved 8 x 8 interior texels (RGBA, FP64) of the rectangle's
-probes. The oracle is checked against this file by tests/test_oracle_vs_reference_shaders.py on any machine.
+probes; per G-buffer pass frame (DDGI flag on, off) the mirror pass's (radiance, distance), the shadow pass's
+visibility and the deferred DDGI block's ambient term of the workload's points. The oracle is checked against
+this file by tests/test_oracle_vs_reference_shaders.py on any machine.
 """
 from __future__ import annotations
 
@@ -51,6 +54,12 @@ def generate() -> dict:
         for k, rect in enumerate(W.CONV_RECTS):
             ref.convolve(f, layer, irr_img, dir_img, atlas, *rect)
             out[f"{name}/conv{k}/texels"] = np.stack([interior(atlas, layer, px, pz) for px, pz in conv_probes(rect)])
+    mpts, spts, qpts = W.mirror_points(arrays), W.shadow_points(arrays), W.surface_points()
+    for name, fp in W.pass_frames():
+        f = fp.to_c()
+        out[f"{name}/mirror"] = ref.mirror(f, prev, mpts)
+        out[f"{name}/shadow"] = ref.shadow_mask(f, spts)
+        out[f"{name}/consumer"] = ref.query_irradiance(f, prev, qpts)
     return out
 
 

@@ -74,7 +74,7 @@ def oracle_outputs():
 
 def test_fixture_exists_and_is_small():
     assert FIXTURE.exists(), "run tests/golden/make_ref_shader_golden.py where the reference sources are present"
-    assert FIXTURE.stat().st_size < 600_000
+    assert FIXTURE.stat().st_size < 700_000
 
 
 @pytest.mark.parametrize("frame", ["camera_relative", "bake_tile"])
@@ -95,6 +95,39 @@ def test_oracle_matches_reference_code_fixture(oracle_outputs, frame):
     sky = np.where(c < 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4)
     missed = np.all(np.abs(rad - sky) <= 1e-12, axis=1)
     assert 0.05 < missed.mean() < 0.95
+
+
+@pytest.mark.parametrize("frame", ["ddgi_on", "ddgi_off"])
+def test_gbuffer_pass_oracles_match_reference_code_fixture(frame):
+    """The oracle's restatements of the other passes against the reference's own stages (mirror_reflections.rgen
+    / .rchit / .rmiss, shadow.rgen / .rchit / .rmiss, the DDGI block of deferred_tiled.comp's doLight), on the
+    same scene, atlas and seeded G-buffer points; hits are the oracle's exact closest hits on both sides."""
+    gold = np.load(FIXTURE)
+    arrays = W.scene_arrays()
+    fp = dict(W.pass_frames())[frame]
+    f = fp.to_c()
+    prev = W.atlas_prev()
+    osc = oracle.OracleScene(arrays, L.SceneDesc)
+    try:
+        mpts = W.mirror_points(arrays)
+        got, unc = oracle.mirror_reflections(osc, W.grid_desc(), f, prev, mpts)
+        want = gold[f"{frame}/mirror"]
+        assert np.max(rel(got, want)) <= 1e-10
+        sky = mpts["sky"] != 0
+        assert np.all(want[sky] == 0.0) and 0.1 < np.mean(want[~sky, 3] < 1e6) < 0.99  # hits and misses
+        # the RT shadow pass: a ray along -lightDir over [0.1, 50]; lit (1) on a miss, 0 on a hit, sky pixels 1
+        spts = W.shadow_points(arrays)
+        d = -np.array(f.lightDir[:], np.float64)
+        lit = np.array([1.0 if p[3] != 0 or osc.closest_hit(p[:3].astype(np.float64), d)[0] < 0 else 0.0
+                        for p in spts])
+        assert np.array_equal(lit, gold[f"{frame}/shadow"])
+        assert 0.01 < gold[f"{frame}/shadow"].mean() < 0.99  # shadowed and lit points
+        # the deferred pass's ambient term of its DDGI block (CLAMP_TO_EDGE sampler, far points use the sky term)
+        qpts = W.surface_points()
+        got = oracle.query_irradiance(W.grid_desc(), f, prev, qpts)
+        assert np.max(rel(got, gold[f"{frame}/consumer"])) <= 1e-10
+    finally:
+        osc.close()
 
 
 def test_fixture_regenerates_from_reference_sources():
