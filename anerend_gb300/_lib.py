@@ -30,6 +30,7 @@ DDGI_FORMAT_RGBA16F = 1
 DDGI_GRID_EDGE_CLAMP = 1 << 0
 DDGI_GRID_WRITE_DIRS = 1 << 1
 DDGI_GRID_RECORD_HITS = 1 << 2
+DDGI_GRID_RAYS_RGBA16F = 1 << 3
 
 DDGI_ELEM_F16 = 0
 DDGI_ELEM_BF16 = 1
@@ -139,7 +140,20 @@ class GridBuffers(C.Structure):
                 ("rayHit", C.c_void_p), ("lattice", C.c_void_p),
                 ("atlasWidth", C.c_int32), ("atlasHeight", C.c_int32),
                 ("rayWidth", C.c_int32), ("rayHeight", C.c_int32),
-                ("rayBlockW", C.c_int32), ("rayBlockH", C.c_int32), ("atlasBytes", C.c_uint64)]
+                ("rayBlockW", C.c_int32), ("rayBlockH", C.c_int32), ("atlasBytes", C.c_uint64),
+                ("rayBytes", C.c_uint64), ("rayFormat", C.c_int32), ("reserved", C.c_int32)]
+
+
+class WaitConfig(C.Structure):
+    _fields_ = [("spinLimit", C.c_uint32), ("stallTest", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
+ALLOC_HOOK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64)
+
+
+class GridExternal(C.Structure):
+    _fields_ = [("atlas", C.c_void_p), ("atlasTemp", C.c_void_p), ("rayRadiance", C.c_void_p),
+                ("rayDirection", C.c_void_p), ("atlasBytes", C.c_uint64), ("rayBytes", C.c_uint64)]
 
 
 # name -> (restype, argtypes); every symbol include/ddgi.h declares
@@ -149,12 +163,15 @@ SIGNATURES = {
     "ddgi_context_destroy": (None, [C.c_void_p]),
     "ddgi_last_error": (C.c_char_p, [C.c_void_p]),
     "ddgi_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ddgi_context_set_waits": (C.c_int, [C.c_void_p, C.POINTER(WaitConfig)]),
+    "ddgi_context_set_alloc_hook": (C.c_int, [C.c_void_p, ALLOC_HOOK, C.c_void_p]),
     "ddgi_scene_create": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.c_void_p, C.POINTER(C.c_void_p)]),
     "ddgi_scene_destroy": (None, [C.c_void_p]),
     "ddgi_scene_info": (C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
     "ddgi_grid_create": (C.c_int, [C.c_void_p, C.POINTER(GridDesc), C.POINTER(C.c_void_p)]),
     "ddgi_grid_destroy": (None, [C.c_void_p]),
     "ddgi_grid_buffers": (C.c_int, [C.c_void_p, C.POINTER(GridBuffers)]),
+    "ddgi_grid_bind_external": (C.c_int, [C.c_void_p, C.POINTER(GridExternal), C.c_void_p]),
     "ddgi_grid_reset": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ddgi_grid_footprint": (C.c_uint64, [C.POINTER(GridDesc), C.c_int]),
     "ddgi_grid_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),

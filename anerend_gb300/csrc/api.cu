@@ -17,6 +17,7 @@ namespace detail {
 
 namespace {
 cudaError_t gridAlloc(DdgiGrid* g, void** p, size_t bytes) {
+  if (allocRefused(g->ctx, bytes)) return cudaErrorMemoryAllocation;
   if (g->asyncAlloc) return cudaMallocAsync(p, bytes, g->allocStream);
   return cudaMalloc(p, bytes);
 }
@@ -60,7 +61,7 @@ int validateGridDesc(DdgiContext* ctx, const DdgiGridDesc* d) {
   if (d->atlasFormat != DDGI_FORMAT_RGBA32F && d->atlasFormat != DDGI_FORMAT_RGBA16F)
     return fail(ctx, DDGI_EINVAL, "atlasFormat=%d unknown", d->atlasFormat);
   if (!(d->hysteresis >= 0.0f && d->hysteresis <= 1.0f)) return fail(ctx, DDGI_EINVAL, "hysteresis must be in [0,1]");
-  if (d->options & ~(DDGI_GRID_EDGE_CLAMP | DDGI_GRID_WRITE_DIRS | DDGI_GRID_RECORD_HITS))
+  if (d->options & ~(DDGI_GRID_EDGE_CLAMP | DDGI_GRID_WRITE_DIRS | DDGI_GRID_RECORD_HITS | DDGI_GRID_RAYS_RGBA16F))
     return fail(ctx, DDGI_EINVAL, "unknown grid option bits 0x%x", d->options);
   long long aw = (long long)kProbePix * d->dims[0], ah = (long long)kProbePix * d->dims[2] * d->dims[1];
   if (aw * ah > (1ll << 31)) return fail(ctx, DDGI_EINVAL, "atlas too large");
@@ -80,6 +81,7 @@ GridGPU makeGridGPU(const DdgiGridDesc& d) {
   g.atlasH = kProbePix * g.Z * g.Y;
   g.atlasFmt = d.atlasFormat;
   g.rayW = g.bw * g.X;
+  g.rayFmt = (d.options & DDGI_GRID_RAYS_RGBA16F) ? DDGI_FORMAT_RGBA16F : DDGI_FORMAT_RGBA32F;
   g.options = d.options;
   g.warpProbes = 1;
   return g;
@@ -277,8 +279,15 @@ int translateGrid(DdgiGrid* g, const float cameraPos[3], int* moved, cudaStream_
   g->lastProbeIdx[0] = ix;
   g->lastProbeIdx[1] = iz;
   int sx = dx > 0 ? 1 : (dx < 0 ? -1 : 0), sz = dz > 0 ? 1 : (dz < 0 ? -1 : 0);
-  CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, st), "translate");
-  g->cur = 1 - g->cur;
+  if (g->extAtlas || g->extTemp) {
+    // a caller's buffer keeps its role: copy the atlas into the temp, shift it back (the reference's two
+    // copies, IrradianceProbeTranslationPass.cpp:83-168)
+    CK(cudaMemcpyAsync(g->atlas[1], g->atlas[0], g->atlasBytes, cudaMemcpyDeviceToDevice, st), "translation copy");
+    CK(launchTranslate(g->g, g->atlas[1], g->atlas[0], sx, sz, st), "translate");
+  } else {
+    CK(launchTranslate(g->g, g->atlas[g->cur], g->atlas[1 - g->cur], sx, sz, st), "translate");
+    g->cur = 1 - g->cur;
+  }
   if (moved) *moved = 1;
   return DDGI_OK;
 }
@@ -290,10 +299,11 @@ long long maxRaySlots(const GridGPU& g) { return ((long long)g.X * g.Z + 31) * g
 uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds) {
   GridGPU g = makeGridGPU(*d);
   uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
+  uint64_t rayTexel = g.rayFmt == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rays = (uint64_t)g.rayW * g.bh * g.Z * g.Y;
-  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + 16 * rays + 16ull * g.N + 4ull * g.N +
+  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + rayTexel * rays + 16ull * g.N + 4ull * g.N +
                    4ull * g.N * kOctTexels + 4ull * kOctTexels;
-  if (d->options & DDGI_GRID_WRITE_DIRS) bytes += 16 * rays;
+  if (d->options & DDGI_GRID_WRITE_DIRS) bytes += rayTexel * rays;
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
   if (convMode != 0) bytes += 6 * rays + tcScratchBytes(g.N);
   bytes += kTraceScratchPerRay * (uint64_t)maxRaySlots(g);  // the launch's trace scratch for this grid
@@ -317,11 +327,12 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
   g->atlasBytes = (uint64_t)g->g.atlasW * g->g.atlasH * texel;
   g->rayH = g->g.bh * g->g.Z * g->g.Y;
   size_t rayTexels = (size_t)g->g.rayW * g->rayH;
+  g->rayBytes = (uint64_t)rayTexels * (g->g.rayFmt == DDGI_FORMAT_RGBA32F ? 16 : 8);
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = gridAlloc(g, &g->atlas[0], g->atlasBytes);
   if (e == cudaSuccess) e = gridAlloc(g, &g->atlas[1], g->atlasBytes);
-  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->rayRad, 16 * rayTexels);
-  if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = gridAlloc(g, (void**)&g->rayDir, 16 * rayTexels);
+  if (e == cudaSuccess) e = gridAlloc(g, &g->rayRad, g->rayBytes);
+  if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = gridAlloc(g, &g->rayDir, g->rayBytes);
   if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = gridAlloc(g, (void**)&g->rayHit, 4 * rayTexels);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->lattice, 16 * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, sizeof(int) * (size_t)g->g.N);
@@ -335,7 +346,7 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
     if (e == cudaSuccess)
       e = gridAlloc(g, (void**)&g->occMemo, sizeof(int) * (size_t)g->g.X * g->g.Y * g->g.Z * g->g.N);
   }
-  if (e == cudaSuccess) e = cudaMemsetAsync(g->rayRad, 0, 16 * rayTexels, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->rayRad, 0, g->rayBytes, st);
   if (e == cudaSuccess) e = launchClearAtlas(g->g, g->atlas[0], st);
   if (e == cudaSuccess && !asyncAlloc) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
@@ -358,10 +369,11 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
 
 void gridDestroy(DdgiGrid* g) {
   if (!g) return;
-  gridFree(g, g->atlas[0]);
-  gridFree(g, g->atlas[1]);
-  gridFree(g, g->rayRad);
-  gridFree(g, g->rayDir);
+  // buffers bound by ddgi_grid_bind_external belong to the caller
+  if (!g->extAtlas) gridFree(g, g->atlas[0]);
+  if (!g->extTemp) gridFree(g, g->atlas[1]);
+  if (!g->extRays) gridFree(g, g->rayRad);
+  if (!g->extDirs) gridFree(g, g->rayDir);
   gridFree(g, g->rayHit);
   gridFree(g, g->lattice);
   gridFree(g, g->order);
@@ -387,8 +399,10 @@ void gridDestroy(DdgiGrid* g) {
 int ensureSoloRecords(DdgiGrid* g) {
   if (g->dQueue) return DDGI_OK;
   DdgiContext* ctx = g->ctx;
-  CK(cudaMalloc(&g->dQueue, kTraceCounters * sizeof(unsigned long long)), "trace counters");
   const long long slots = maxRaySlots(g->g);
+  if (allocRefused(ctx, kTraceScratchPerRay * (size_t)slots + kTraceCounters * sizeof(unsigned long long)))
+    return fail(ctx, DDGI_ENOMEM, "trace scratch: refused by the allocation hook");
+  CK(cudaMalloc(&g->dQueue, kTraceCounters * sizeof(unsigned long long)), "trace counters");
   CK(cudaMalloc(&g->dHits, kTraceScratchPerRay * (size_t)slots), "trace scratch");
   g->dShadow = g->dHits + slots;
   return DDGI_OK;
@@ -402,6 +416,22 @@ using namespace ddgi::detail;
 extern "C" {
 
 int ddgi_abi_version(void) { return DDGI_ABI_VERSION; }
+
+int ddgi_context_set_waits(DdgiContext* ctx, const DdgiWaitConfig* cfg) {
+  if (!ctx || !cfg) return fail(ctx, DDGI_EINVAL, "NULL argument to ddgi_context_set_waits");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->waits.spin = cfg->spinLimit ? cfg->spinLimit : WaitCfg{}.spin;
+  ctx->waits.stall = cfg->stallTest ? 1u : 0u;
+  return DDGI_OK;
+}
+
+int ddgi_context_set_alloc_hook(DdgiContext* ctx, DdgiAllocHook hook, void* user) {
+  if (!ctx) return DDGI_EINVAL;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->allocHook = hook;
+  ctx->allocUser = user;
+  return DDGI_OK;
+}
 
 int ddgi_context_create(int device, DdgiContext** out) {
   if (!out) return DDGI_EINVAL;
@@ -493,6 +523,7 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
   sc->ctx = ctx;
   auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
     if (!bytes) return cudaSuccess;
+    if (allocRefused(ctx, bytes)) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(dst, bytes);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st);
@@ -519,7 +550,7 @@ int ddgi_scene_create(DdgiContext* ctx, const DdgiSceneDesc* d, void* stream, Dd
   sc->view.instances = sc->instances;
   sc->view.materials = sc->materials;
   if (tris > 0) {
-    e = cudaMalloc(&sc->shade, 48ull * tris);
+    e = allocRefused(ctx, 48ull * tris) ? cudaErrorMemoryAllocation : cudaMalloc(&sc->shade, 48ull * tris);
     if (e == cudaSuccess) {
       sc->view.shade = sc->shade;
       e = launchShadingRecords(sc->view, d->numIndices, d->numVertices, sc->shade, ctx->dErr, st);
@@ -668,8 +699,8 @@ uint64_t ddgi_grid_footprint(const DdgiGridDesc* desc, int convMode) {
 int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
   if (!g || !o) return DDGI_EINVAL;
   o->atlas = g->atlas[g->cur];
-  o->rayRadiance = (float*)g->rayRad;
-  o->rayDirection = (float*)g->rayDir;
+  o->rayRadiance = g->rayRad;
+  o->rayDirection = g->rayDir;
   o->rayHit = g->rayHit;
   o->lattice = (float*)g->lattice;
   o->atlasWidth = g->g.atlasW;
@@ -679,6 +710,65 @@ int ddgi_grid_buffers(const DdgiGrid* g, DdgiGridBuffers* o) {
   o->rayBlockW = g->g.bw;
   o->rayBlockH = g->g.bh;
   o->atlasBytes = g->atlasBytes;
+  o->rayBytes = g->rayBytes;
+  o->rayFormat = g->g.rayFmt;
+  o->reserved = 0;
+  return DDGI_OK;
+}
+
+int ddgi_grid_bind_external(DdgiGrid* g, const DdgiGridExternal* x, void* stream) {
+  if (!g || !x) return fail(g ? g->ctx : nullptr, DDGI_EINVAL, "NULL argument to ddgi_grid_bind_external");
+  DdgiContext* ctx = g->ctx;
+  auto misaligned = [](const void* p) { return ((uintptr_t)p & 15) != 0; };
+  if (misaligned(x->atlas) || misaligned(x->atlasTemp) || misaligned(x->rayRadiance) || misaligned(x->rayDirection))
+    return fail(ctx, DDGI_EINVAL, "external buffers must be 16-byte aligned");
+  if ((x->atlas || x->atlasTemp) && x->atlasBytes != g->atlasBytes)
+    return fail(ctx, DDGI_EINVAL, "external atlas must be %llu bytes, got %llu", (unsigned long long)g->atlasBytes,
+                (unsigned long long)x->atlasBytes);
+  if ((x->rayRadiance || x->rayDirection) && x->rayBytes != g->rayBytes)
+    return fail(ctx, DDGI_EINVAL, "external ray images must be %llu bytes, got %llu", (unsigned long long)g->rayBytes,
+                (unsigned long long)x->rayBytes);
+  if (x->rayDirection && !(g->desc.options & DDGI_GRID_WRITE_DIRS))
+    return fail(ctx, DDGI_EINVAL, "the grid writes no direction image (DDGI_GRID_WRITE_DIRS)");
+  if (x->atlas && x->atlas == x->atlasTemp) return fail(ctx, DDGI_EINVAL, "atlas and atlasTemp must differ");
+  if (g->asyncAlloc) return fail(ctx, DDGI_EINVAL, "served grids take no external buffers");
+  // nothing in flight may still use the buffers released below
+  CK(cudaSetDevice(ctx->device), "set device");
+  CK(cudaStreamSynchronize((cudaStream_t)stream), "bind sync");
+  if (g->dlDone) CK(cudaEventSynchronize(g->dlDone), "bind sync");
+  CK(cudaDeviceSynchronize(), "bind sync");
+  if (x->atlas || x->atlasTemp) {
+    // roles, not slots: the current atlas and the temp (a grid that never had a binding swaps them on a move);
+    // from now on the current atlas is slot 0, the temp slot 1, and translations copy instead of swapping
+    void* cur = g->atlas[g->cur];
+    void* tmp = g->atlas[1 - g->cur];
+    bool curExt = g->extAtlas, tmpExt = g->extTemp;
+    if (x->atlas) {
+      if (!curExt) gridFree(g, cur);
+      cur = x->atlas;
+      curExt = true;
+    }
+    if (x->atlasTemp) {
+      if (!tmpExt) gridFree(g, tmp);
+      tmp = x->atlasTemp;
+      tmpExt = true;
+    }
+    g->atlas[0] = cur;
+    g->atlas[1] = tmp;
+    g->cur = 0;
+    g->extAtlas = curExt;
+    g->extTemp = tmpExt;
+  }
+  if (x->rayRadiance) {
+    if (!g->extRays) gridFree(g, g->rayRad);
+    g->rayRad = x->rayRadiance;
+    g->extRays = true;
+  }
+  if (x->rayDirection) {
+    if (!g->extDirs) gridFree(g, g->rayDir);
+    g->rayDir = x->rayDirection;
+    g->extDirs = true;
+  }
   return DDGI_OK;
 }
 
@@ -788,7 +878,7 @@ int ddgi_convolve(DdgiGrid* g, const DdgiFrame* frame, void* stream) {
     if (!g->rad16Written || b < g->tracedBegin || e > g->tracedEnd)
       CK(launchPackRays16(g->g, fmt, g->rayRad, g->rad16, b, e, pTotal, st), "pack rays");
     CK(launchConvTc(g->g, fmt, g->rad16, pTotal, g->lattice, g->tcScratch, g->atlas[g->cur], b, e, g->desc.hysteresis,
-                    frame->flags, ctx->dErr, st),
+                    frame->flags, ctx->dErr, st, ctx->waits),
        "tensor-core convolve");
     return DDGI_OK;
   }
@@ -830,6 +920,7 @@ int ddgi_atlas_download_async(DdgiGrid* g, void* host, uint64_t bytes, void* str
   if (bytes != g->atlasBytes) return fail(ctx, DDGI_EINVAL, "atlas is %llu bytes, got %llu",
                                           (unsigned long long)g->atlasBytes, (unsigned long long)bytes);
   if (!g->dlStage) {
+    if (allocRefused(ctx, g->atlasBytes)) return fail(ctx, DDGI_ENOMEM, "atlas download staging: refused by the allocation hook");
     CK(cudaMalloc(&g->dlStage, g->atlasBytes), "atlas download staging");
     CK(cudaStreamCreateWithFlags(&g->dlStream, cudaStreamNonBlocking), "atlas download stream");
     CK(cudaEventCreateWithFlags(&g->dlSnap, cudaEventDisableTiming), "atlas download event");
@@ -908,13 +999,13 @@ int ddgi_atlas_import_rgba16f(DdgiGrid* g, const void* host, uint64_t bytes, voi
   return DDGI_OK;
 }
 
-int ddgi_rays_download(DdgiGrid* g, float* radiance, int32_t* hits, float* lattice, void* stream) {
+int ddgi_rays_download(DdgiGrid* g, void* radiance, int32_t* hits, float* lattice, void* stream) {
   if (!g) return DDGI_EINVAL;
   DdgiContext* ctx = g->ctx;
   cudaStream_t st = (cudaStream_t)stream;
   size_t texels = (size_t)g->g.rayW * g->rayH;
   if (hits && !g->rayHit) return fail(ctx, DDGI_EINVAL, "grid was created without DDGI_GRID_RECORD_HITS");
-  if (radiance) CK(cudaMemcpyAsync(radiance, g->rayRad, 16 * texels, cudaMemcpyDeviceToHost, st), "ray download");
+  if (radiance) CK(cudaMemcpyAsync(radiance, g->rayRad, g->rayBytes, cudaMemcpyDeviceToHost, st), "ray download");
   if (hits) CK(cudaMemcpyAsync(hits, g->rayHit, 4 * texels, cudaMemcpyDeviceToHost, st), "hit download");
   if (lattice) CK(cudaMemcpyAsync(lattice, g->lattice, 16 * (size_t)g->g.N, cudaMemcpyDeviceToHost, st), "lattice download");
   CK(cudaStreamSynchronize(st), "ray download sync");
@@ -1015,7 +1106,7 @@ int ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* s
   return launchLattice(numRays, rot, (float4*)dirs, (cudaStream_t)stream) == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
 }
 
-int ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs, void* atlas,
+int ddgi_convolve_raw(const DdgiGridDesc* desc, const void* rayRadiance, const float* dirs, void* atlas,
                       int layerBegin, int layerEnd, uint32_t flags, void* stream) {
   if (validateGridDesc(nullptr, desc) != DDGI_OK || !rayRadiance || !dirs || !atlas) return DDGI_EINVAL;
   if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return DDGI_EINVAL;
@@ -1027,7 +1118,7 @@ int ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const 
   float* ws = wt + (size_t)g.N * kOctTexels;
   cudaError_t e = launchConvWeights(g.N, (const float4*)dirs, wt, ws, st);
   if (e == cudaSuccess)
-    e = launchConvFp32(g, (const float4*)rayRadiance, wt, ws, atlas, layerBegin, layerEnd, desc->hysteresis, flags, st);
+    e = launchConvFp32(g, rayRadiance, wt, ws, atlas, layerBegin, layerEnd, desc->hysteresis, flags, st);
   cudaFreeAsync(wt, st);
   return e == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
 }
@@ -1047,19 +1138,19 @@ int ddgi_convolve_tc_raw(DdgiContext* ctx, const DdgiGridDesc* desc, const void*
   void* scratch = nullptr;
   CK(cudaMallocAsync(&scratch, tcScratchBytes(g.N), st), "tensor-core weight scratch");
   cudaError_t e = launchConvTc(g, elemFormat, radiance16, g.X * g.Y * g.Z, (const float4*)dirs, scratch, atlas,
-                               layerBegin, layerEnd, desc->hysteresis, flags, ctx->dErr, st);
+                               layerBegin, layerEnd, desc->hysteresis, flags, ctx->dErr, st, ctx->waits);
   cudaFreeAsync(scratch, st);
   if (e != cudaSuccess) return cudaFail(ctx, e, "tensor-core convolve");
   return DDGI_OK;
 }
 
-int ddgi_pack_rays16(const DdgiGridDesc* desc, const float* rayRadiance, void* radiance16, int elemFormat,
+int ddgi_pack_rays16(const DdgiGridDesc* desc, const void* rayRadiance, void* radiance16, int elemFormat,
                      int layerBegin, int layerEnd, void* stream) {
   if (validateGridDesc(nullptr, desc) != DDGI_OK || !rayRadiance || !radiance16) return DDGI_EINVAL;
   if (elemFormat != DDGI_ELEM_F16 && elemFormat != DDGI_ELEM_BF16) return DDGI_EINVAL;
   if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return DDGI_EINVAL;
   GridGPU g = makeGridGPU(*desc);
-  return launchPackRays16(g, elemFormat, (const float4*)rayRadiance, radiance16, layerBegin, layerEnd,
+  return launchPackRays16(g, elemFormat, rayRadiance, radiance16, layerBegin, layerEnd,
                           g.X * g.Y * g.Z, (cudaStream_t)stream) == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
 }
 

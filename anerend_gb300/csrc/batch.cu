@@ -123,7 +123,7 @@ int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long t
      "batched trace");
   if (t.convMode != 0) {
     int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
-    CK(launchConvTcItems(fmt, S->tcHost.data(), S->dTc(), n, totalUnits, ctx->dErr, st),
+    CK(launchConvTcItems(fmt, S->tcHost.data(), S->dTc(), n, totalUnits, ctx->dErr, st, ctx->waits),
        "batched tensor-core convolve");
   } else {
     CK(launchConvFp32Batch(S->dConv(), n, totalGroups, st), "batched convolve");

@@ -96,26 +96,39 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
     const long long total = (long long)(it.layerEnd - it.layerBegin) * probesPerLayer;
     const long long base = (tile - it.groupBegin) * kTileProbes;
     const int N = g.N;
-    // this thread stages ray (j0 + tg) of probes pg + 8k of the tile (k < kRLoads)
-    const float4* rsrc[kRLoads];
+    // this thread stages ray (j0 + tg) of probes pg + 8k of the tile (k < kRLoads): the texel index of each
+    // probe's ray block in the ray image, -1 past the tile's probes
+    long long rsrc[kRLoads];
 #pragma unroll
     for (int k = 0; k < kRLoads; ++k) {
       long long pl = base + pg + 8 * k;
-      rsrc[k] = nullptr;
+      rsrc[k] = -1;
       if (pl < total) {
         int layer = it.layerBegin + (int)(pl / probesPerLayer);
         int p = (int)(pl % probesPerLayer);
         int px = p % g.X, pz = p / g.X;
-        rsrc[k] = it.rayRad + (size_t)((layer * g.Z + pz) * g.bh) * g.rayW + (size_t)px * g.bw;
+        rsrc[k] = (long long)((layer * g.Z + pz) * g.bh) * g.rayW + (long long)px * g.bw;
       }
     }
     const float4* W4 = reinterpret_cast<const float4*>(it.wt);
+    const bool rays16 = g.rayFmt == DDGI_FORMAT_RGBA16F;  // the same for the whole item
     float4 rn[kRLoads], wn[kWLoads];
     auto fetch = [&](int j0) {
       const int j = j0 + tg;
-      const size_t off = (size_t)(j / g.bw) * g.rayW + (j % g.bw);
+      const long long off = (long long)(j / g.bw) * g.rayW + (j % g.bw);
 #pragma unroll
-      for (int k = 0; k < kRLoads; ++k) rn[k] = rsrc[k] ? __ldg(rsrc[k] + off) : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < kRLoads; ++k) {
+        if (rsrc[k] < 0) {
+          rn[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else if (rays16) {
+          const uint2 raw = __ldg(reinterpret_cast<const uint2*>(it.rayRad) + rsrc[k] + off);
+          const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+          const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+          rn[k] = make_float4(a.x, a.y, b.x, b.y);
+        } else {
+          rn[k] = __ldg(reinterpret_cast<const float4*>(it.rayRad) + rsrc[k] + off);
+        }
+      }
 #pragma unroll
       for (int k = 0; k < kWLoads; ++k) wn[k] = __ldg(W4 + (size_t)j0 * (kOctTexels / 4) + threadIdx.x + k * kTileThreads);
     };
@@ -227,7 +240,7 @@ cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum,
   return cudaGetLastError();
 }
 
-cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* wt, const float* wsum,
+cudaError_t launchConvFp32(const GridGPU& g, const void* rayRad, const float* wt, const float* wsum,
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream) {
   if (layerEnd <= layerBegin) return cudaSuccess;

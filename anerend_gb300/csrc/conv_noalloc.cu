@@ -9,7 +9,7 @@
 //   - processes whose device memory is fully committed to a budget (a serving loop admitting work by HBM
 //     footprint), where an extra allocation at update time could fail or push another request out.
 // This file gives them ddgi_convolve_raw_noalloc: the same kernels, with the scratch in a file-scope
-// __device__ array of fixed size (kNoAllocMaxRays x 64 + 64 floats = 132,352 bytes). Every GPU that loads
+// __device__ array of fixed size (kNoAllocMaxRays x 64 + 64 floats = 131,328 bytes). Every GPU that loads
 // the library holds that array until the process exits.
 //
 // The first call on a device looks up the array's device address with cudaGetSymbolAddress (with that
@@ -18,8 +18,7 @@
 // it later reads (nothing accumulates in the scratch), so no clearing is needed; but calls that overlap on
 // the GPU (different streams without ordering between them) race on the array and must be serialised by
 // the caller.
-#include "ddgi_common.cuh"
-#include "kernels.h"
+#include "objects.h"
 
 #include <mutex>
 
@@ -48,44 +47,25 @@ int scratchAddress(float** out) {
   return DDGI_OK;
 }
 
-bool isPow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
-
 }  // namespace
 
-extern "C" int ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs,
+extern "C" int ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const void* rayRadiance, const float* dirs,
                                          void* atlas, int layerBegin, int layerEnd, uint32_t flags,
                                          void* stream) {
-  if (!desc || !rayRadiance || !dirs || !atlas) return DDGI_EINVAL;
-  for (int i = 0; i < 3; ++i)
-    if (desc->dims[i] <= 0 || desc->dims[i] > 4096 || !(desc->step[i] > 0.0f)) return DDGI_EINVAL;
-  // the scratch holds the weights of at most kNoAllocMaxRays rays
-  if (!isPow2(desc->raysPerProbe) || desc->raysPerProbe < 16 || desc->raysPerProbe > kNoAllocMaxRays)
-    return DDGI_EINVAL;
-  if (desc->atlasFormat != DDGI_FORMAT_RGBA32F && desc->atlasFormat != DDGI_FORMAT_RGBA16F) return DDGI_EINVAL;
-  if (!(desc->hysteresis >= 0.0f && desc->hysteresis <= 1.0f)) return DDGI_EINVAL;
+  // the same argument checks as ddgi_convolve_raw, then the one limit of the static scratch
+  if (ddgi::detail::validateGridDesc(nullptr, desc) != DDGI_OK || !rayRadiance || !dirs || !atlas) return DDGI_EINVAL;
   if (layerBegin < 0 || layerEnd > desc->dims[1] || layerBegin > layerEnd) return DDGI_EINVAL;
+  if (desc->raysPerProbe > kNoAllocMaxRays) return DDGI_EINVAL;  // the scratch holds the weights of that many rays
   float* scratch = nullptr;
   int rc = scratchAddress(&scratch);
   if (rc != DDGI_OK) return rc;
-  ddgi::GridGPU g{};
-  g.X = desc->dims[0];
-  g.Y = desc->dims[1];
-  g.Z = desc->dims[2];
-  g.N = desc->raysPerProbe;
-  ddgi::rayBlock(g.N, g.bw, g.bh);
-  g.step = ddgi::f3(desc->step[0], desc->step[1], desc->step[2]);
-  g.originY = desc->originY;
-  g.atlasW = ddgi::kProbePix * g.X;
-  g.atlasH = ddgi::kProbePix * g.Z * g.Y;
-  g.atlasFmt = desc->atlasFormat;
-  g.rayW = g.bw * g.X;
-  g.options = desc->options;
+  const ddgi::GridGPU g = ddgi::detail::makeGridGPU(*desc);
   float* wt = scratch;
   float* wsum = scratch + (size_t)g.N * ddgi::kOctTexels;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = ddgi::launchConvWeights(g.N, (const float4*)dirs, wt, wsum, st);
   if (e == cudaSuccess)
-    e = ddgi::launchConvFp32(g, (const float4*)rayRadiance, wt, wsum, atlas, layerBegin, layerEnd, desc->hysteresis,
+    e = ddgi::launchConvFp32(g, rayRadiance, wt, wsum, atlas, layerBegin, layerEnd, desc->hysteresis,
                              flags, st);
   return e == cudaSuccess ? DDGI_OK : DDGI_EDEVICE;
 }

@@ -16,8 +16,9 @@
 // A single-item launch carries its record and tensor maps in the kernel parameters (TcOne); a batch reads
 // its records from device memory (TcMany), so a captured launch sees per-frame values written between replays.
 //
-// Every mbarrier wait is bounded: on timeout the kernel raises DDGI_DEVERR_TIMEOUT, stops issuing work,
-// waits (bounded) for its own TMA loads and MMAs in flight, frees its TMEM and returns.
+// Every mbarrier wait is bounded (WaitCfg::spin attempts): on timeout the kernel raises DDGI_DEVERR_TIMEOUT, stops
+// issuing work, waits (bounded by kDrainLimit, whatever WaitCfg says) for its own TMA loads and MMAs in flight,
+// frees its TMEM and returns.
 #include "ddgi_common.cuh"
 #include "kernels.h"
 
@@ -47,7 +48,8 @@ constexpr int kThreadsTc = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warp
 constexpr int kStageRow = 17;
 constexpr int kStageWarpFloats = 3 * 32 * kStageRow;
 constexpr size_t kSmemTc = (size_t)kStages * kStageBytes + kEpiWarps * kStageWarpFloats * sizeof(float) + 1024;
-constexpr uint32_t kSpinLimit = 1u << 22;
+// attempts of a wait for the kernel's own copies and MMAs in flight before the CTA exits (after a timeout)
+constexpr uint32_t kDrainLimit = 1u << 22;
 
 DDGI_D uint32_t smemU32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -69,9 +71,9 @@ DDGI_D bool mbarTryWait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; false after kSpinLimit attempts.
-DDGI_D bool mbarWait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+// Bounded wait; false after `limit` attempts (about 64 ns apart after the first 32).
+DDGI_D bool mbarWait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbarTryWait(bar, parity)) return true;
     if (i > 32) __nanosleep(64);
   }
@@ -235,10 +237,12 @@ DDGI_D bool nextTile(const Src& src, int& unit, int unitEnd, TcTile& t) {
 
 template <int kFmt, class Src>
 __global__ void __launch_bounds__(kThreadsTc, 1)
-    k_conv_tc(const __grid_constant__ Src src, int totalUnits, uint32_t* __restrict__ err) {
+    k_conv_tc(const __grid_constant__ Src src, int totalUnits, uint32_t* __restrict__ err, WaitCfg waits) {
   extern __shared__ uint8_t smemRaw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smemRaw + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t fullBar[kStages], emptyBar[kStages], accFull[2], accEmpty[2], drainBar;
+  // neverBar: no thread ever arrives on it; with waits.stall the epilogue's first wait is on it, so the
+  // timeout path runs (the failure-detection test)
+  __shared__ uint64_t fullBar[kStages], emptyBar[kStages], accFull[2], accEmpty[2], drainBar, neverBar;
   __shared__ uint32_t tmemSlot;
   __shared__ int abortFlag;
 
@@ -251,6 +255,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     for (int s = 0; s < kStages; ++s) { mbarInit(&fullBar[s], 1); mbarInit(&emptyBar[s], 1); }
     for (int b = 0; b < 2; ++b) { mbarInit(&accFull[b], 1); mbarInit(&accEmpty[b], 32 * kEpiWarps); }
     mbarInit(&drainBar, 1);
+    mbarInit(&neverBar, 1);
     abortFlag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         const uint32_t bytes = (uint32_t)(3 * tile.units * kAUnitBytes + kWTileBytes);
         bool ok = true;
         for (int kc = 0; kc < it.numChunks; ++kc) {
-          if (!mbarWait(&emptyBar[s], phase ^ 1)) { fail(); ok = false; break; }
+          if (!mbarWait(&emptyBar[s], phase ^ 1, waits.spin)) { fail(); ok = false; break; }
           pending[s] = false;
           uint8_t* st = smem + (size_t)s * kStageBytes;
           mbarExpectTx(&fullBar[s], bytes);
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
       if (aborted()) {  // let loads in flight land before the CTA exits
         for (int k = 0; k < kStages; ++k)
-          if (pending[k]) mbarWait(&fullBar[k], pendingParity[k]);
+          if (pending[k]) mbarWait(&fullBar[k], pendingParity[k], kDrainLimit);
       }
     }
   } else if (warp == 1) {
@@ -319,12 +324,12 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         const int numChunks = src.item(tile.item).numChunks;
         int b = local & 1;
         uint32_t accPhase = (local >> 1) & 1;
-        if (!mbarWait(&accEmpty[b], accPhase ^ 1)) { fail(); break; }
+        if (!mbarWait(&accEmpty[b], accPhase ^ 1, waits.spin)) { fail(); break; }
         tcFenceAfter();
         const uint32_t dBase = tmem + (uint32_t)(b * 3 * kOctTexels);
         bool ok = true;
         for (int kc = 0; kc < numChunks; ++kc) {
-          if (!mbarWait(&fullBar[s], phase)) { fail(); ok = false; break; }
+          if (!mbarWait(&fullBar[s], phase, waits.spin)) { fail(); ok = false; break; }
           tcFenceAfter();
           uint32_t st = smemU32(smem + (size_t)s * kStageBytes);
 #pragma unroll
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
       if (issued) {  // drain: every MMA issued by this thread has completed
         mmaCommit(&drainBar);
-        mbarWait(&drainBar, 0);
+        mbarWait(&drainBar, 0, kDrainLimit);
       }
     }
   } else {
@@ -385,9 +390,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       const bool rowsLive = warpProbe0 < tileEnd;  // warp-uniform
       const uint32_t laneAddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 3 * kOctTexels);
       bool ok = true;
+      if (waits.stall && local == 0) {  // the test hook: a wait that no arrival ends
+        if (!__all_sync(0xffffffffu, mbarWait(&neverBar, 0, waits.spin))) {
+          if (lane == 0) fail();
+          break;
+        }
+      }
       if (!rowsLive) {
         // warp-uniform outcome
-        if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase))) {
+        if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase, waits.spin))) {
           if (lane == 0) fail();
           break;
         }
@@ -405,7 +416,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         }
         if (blk == 2 * half) {
           // warp-uniform outcome: the tcgen05.ld below is warp-collective
-          if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase))) {
+          if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase, waits.spin))) {
             if (lane == 0) fail();
             ok = false;
             break;
@@ -507,9 +518,10 @@ __global__ void __launch_bounds__(256) k_tc_weights(const unsigned char* __restr
   }
 }
 
-// RGBA32F ray image -> planar 16-bit radiance, row c * pTotal + p (p linear over the grid), N rays per row.
+// Ray image (g.rayFmt texels) -> planar 16-bit radiance, row c * pTotal + p (p linear over the grid), N rays
+// per row.
 template <int kFmt>
-__global__ void k_pack_rays16(GridGPU g, const float4* __restrict__ rayRad, uint16_t* __restrict__ out, int pBegin,
+__global__ void k_pack_rays16(GridGPU g, const void* __restrict__ rayRad, uint16_t* __restrict__ out, int pBegin,
                               int pEnd, int pTotal) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = (long long)(pEnd - pBegin) * g.N;
@@ -518,7 +530,7 @@ __global__ void k_pack_rays16(GridGPU g, const float4* __restrict__ rayRad, uint
   int px = p % g.X, pzAll = p / g.X;
   int rx = px * g.bw + (j % g.bw);
   int ry = pzAll * g.bh + (j / g.bw);
-  float4 v = rayRad[(size_t)ry * g.rayW + rx];
+  const float4 v = loadTexel(rayRad, g.rayFmt, (size_t)ry * g.rayW + rx);
   float c[3] = {v.x, v.y, v.z};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -556,7 +568,7 @@ bool makeMap(CUtensorMap* m, int fmt, const void* base, uint64_t rows, uint64_t 
 
 }  // namespace
 
-cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad, void* out16, int layerBegin,
+cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const void* rayRad, void* out16, int layerBegin,
                              int layerEnd, int pTotal, cudaStream_t stream) {
   int pBegin = layerBegin * g.X * g.Z, pEnd = layerEnd * g.X * g.Z;
   long long total = (long long)(pEnd - pBegin) * g.N;
@@ -628,7 +640,7 @@ cudaError_t tcLaunchSetup(Kern kern, int slot, int* sms) {
 }
 
 template <int kFmt, class Src>
-cudaError_t launchTc(const Src& src, int slot, int totalUnits, uint32_t* err, cudaStream_t stream) {
+cudaError_t launchTc(const Src& src, int slot, int totalUnits, uint32_t* err, WaitCfg waits, cudaStream_t stream) {
   int sms = 0;
   cudaError_t e = tcLaunchSetup(k_conv_tc<kFmt, Src>, slot, &sms);
   if (e != cudaSuccess) return e;
@@ -642,7 +654,8 @@ cudaError_t launchTc(const Src& src, int slot, int totalUnits, uint32_t* err, cu
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_conv_tc<kFmt, Src>, src, totalUnits, err);
+  if (waits.spin == 0) waits.spin = WaitCfg{}.spin;
+  return cudaLaunchKernelEx(&cfg, k_conv_tc<kFmt, Src>, src, totalUnits, err, waits);
 }
 
 }  // namespace
@@ -650,7 +663,7 @@ cudaError_t launchTc(const Src& src, int slot, int totalUnits, uint32_t* err, cu
 // Weights of every item, then the tensor-core convolution of all items' units in one launch.
 // dItems: numItems TcItem records in device memory (copied from the TcItemHost.item bytes).
 cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
-                              int totalUnits, uint32_t* err, cudaStream_t stream) {
+                              int totalUnits, uint32_t* err, cudaStream_t stream, WaitCfg waits) {
   if (numItems <= 0 || totalUnits <= 0) return cudaSuccess;
   if (numItems > kMaxTcItems) return cudaErrorInvalidValue;
   const unsigned char* items = (const unsigned char*)dItems;
@@ -670,13 +683,14 @@ cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const vo
   }
   src.items = items;
   src.n = numItems;
-  return elemFmt == 0 ? launchTc<0>(src, 0, totalUnits, err, stream) : launchTc<1>(src, 1, totalUnits, err, stream);
+  return elemFmt == 0 ? launchTc<0>(src, 0, totalUnits, err, waits, stream)
+                      : launchTc<1>(src, 1, totalUnits, err, waits, stream);
 }
 
 // One grid: the record and the tensor maps travel in the kernel parameters (no copy to the device).
 cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
                          void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
-                         uint32_t* err, cudaStream_t stream) {
+                         uint32_t* err, cudaStream_t stream, WaitCfg waits) {
   if (layerEnd <= layerBegin) return cudaSuccess;
   TcItemHost h;
   if (!tcPrepareItem(g, elemFmt, rad16, pTotal, dirs, scratch, atlas, layerBegin, layerEnd, hysteresis, flags, 0, &h))
@@ -690,7 +704,8 @@ cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int p
   else k_tc_weights<1><<<wg, 256, 0, stream>>>(nullptr, one.it);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return elemFmt == 0 ? launchTc<0>(one, 2, h.units, err, stream) : launchTc<1>(one, 3, h.units, err, stream);
+  return elemFmt == 0 ? launchTc<0>(one, 2, h.units, err, waits, stream)
+                      : launchTc<1>(one, 3, h.units, err, waits, stream);
 }
 
 }  // namespace ddgi

@@ -167,7 +167,7 @@ DDGI_HD void rayBlock(int n, int& bw, int& bh) {
   bh = n / bw;
 }
 
-// ---- atlas texel access ----------------------------------------------------------------------------
+// ---- atlas and ray-image texel access -----------------------------------------------------------------
 DDGI_D float4 loadTexel(const void* atlas, int fmt, size_t idx) {
   if (fmt == DDGI_FORMAT_RGBA32F) return reinterpret_cast<const float4*>(atlas)[idx];
   uint2 raw = reinterpret_cast<const uint2*>(atlas)[idx];
@@ -248,6 +248,7 @@ struct GridGPU {
   float originY;
   int atlasW, atlasH, atlasFmt;
   int rayW;
+  int rayFmt;      // texel format of the ray images (DDGI_FORMAT_RGBA32F or DDGI_FORMAT_RGBA16F)
   uint32_t options;
   int bvhWide;     // 1: traverse the 8-wide BVH, 0: the binary one
   int warpProbes;  // probes per warp (power of two, 32 / warpProbes <= N)

@@ -19,8 +19,8 @@ struct TraceItem {
   const float4* lattice;  // written by the batched lattice kernel
   const int* order;
   const void* atlasPrev;
-  float4* rayRad;
-  float4* rayDir;
+  void* rayRad;  // ray images in g.rayFmt texels
+  void* rayDir;
   int* rayHit;
   long long warpBegin;    // first warp of this item (its ray slots start at 32 * warpBegin)
   // Closest-hit seeding. A ray first tests a candidate triangle: the closest hit of its probe's ray in the
@@ -81,14 +81,14 @@ cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f,
 // probe_conv.comp: weights table (N x 64, transposed) and per-texel weight sums from the lattice.
 cudaError_t launchConvWeights(int n, const float4* dirs, float* wt, float* wsum, cudaStream_t stream);
 // Convolution + hysteresis (or bake accumulation) of layers [layerBegin, layerEnd) into `atlas`.
-cudaError_t launchConvFp32(const GridGPU& g, const float4* rayRad, const float* wt, const float* wsum,
+cudaError_t launchConvFp32(const GridGPU& g, const void* rayRad, const float* wt, const float* wsum,
                            void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
                            cudaStream_t stream);
 
 // FP32 convolution of many grids in one launch (conv.cu).
 struct ConvItem {
   GridGPU g;
-  const float4* rayRad;
+  const void* rayRad;  // g.rayFmt texels
   const float4* dirs;
   float* wt;        // N x 64 weights of this item (written by the weights kernel)
   float* wsum;
@@ -105,6 +105,14 @@ int convTileProbes(long long probes);
 cudaError_t launchConvFp32Batch(const ConvItem* dItems, int numItems, long long totalGroups, cudaStream_t stream,
                                 int tileProbes = 16);
 
+// Bounded device waits of the tensor-core convolution (DdgiWaitConfig): attempts per mbarrier wait before it
+// gives up (0 means the default), and the test hook that makes each CTA's first accumulator wait wait for a
+// phase no arrival completes, so that the timeout path runs.
+struct WaitCfg {
+  uint32_t spin = 1u << 22;
+  uint32_t stall = 0;
+};
+
 // Tensor-core convolution (conv_tc.cu). rad16: planar 16-bit radiance (elemFmt 0 FP16, 1 BF16), row
 // c * pTotal + p; N a multiple of 64. scratch: tcScratchBytes(N) bytes (16-bit weights + two sum rows).
 size_t tcScratchBytes(int n);
@@ -120,11 +128,11 @@ bool tcPrepareItem(const GridGPU& g, int elemFmt, const void* rad16, int pTotal,
                    void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags, int unitBegin,
                    TcItemHost* out);
 cudaError_t launchConvTcItems(int elemFmt, const TcItemHost* hostItems, const void* dItems, int numItems,
-                              int totalUnits, uint32_t* err, cudaStream_t stream);
+                              int totalUnits, uint32_t* err, cudaStream_t stream, WaitCfg waits = WaitCfg{});
 cudaError_t launchConvTc(const GridGPU& g, int elemFmt, const void* rad16, int pTotal, const float4* dirs,
                          void* scratch, void* atlas, int layerBegin, int layerEnd, float hysteresis, uint32_t flags,
-                         uint32_t* err, cudaStream_t stream);
-cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const float4* rayRad, void* out16, int layerBegin,
+                         uint32_t* err, cudaStream_t stream, WaitCfg waits = WaitCfg{});
+cudaError_t launchPackRays16(const GridGPU& g, int elemFmt, const void* rayRad, void* out16, int layerBegin,
                              int layerEnd, int pTotal, cudaStream_t stream);
 
 // Translation copy (IrradianceProbeTranslationPass.cpp:83-168): out = in shifted by (sx, sz) probes.

@@ -55,7 +55,19 @@ struct DdgiContext {
   uint32_t* dErr = nullptr;  // sticky device error word
   std::mutex mu;
   std::string err;
+  ddgi::WaitCfg waits;                 // bounded device waits (ddgi_context_set_waits)
+  DdgiAllocHook allocHook = nullptr;   // ddgi_context_set_alloc_hook
+  void* allocUser = nullptr;
 };
+
+namespace ddgi {
+namespace detail {
+// The context's allocation hook: true when it refuses an allocation of `bytes` (no hook: never).
+inline bool allocRefused(const DdgiContext* ctx, size_t bytes) {
+  return ctx && ctx->allocHook && ctx->allocHook(ctx->allocUser, (uint64_t)bytes) != 0;
+}
+}  // namespace detail
+}  // namespace ddgi
 
 struct DdgiScene {
   DdgiContext* ctx = nullptr;
@@ -82,8 +94,8 @@ struct DdgiGrid {
   GridGPU g{};
   void* atlas[2] = {nullptr, nullptr};  // current atlas and the translation temp (swapped on a move)
   int cur = 0;
-  float4* rayRad = nullptr;
-  float4* rayDir = nullptr;
+  void* rayRad = nullptr;   // ray images in g.rayFmt texels
+  void* rayDir = nullptr;
   int* rayHit = nullptr;
   float4* lattice = nullptr;
   int* order = nullptr;   // trace-kernel direction order (N ints)
@@ -102,6 +114,11 @@ struct DdgiGrid {
   float* wsum = nullptr;  // 64 weight sums
   int rayH = 0;
   uint64_t atlasBytes = 0;
+  uint64_t rayBytes = 0;  // one ray image
+  // buffers bound by ddgi_grid_bind_external (the caller's; never freed here): the current atlas (slot 0),
+  // the translation temp (slot 1), the ray images. With either atlas bound, translations copy instead of
+  // swapping the two slots.
+  bool extAtlas = false, extTemp = false, extRays = false, extDirs = false;
   int lastProbeIdx[2] = {0, 0};  // IrradianceProbeTranslationPass.h:17
   int currentLayer = 0;          // IrradianceProbeRayTracingPass _currentLayer
   int tracedBegin = 0, tracedEnd = 0;  // the "ProbeLayer" blackboard value, as a range

@@ -518,8 +518,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
       }
       // stores (rgen:108-109)
       const size_t idx = rayIndex(g, rs);
-      T.rayRad[idx] = make_float4(L.x, L.y, L.z, 1.0f);
-      if (T.rayDir) T.rayDir[idx] = make_float4(dir.x, dir.y, dir.z, 1.0f);
+      storeTexel(T.rayRad, g.rayFmt, idx, make_float4(L.x, L.y, L.z, 1.0f));
+      if (T.rayDir) storeTexel(T.rayDir, g.rayFmt, idx, make_float4(dir.x, dir.y, dir.z, 1.0f));
       if (T.rayHit) T.rayHit[idx] = hitCode;
       if (g.rad16) storeRad16(g, rs, L);
     }
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(256) k_shadow_resolve(const __grid_constant__ 
     if (!shadowed) continue;
     const float3 Ls = xyz(hr);
     const size_t idx = rayIndex(T.g, rs);
-    T.rayRad[idx] = make_float4(Ls.x, Ls.y, Ls.z, 1.0f);
+    storeTexel(T.rayRad, T.g.rayFmt, idx, make_float4(Ls.x, Ls.y, Ls.z, 1.0f));
     if (T.rayHit) T.rayHit[idx] |= 1;
     if (T.g.rad16) storeRad16(T.g, rs, Ls);
   }

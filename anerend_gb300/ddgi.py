@@ -224,9 +224,20 @@ class ProbeGrid:
         arr = np.ascontiguousarray(arr)
         self.ctx.check(self.ctx.lib.ddgi_atlas_upload(self.handle, _ptr(arr), arr.nbytes, stream))
 
-    def download_rays(self, hits: bool = False, stream: int = 0):
+    def bind_external(self, atlas: int = 0, atlas_temp: int = 0, ray_radiance: int = 0, ray_direction: int = 0,
+                      stream: int = 0) -> None:
+        """Use caller-owned device buffers (pointers; 0 keeps the current binding) in place of the grid's own
+        (ddgi_grid_bind_external): zero-copy interop with a renderer that owns the atlas and ray images."""
         b = self.buffers
-        rad = np.empty((b.rayHeight, b.rayWidth, 4), np.float32)
+        x = L.GridExternal(atlas or None, atlas_temp or None, ray_radiance or None, ray_direction or None,
+                           b.atlasBytes, b.rayBytes)
+        self.ctx.check(self.ctx.lib.ddgi_grid_bind_external(self.handle, C.byref(x), stream))
+
+    def download_rays(self, hits: bool = False, stream: int = 0):
+        """(radiance, hits, lattice): radiance in the grid's ray format (float32, or float16 with
+        DDGI_GRID_RAYS_RGBA16F), shape (rayHeight, rayWidth, 4)."""
+        b = self.buffers
+        rad = np.empty((b.rayHeight, b.rayWidth, 4), np.float32 if b.rayFormat == L.DDGI_FORMAT_RGBA32F else np.float16)
         hit = np.empty((b.rayHeight, b.rayWidth), np.int32) if hits else None
         lat = np.empty((self.desc.raysPerProbe, 4), np.float32)
         self.ctx.check(self.ctx.lib.ddgi_rays_download(self.handle, _ptr(rad), _ptr(hit) if hits else None,

@@ -268,6 +268,47 @@ def _texel_dirs64(np):
     return d / np.linalg.norm(d, axis=1, keepdims=True)
 
 
+def _oracle_conv_blocks(R, dirs64):
+    """The FP64 oracle's convolution (oracle.convolve, probe_conv.comp:21-90) of K probes with hysteresis 0:
+    R is (3, K, n) FP64 radiance, dirs64 the (n, 3) ray directions; returns the (K, 8, 8, 3) interior texels.
+    The probes are laid out as a K x 1 x 1 grid, since each probe's convolution depends only on its own rays."""
+    from anerend_gb300 import ddgi
+    from oracle import oracle
+
+    K, n = R.shape[1], R.shape[2]
+    g = oracle.GridGeom(K, 1, 1, n)
+    bw, _ = g.block
+    rh, rw = g.ray_hw
+    img = np.zeros((rh, rw, 4))
+    img[..., 3] = 1.0
+    j = np.arange(n)
+    img[(j // bw)[None, :], np.arange(K)[:, None] * bw + (j % bw)[None, :], :3] = R.transpose(1, 2, 0)
+    ah, aw = g.atlas_hw
+    atlas = np.zeros((ah, aw, 4))
+    atlas[..., 3] = 1.0
+    oracle.convolve(ddgi.grid_desc((K, 1, 1), rays_per_probe=n, hysteresis=0.0), img, dirs64, atlas, 0, 1, 0,
+                    hysteresis=0.0)
+    return atlas[1:9, :, :3].reshape(8, K, 10, 3)[:, :, 1:9, :].transpose(1, 0, 2, 3)
+
+
+def _atlas_blocks(atlas, dims, probes):
+    """(K, 8, 8, 3) interior texels of probes p = (layer * Z + z) * X + x of an RGBA atlas (10 Z Y, 10 X, 4)."""
+    X, _, Z = dims
+    x, z, layer = probes % X, (probes // X) % Z, probes // (X * Z)
+    t = np.arange(8)
+    r0, c0 = 10 * (Z * layer + z) + 1, 10 * x + 1
+    return atlas[r0[:, None, None] + t[None, :, None], c0[:, None, None] + t[None, None, :], :3]
+
+
+def _rel_err_stats(pairs):
+    """max / p99 / mean per-texel-channel relative error over (got, want) block pairs, each pair's denominator
+    floored at 1e-6 x its mean irradiance."""
+    e = np.concatenate([(np.abs(got.astype(np.float64) - want) / np.maximum(np.abs(want), 1e-6 * np.abs(want).mean()))
+                        .ravel() for got, want in pairs])
+    return {"max": float(e.max()), "p99": float(np.percentile(e, 99)), "mean": float(e.mean()),
+            "texel_channels": int(e.size)}
+
+
 def measure_precision(ctx, stream):
     """Convolution of the 65,536-probe / 512-ray precision workload (radiance log-uniform in [1e-3, 1e2] per
     channel, seeded, generated on the device) on tensor cores (FP16, BF16) and on CUDA cores (FP32): time per
@@ -303,6 +344,15 @@ def measure_precision(ctx, stream):
     ci = (10 * torch.arange(dims[0]).cuda()[None, None, :, None, None] + 1 + torch.arange(8).cuda()[None, None, None, None, :])
     ri, ci = torch.broadcast_tensors(ri, ci)
 
+    # the oracle's check: a seeded 1 % subset of the probes, convolved by oracle.convolve in FP64 from the FP32
+    # radiance and the device's FP32 lattice
+    sub = np.sort(np.random.default_rng(0).choice(P, P // 100, replace=False))
+    want_sub = _oracle_conv_blocks(R32[:, torch.from_numpy(sub).cuda(), :].double().cpu().numpy(),
+                                   dirs.view(n, 4)[:, :3].double().cpu().numpy())
+
+    def oracle_errors():
+        return _rel_err_stats([(_atlas_blocks(atlas.cpu().numpy(), dims, sub), want_sub)])
+
     def errors():
         got = atlas[ri, ci, :3].permute(5, 0, 1, 2, 3, 4).double()
         e = ((got - ref).abs() / torch.clamp(ref.abs(), min=floor)).flatten()
@@ -324,7 +374,8 @@ def measure_precision(ctx, stream):
         atlas.zero_()
         tc(dd=d0)
         torch.cuda.synchronize()
-        prec[f"tc_{name}_rel_err"] = errors()
+        prec[f"tc_{name}_rel_err"] = oracle_errors()
+        prec[f"tc_{name}_rel_err_full_grid"] = errors()
         del r16
     bw, bh = 32, 16
     img = torch.ones((bh * dims[2] * dims[1], bw * dims[0], 4), device="cuda")
@@ -344,9 +395,13 @@ def measure_precision(ctx, stream):
     atlas.zero_()
     fp32(dd=d0)
     torch.cuda.synchronize()
-    prec["fp32_rel_err"] = errors()
+    prec["fp32_rel_err"] = oracle_errors()
+    prec["fp32_rel_err_full_grid"] = errors()
     prec["tc_fp16_speedup_vs_fp32"] = prec["fp32_cuda_core_ms"] / prec["tc_fp16_ms"]
-    prec["error_reference"] = "same formula in FP64 on the device (torch float64); floor 1e-6 x mean irradiance"
+    prec["error_reference"] = ("*_rel_err: the FP64 oracle (oracle.convolve) on a seeded 1% probe subset "
+                               f"({len(sub)} probes); *_rel_err_full_grid: every probe against the same formula "
+                               "in FP64 on the device; floor 1e-6 x mean irradiance")
+    prec["meets_1e-3"] = {k: prec[f"{k}_rel_err"]["max"] <= 1e-3 for k in ("tc_fp16", "tc_bf16", "fp32")}
     del img, atlas, ref, W
     torch.cuda.empty_cache()
     return prec
@@ -441,6 +496,42 @@ def measure_mirror(ctx, scene, w, stream):
     return {"points": n, "ms": ms, "reflected_rays_per_s": n / ms * 1e3, "hit_fraction": hit}
 
 
+def _batched_conv_error(ctx, stream, specs, scs, tuning, conv_mode, picks=8, probes_per_grid=256):
+    """Per-texel error of a batched update's convolution against the FP64 oracle: hysteresis-0 copies of a
+    seeded subset of the batched grids run two batched updates with `conv_mode`; on up to probes_per_grid
+    seeded probes of each, the atlas texels are compared with oracle.convolve of the same traced FP32 radiance
+    and lattice."""
+    from anerend_gb300 import ddgi, scenes
+    from oracle import oracle
+
+    rng = np.random.default_rng(1)
+    sel = sorted(int(i) for i in rng.choice(len(specs), picks, replace=False))
+    grids = [ddgi.ProbeGrid(ctx, specs[i].dims, specs[i].step, specs[i].rays, specs[i].origin_y, 0.0) for i in sel]
+    batch = ddgi.Batch(ctx, [(g, scs[specs[i].scene]) for g, i in zip(grids, sel)])
+    batch.set_tuning(conv_mode=conv_mode, use_graph=0, **tuning)
+    for f in range(2):
+        batch.update([ddgi.FrameParams(camera_pos=specs[i].camera, rotation=scenes.rotation(i, f)) for i in sel],
+                     stream)
+    ctx.sync(stream)
+    pairs = []
+    for g, i in zip(grids, sel):
+        X, Y, Z = specs[i].dims
+        n = specs[i].rays
+        rad, _, lat = g.download_rays()
+        atlas = g.download_atlas()
+        idx = np.sort(rng.choice(X * Y * Z, min(X * Y * Z, probes_per_grid), replace=False))
+        x, z, layer = idx % X, (idx // X) % Z, idx // (X * Z)
+        bw, bh = oracle.GridGeom(X, Y, Z, n).block
+        j = np.arange(n)
+        R = rad[((layer * Z + z) * bh)[:, None] + (j // bw)[None, :], (x * bw)[:, None] + (j % bw)[None, :], :3]
+        want = _oracle_conv_blocks(R.astype(np.float64).transpose(2, 0, 1), lat[:, :3].astype(np.float64))
+        pairs.append((_atlas_blocks(atlas, specs[i].dims, idx), want))
+    batch.close()
+    for g in grids:
+        g.close()
+    return _rel_err_stats(pairs)
+
+
 def measure_batched(ctx, stream, serving=True):
     """The 64-grid batched workload against its plain one-grid-at-a-time form and, with `serving`, the serving
     loop over the same resident scenes."""
@@ -470,12 +561,13 @@ def measure_batched(ctx, stream, serving=True):
     plain_ms = _time_updates(torch, plain, bframes, 3)
     batch = ddgi.Batch(ctx, items)
     res_b = {"grids": len(specs), "scenes": len(tris), "triangles": sum(tris), "rays": brays,
+             "probes": sum(sp.probes for sp in specs),
              "plain_fp32_ms": plain_ms, "plain_fp32_rays_per_s": brays / plain_ms * 1e3}
-    # launch shape from the autotuner (timed on the BF16 tensor-core form; the trace dominates, so the shape
+    # launch shape from the autotuner, timed on the FP16 tensor-core form (the trace dominates, so the shape
     # carries over to the other convolution modes)
     from anerend_gb300 import autotune
 
-    batch.set_tuning(conv_mode=2, use_graph=1)
+    batch.set_tuning(conv_mode=1, use_graph=1)
     tuned = autotune.tune_batch(batch, bframes, autotune.batch_signature(specs, tris), stream, reps=2, warmup=2,
                                 use_cache=False)
     res_b["autotuned"] = {"tuning": tuned["tuning"], "trials": len(tuned["trials"]), "best_ms": tuned["ms"]}
@@ -484,11 +576,27 @@ def measure_batched(ctx, stream, serving=True):
         ms = _time_updates(torch, lambda fr: batch.update(fr, stream), bframes, 4)
         res_b[f"{name}_ms"] = ms
         res_b[f"{name}_rays_per_s"] = brays / ms * 1e3
-        res_b[f"{name}_probe_updates_per_s"] = sum(sp.probes for sp in specs) / ms * 1e3
-    res_b["speedup_batched_tc_vs_plain"] = plain_ms / res_b["batched_tc_bf16_ms"]
+        res_b[f"{name}_probe_updates_per_s"] = res_b["probes"] / ms * 1e3
     res_b["graph_launches"] = int(batch.stats.graphLaunches)
-    out["batched"] = res_b
     batch.close()
+    # the same grids one at a time with the batch's tuned launch shape and the FP16 tensor-core convolution,
+    # so the gain of batching itself shows beside the gain of the tuned kernels
+    for gg in grids:
+        gg.set_tuning(conv_mode=1)
+    res_b["tuned_per_grid_fp16_ms"] = _time_updates(torch, plain, bframes, 3)
+    # the speed-up claim is made at the FP16 tensor-core form, whose per-texel error against the FP64 oracle
+    # stays within 1e-3 (measured below); BF16 is reported beside it only
+    res_b["speedup_batched_tc_vs_plain"] = plain_ms / res_b["batched_tc_fp16_ms"]
+    res_b["speedup_batched_tc_vs_tuned_per_grid"] = res_b["tuned_per_grid_fp16_ms"] / res_b["batched_tc_fp16_ms"]
+    res_b["speedup_batched_tc_bf16_vs_plain"] = plain_ms / res_b["batched_tc_bf16_ms"]
+    res_b["speedup_mode"] = "FP16 tensor-core convolution (convMode 1)"
+    res_b["conv_rel_err_vs_oracle"] = {
+        name: _batched_conv_error(ctx, stream, specs, scs, tuned["tuning"], conv) for name, conv in
+        (("tc_fp16", 1), ("tc_bf16", 2), ("fp32", 0))}
+    res_b["conv_rel_err_vs_oracle"]["sample"] = ("8 seeded grids of the 64 (hysteresis 0 copies, 2 batched updates), "
+                                                 "up to 256 seeded probes each, oracle.convolve in FP64 on the traced "
+                                                 "FP32 radiance")
+    out["batched"] = res_b
     for gg in grids:
         gg.close()
     for sc in scs:
@@ -503,7 +611,7 @@ def measure_batched(ctx, stream, serving=True):
     sw = scenes.SERVING
     stris = scenes.serving_scene_tris(sw)
     scs = [ddgi.Scene(ctx, scenes.build_scene_tris(t, 2000 + i, bwl.box_lo, bwl.box_hi)) for i, t in enumerate(stris)]
-    srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=2, max_batch_mrays=8)
+    srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=1, max_batch_mrays=8)
     for sc in scs:
         srv.submit(sc, ddgi.grid_desc((4, 4, 4), rays_per_probe=64, hysteresis=0.97),
                    ddgi.FrameParams(camera_pos=(0.0, 0.0, 0.0), rotation=scenes.rotation(0, 0)))
@@ -512,7 +620,7 @@ def measure_batched(ctx, stream, serving=True):
     serv = {"scenes": len(scs), "triangles": sum(stris), "triangles_min": min(stris), "triangles_max": max(stris)}
     for rate, dur in ((2000.0, 1.5), (1000.0, 1.5), (500.0, 2.0), (200.0, 2.0)):
         reqs = scenes.serving_requests(sw, int(rate * dur), rate)
-        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=2, max_batch_mrays=8)
+        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=1, max_batch_mrays=8)
         t0 = time.perf_counter()
         for (ta, si, dms, rr, cam, k) in reqs:
             now = time.perf_counter() - t0
@@ -645,7 +753,9 @@ def run_ours(args, rank, local, world):
     trace_avg_s = sum(trace_ms) / len(trace_ms) / 1e3
     alg_bytes = rays_per_step * (hit_frac * BYTES_PER_HIT + (1 - hit_frac) * BYTES_PER_MISS)
     achieved = alg_bytes / trace_avg_s / 1e9
-    # DRAM bytes of one trace launch, from the ncu capture summarised beside the profile (same workload)
+    # DRAM bytes of one trace launch: copied from the ncu capture of the same kernels on the same workload that
+    # profiles/trace_wavefront_single_grid.md summarises (ncu does not run inside the bench), so it is not a
+    # figure of this run; the line says so in roofline.traffic_source
     traffic = None
     tp = ROOT / "profiles" / "trace_wavefront_single_grid.md"
     if tp.exists():
@@ -685,7 +795,10 @@ def run_ours(args, rank, local, world):
             "roofline": {"kernel": "trace (k_trace_closest + k_shade + k_trace_shadow + k_shadow_resolve)", "bound": "hbm",
                          "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                         "traffic": traffic, "peak_source": peaks["source"],
+                         "traffic": traffic,
+                         "traffic_source": "copied from the ncu capture in profiles/trace_wavefront_single_grid.md, "
+                                           "not measured in this run",
+                         "peak_source": peaks["source"],
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "gpu_launches": launches,

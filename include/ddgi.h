@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DDGI_ABI_VERSION 1
+#define DDGI_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------------------------- */
 #define DDGI_OK            0
@@ -61,6 +61,11 @@ extern "C" {
                                             wrapping like the reference's REPEAT sampler does          */
 #define DDGI_GRID_WRITE_DIRS   (1u << 1) /* also write the per-ray direction image (ProbeRaysDirTex)     */
 #define DDGI_GRID_RECORD_HITS  (1u << 2) /* keep a per-ray hit record (global triangle id, shadow bit)   */
+#define DDGI_GRID_RAYS_RGBA16F (1u << 3) /* ray radiance and direction images in RGBA16F, the format of the
+                                            reference's ProbeRaysIrrTex / ProbeRaysDirTex
+                                            (IrradianceProbeRayTracingPass.cpp:42-74, stored at
+                                            irradiance_probe_update.rgen:108-109; round to nearest even),
+                                            instead of RGBA32F                                          */
 
 /* ---- scene records --------------------------------------------------------------------------------- */
 
@@ -164,17 +169,20 @@ typedef struct DdgiTuning {
   int32_t reserved[2];
 } DdgiTuning;
 
-/* Device views of the grid's buffers (owned by the grid). */
+/* Device views of the grid's buffers (owned by the grid, or the caller's after ddgi_grid_bind_external). */
 typedef struct DdgiGridBuffers {
   void*    atlas;           /* current atlas, atlasFormat texels, atlasWidth x atlasHeight */
-  float*   rayRadiance;     /* RGBA32F ray image, rayWidth x rayHeight (all layers stacked) */
-  float*   rayDirection;    /* RGBA32F ray image, or NULL without DDGI_GRID_WRITE_DIRS */
+  void*    rayRadiance;     /* ray image of rayFormat texels, rayWidth x rayHeight (all layers stacked) */
+  void*    rayDirection;    /* ray image of rayFormat texels, or NULL without DDGI_GRID_WRITE_DIRS */
   int32_t* rayHit;          /* per ray (same texel order): global triangle id or -1; NULL unless RECORD_HITS */
   float*   lattice;         /* N x float4 rotated ray directions of the last trace */
   int32_t  atlasWidth, atlasHeight;
   int32_t  rayWidth, rayHeight;
   int32_t  rayBlockW, rayBlockH;
   uint64_t atlasBytes;
+  uint64_t rayBytes;        /* bytes of one ray image: rayWidth x rayHeight x (16 or 8) */
+  int32_t  rayFormat;       /* DDGI_FORMAT_RGBA32F, or DDGI_FORMAT_RGBA16F with DDGI_GRID_RAYS_RGBA16F */
+  int32_t  reserved;
 } DdgiGridBuffers;
 
 typedef struct DdgiContext DdgiContext;
@@ -194,6 +202,29 @@ const char* ddgi_last_error(const DdgiContext* ctx);
 int         ddgi_sync(DdgiContext* ctx, void* stream);
 int         ddgi_abi_version(void);
 
+/* ---- failure detection ------------------------------------------------------------------------------------ */
+
+/* Bounded device waits. The tensor-core convolution's mbarrier waits give up after spinLimit attempts (about
+ * 64 ns apart); the kernel then raises DDGI_ETIMEDOUT for the next ddgi_sync, stops issuing work, waits for its
+ * own copies and tensor-core work in flight, releases its tensor memory and returns, so the context stays
+ * usable. No counterpart in the reference, whose fence waits never time out (VulkanRenderer.cpp:1156, 4825). */
+typedef struct DdgiWaitConfig {
+  uint32_t spinLimit;    /* attempts per wait before it gives up; 0: the default, 1 << 22 (about 0.3 s) */
+  uint32_t stallTest;    /* test hook, 0 in production: nonzero makes each CTA's first accumulator wait wait for
+                            a phase that no arrival completes, so that the timeout path runs */
+  uint32_t reserved[2];
+} DdgiWaitConfig;
+int ddgi_context_set_waits(DdgiContext* ctx, const DdgiWaitConfig* cfg);
+
+/* Allocation hook: called with the size before each device allocation of a grid (its buffers at creation, the
+ * tensor-core operand buffers on first use, the single-grid trace scratch, the download staging) or of a scene
+ * (its records and shading records; the BVH build's own buffers are not covered). A nonzero return refuses the
+ * allocation: the call that needed it fails with DDGI_ENOMEM and leaves nothing half-built. The hook may run on
+ * the serving loop's worker thread. NULL removes it. No counterpart in the reference, whose allocation failures
+ * print and return (VulkanRenderer.cpp:1356-1358). */
+typedef int (*DdgiAllocHook)(void* user, uint64_t bytes);
+int ddgi_context_set_alloc_hook(DdgiContext* ctx, DdgiAllocHook hook, void* user);
+
 /* ---- scene (replaces BLAS/TLAS builds, VulkanRenderer.cpp:1265-1490, UpdateTLASPass.cpp:128-248) ---- */
 
 /* Copies the host arrays to the device, flattens instances to world-space triangles and builds an LBVH
@@ -211,6 +242,29 @@ int  ddgi_scene_info(const DdgiScene* scene, DdgiSceneInfo* info);
 int  ddgi_grid_create(DdgiContext* ctx, const DdgiGridDesc* desc, DdgiGrid** out);
 void ddgi_grid_destroy(DdgiGrid* grid);
 int  ddgi_grid_buffers(const DdgiGrid* grid, DdgiGridBuffers* out);
+
+/* Caller-owned device buffers for a grid (zero-copy interop with a renderer that owns the images, as the
+ * reference's RenderResourceVault owns "ProbeRaysConvTex", "TempProbeTex", "ProbeRaysIrrTex" and
+ * "ProbeRaysDirTex", IrradianceProbeConvolvePass.cpp:62-99, IrradianceProbeTranslationPass.cpp:20-44,
+ * IrradianceProbeRayTracingPass.cpp:42-74). Each buffer is tightly packed in the grid's layout (rows of
+ * width x texel bytes, no padding), 16-byte aligned, on the grid's device. NULL keeps the current binding. */
+typedef struct DdgiGridExternal {
+  void*    atlas;         /* the current atlas: atlasBytes of atlasFormat texels                        */
+  void*    atlasTemp;     /* the translation temp, atlasBytes; NULL keeps the grid's own                */
+  void*    rayRadiance;   /* the ray radiance image: rayBytes of the grid's ray format                  */
+  void*    rayDirection;  /* the ray direction image (grids with DDGI_GRID_WRITE_DIRS), rayBytes         */
+  uint64_t atlasBytes;    /* must equal DdgiGridBuffers.atlasBytes when atlas or atlasTemp is given      */
+  uint64_t rayBytes;      /* must equal DdgiGridBuffers.rayBytes when a ray image is given              */
+} DdgiGridExternal;
+
+/* Binds caller-owned buffers in place of the grid's own (which are released): from then on the passes read
+ * and write the caller's memory directly, with no copies. A bound atlas is taken as the grid's current
+ * atlas as it stands (ddgi_grid_reset clears it). With a bound atlas the translation pass copies the atlas
+ * into the temp and shifts it back into the atlas, as the reference's pass does (two copies,
+ * IrradianceProbeTranslationPass.cpp:83-168), so the current atlas always stays in the caller's buffer.
+ * Waits for `stream` and for the grid's own work before releasing anything. The caller keeps ownership: the
+ * buffers must outlive the grid or a later binding. DDGI_EINVAL on a size, alignment or option mismatch. */
+int  ddgi_grid_bind_external(DdgiGrid* grid, const DdgiGridExternal* ext, void* stream);
 /* Clears the atlas to (0,0,0,1) and the translation state to (0,0). */
 int  ddgi_grid_reset(DdgiGrid* grid, void* stream);
 /* Device bytes a grid of this description made by ddgi_grid_create holds with the given DdgiTuning.convMode
@@ -264,10 +318,11 @@ int  ddgi_atlas_download_wait(DdgiGrid* grid);
 int  ddgi_atlas_export_rgba16f(DdgiGrid* grid, void* host, uint64_t bytes, void* stream);
 int  ddgi_atlas_import_rgba16f(DdgiGrid* grid, const void* host, uint64_t bytes, void* stream);
 
-/* Reads back the grid's ray buffers into host memory (any pointer may be NULL): radiance is
- * rayWidth*rayHeight RGBA floats, hits rayWidth*rayHeight int32 (needs DDGI_GRID_RECORD_HITS; global triangle
- * id * 2 + shadowed, or -1 for a miss), lattice N float4. The copy is complete when the call returns. */
-int  ddgi_rays_download(DdgiGrid* grid, float* radiance, int32_t* hits, float* lattice, void* stream);
+/* Reads back the grid's ray buffers into host memory (any pointer may be NULL): radiance is the
+ * rayWidth*rayHeight texel ray image in the grid's ray format (DdgiGridBuffers.rayBytes), hits
+ * rayWidth*rayHeight int32 (needs DDGI_GRID_RECORD_HITS; global triangle id * 2 + shadowed, or -1 for a miss),
+ * lattice N float4. The copy is complete when the call returns. */
+int  ddgi_rays_download(DdgiGrid* grid, void* radiance, int32_t* hits, float* lattice, void* stream);
 
 /* ---- dynamic scenes -------------------------------------------------------------------------------------- */
 
@@ -459,21 +514,22 @@ void ddgi_server_destroy(DdgiServer* server);
  * computed in FP64 on the device and stored as N float4 (x, y, z, 0). */
 int  ddgi_fibonacci_lattice(int numRays, const float rot[9], float* dirs, void* stream);
 
-/* probe_conv.comp on device buffers: rayRadiance in the RGBA32F ray-image layout of `desc`, dirs = N float4
- * lattice, atlas in desc->atlasFormat. Updates layers [layerBegin, layerEnd). flags: DDGI_UBO_* bits. */
-int  ddgi_convolve_raw(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs, void* atlas,
+/* probe_conv.comp on device buffers: rayRadiance in the ray-image layout of `desc` (RGBA32F texels, or RGBA16F
+ * with DDGI_GRID_RAYS_RGBA16F in desc->options), dirs = N float4 lattice, atlas in desc->atlasFormat. Updates
+ * layers [layerBegin, layerEnd). flags: DDGI_UBO_* bits. */
+int  ddgi_convolve_raw(const DdgiGridDesc* desc, const void* rayRadiance, const float* dirs, void* atlas,
                        int layerBegin, int layerEnd, uint32_t flags, void* stream);
 
 /* ddgi_convolve_raw for callers that cannot allocate device memory while they update probes (renderers
  * that reserve all memory before the frame loop and forbid allocation inside a frame; processes whose
  * device memory is committed to a budget). It has no counterpart in the reference. The weight scratch
- * lives in a static device array of DDGI_NOALLOC_MAX_RAYS x 64 + 64 floats (132,352 bytes, held on every
+ * lives in a static device array of DDGI_NOALLOC_MAX_RAYS x 64 + 64 floats (131,328 bytes, held on every
  * GPU that loads the library until exit); the call allocates nothing. Returns DDGI_EINVAL when
  * desc->raysPerProbe exceeds DDGI_NOALLOC_MAX_RAYS. The first call on a device looks up the array's
  * address: make it before any stream capture. All calls share the array; calls that overlap on the GPU
  * race on it and must be ordered by the caller. */
 #define DDGI_NOALLOC_MAX_RAYS 512
-int  ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const float* rayRadiance, const float* dirs,
+int  ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const void* rayRadiance, const float* dirs,
                                void* atlas, int layerBegin, int layerEnd, uint32_t flags, void* stream);
 
 /* 16-bit element formats of the tensor-core convolution's radiance and weights */
@@ -488,8 +544,9 @@ int  ddgi_convolve_raw_noalloc(const DdgiGridDesc* desc, const float* rayRadianc
 int  ddgi_convolve_tc_raw(DdgiContext* ctx, const DdgiGridDesc* desc, const void* radiance16, int elemFormat,
                           const float* dirs, void* atlas, int layerBegin, int layerEnd, uint32_t flags,
                           void* stream);
-/* Converts the RGBA32F ray image of layers [layerBegin, layerEnd) into the planar 16-bit layout above. */
-int  ddgi_pack_rays16(const DdgiGridDesc* desc, const float* rayRadiance, void* radiance16, int elemFormat,
+/* Converts the ray image (the format of desc, as ddgi_convolve_raw) of layers [layerBegin, layerEnd) into the
+ * planar 16-bit layout above. */
+int  ddgi_pack_rays16(const DdgiGridDesc* desc, const void* rayRadiance, void* radiance16, int elemFormat,
                       int layerBegin, int layerEnd, void* stream);
 
 /* The translation copy of IrradianceProbeTranslationPass.cpp:83-168 from atlasIn to atlasOut (distinct

@@ -574,6 +574,23 @@ void oracle_lattice(int n, const float rot[9], double* out) {
   }
 }
 
+// The value an RGBA16F image holds after a float32 store of v (the ray images of
+// IrradianceProbeRayTracingPass.cpp:42-74 are R16G16B16A16_SFLOAT): v rounded to float32, then to the nearest
+// binary16 value, ties to even (11-bit significand; subnormal spacing 2^-24 below 2^-14; past 65504 the value
+// rounds to infinity from 65520 on).
+static double storedHalf(double v) {
+  const double x = (double)(float)v;
+  if (!std::isfinite(x) || x == 0.0) return x;
+  const double ax = std::fabs(x);
+  int e = 0;
+  std::frexp(ax, &e);                          // ax = m 2^e, m in [0.5, 1): the leading bit is 2^(e-1)
+  const int lead = std::max(e - 1, -14);
+  const double spacing = std::ldexp(1.0, lead - 10);
+  double r = std::nearbyint(ax / spacing) * spacing;  // ax / spacing is exact; nearbyint rounds ties to even
+  if (r > 65504.0) r = INFINITY;
+  return std::copysign(r, x);
+}
+
 // Traces layers [layerBegin, layerEnd) of a grid (rgen + rchit + rmiss). atlasPrev: RGBA doubles of the
 // atlas before this frame. Outputs in the ray-image layout (rayW x rayH texels): radiance RGBA doubles,
 // hit code (global id * 2 + shadowed, or -1 on a miss) and uncertainty bits (1 primary, 2 shadow).
@@ -619,6 +636,11 @@ int oracle_trace(void* scene, const DdgiGridDesc* desc, const DdgiFrame* f, cons
     int rx = px * g.bw + j % g.bw;
     int ry = (layer * g.Z + pz) * g.bh + j / g.bw;
     size_t idx = (size_t)ry * g.rayW + rx;
+    if (desc->options & DDGI_GRID_RAYS_RGBA16F) {  // the store into the RGBA16F ray image (rgen:108-109)
+      L.x = storedHalf(L.x);
+      L.y = storedHalf(L.y);
+      L.z = storedHalf(L.z);
+    }
     rayRad[4 * idx] = L.x;
     rayRad[4 * idx + 1] = L.y;
     rayRad[4 * idx + 2] = L.z;

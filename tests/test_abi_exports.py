@@ -37,7 +37,7 @@ def test_bindings_cover_header():
 
 def test_abi_version_callable_without_gpu(lib):
     lib.ddgi_abi_version.restype = ctypes.c_int
-    assert lib.ddgi_abi_version() == 1
+    assert lib.ddgi_abi_version() == 2
 
 
 def test_struct_sizes_match_header():

@@ -45,7 +45,8 @@ def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30):
         srv.close()
 
 
-@pytest.mark.parametrize("conv_mode", [0, 1])
+# 1 (FP16 tensor cores) is the mode the serving bench runs
+@pytest.mark.parametrize("conv_mode", [0, 1, 2])
 def test_request_alone_equals_in_the_mix(ctx, conv_mode):
     scs = _scenes(ctx)
     try:

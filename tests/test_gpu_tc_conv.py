@@ -3,7 +3,12 @@
 The inputs are the FP64 radiance R (log-uniform per channel in [1e-3, 1e2], the precision workload's
 distribution); the device sees R rounded to FP16 or BF16 and weights rounded likewise, accumulates in FP32
 and blends in FP32. Stated tolerances, per texel channel relative to the FP64 oracle on the unrounded R:
-FP16 <= 1e-3 (max), BF16 <= 1e-2 (max); against the oracle fed the same rounded R: FP16 <= 2e-3, BF16 <= 8e-3."""
+FP16 <= 1e-3 (max), the bound the engine's batched and served updates are held to; BF16 <= 8e-3 (max). Each
+rounding (of a radiance and of a weight; unit roundoff 2^-11 for FP16, 2^-9 for BF16) moves a weighted mean by
+an amount that grows with the spread of the radiance it averages, here five decades: BF16 measured up to 4.1e-3
+on these inputs and 5.7e-3 on traced radiance, so BF16 does not meet 1e-3 and is offered only as an extra mode.
+Against the oracle fed the same rounded R: FP16 <= 2e-3, BF16 <= 8e-3 (the weights are still rounded to 16 bits
+and the bake sums are not renormalised)."""
 import ctypes as C
 
 import numpy as np
@@ -98,7 +103,7 @@ def test_tc_convolve_matches_fp64(ctx, fmt, n, dims, layers, bake):
     oracle.convolve(d, ray_image(g, r16d), dirs64, want_rounded, b, e, flags)
     err_exact = np.abs(got - want_exact) / np.maximum(np.abs(want_exact), 1e-6)
     err_round = np.abs(got - want_rounded) / np.maximum(np.abs(want_rounded), 1e-6)
-    bound = 1e-3 if fmt == L.DDGI_ELEM_F16 else 1e-2
+    bound = 1e-3 if fmt == L.DDGI_ELEM_F16 else 8e-3
     assert err_exact[..., :3].max() <= bound, (float(err_exact[..., :3].max()), float(np.percentile(err_exact, 99)))
     # weights rounded to 16 bits: FP16 unit roundoff 2^-11, BF16 2^-8 (bake sums are not renormalised)
     assert err_round[..., :3].max() <= (2e-3 if fmt == L.DDGI_ELEM_F16 else 8e-3), float(err_round[..., :3].max())
@@ -120,7 +125,8 @@ def test_tc_rejects_bad_arguments(ctx):
 @pytest.mark.parametrize("conv_mode", [1, 2])
 def test_grid_update_with_tensor_core_convolution(ctx, conv_mode):
     """Full probe updates of the 8x4x8 / 64-ray workload with the tensor-core convolution against the FP64
-    oracle: hits bit-exact on certain rays, atlas within the 16-bit tolerance."""
+    oracle: hits bit-exact on certain rays, atlas within the 16-bit tolerance (FP16 2e-3, BF16 8e-3 at the
+    99.9th percentile: eight hysteresis-blended frames, each feeding the next frame's probe lookup)."""
     w = scenes.CPU_REFERENCE
     arrays = scenes.build_scene(w)
     scene = ddgi.Scene(ctx, arrays)
@@ -139,7 +145,7 @@ def test_grid_update_with_tensor_core_convolution(ctx, conv_mode):
             assert np.array_equal(hits[certain], og.hits[certain])
         atlas = grid.download_atlas().astype(np.float64)
         err = np.abs(atlas - og.atlas) / np.maximum(np.abs(og.atlas), 1e-3)
-        bound = 2e-3 if conv_mode == 1 else 1.5e-2
+        bound = 2e-3 if conv_mode == 1 else 8e-3
         assert np.percentile(err, 99.9) <= bound, np.percentile(err, [50, 99, 99.9, 100])
     finally:
         osc.close()

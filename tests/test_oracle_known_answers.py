@@ -360,3 +360,33 @@ def test_mirror_indirect_term_gated_by_ddgi_flag(flags, indirect):
     if indirect:
         want = want + 0.25 * (np.array([0.2, 0.4, 0.8]) * 0.5 * 3.1415926 * np.array([0.5, 0.6, 0.7]))
     assert np.allclose(out[0, :3], want, rtol=1e-6)  # float32 material inputs
+
+
+def test_rgba16f_ray_image_store_rounds_to_half():
+    # DDGI_GRID_RAYS_RGBA16F: every stored ray radiance is the binary16 value nearest to the FP32 value (the
+    # store into the reference's R16G16B16A16_SFLOAT ray image, rgen:108-109); everything else is unchanged
+    w = scenes.CPU_REFERENCE
+    arrays = scenes.build_scene(w)
+    s = oracle.OracleScene(arrays, L.SceneDesc)
+    try:
+        outs = []
+        for opts in (0, L.DDGI_GRID_RAYS_RGBA16F):
+            d = grid_desc(w.dims, w.rays, 0.97, w.step, w.origin_y, options=opts)
+            g = oracle.OracleGrid(d)
+            fp = L.Frame()
+            fp.lightDir[:] = list(np.array(w.light_dir) / np.linalg.norm(w.light_dir))
+            fp.sunIntensity, fp.skyIntensity = w.sun, w.sky_intensity
+            fp.skyColor[:] = list(w.sky)
+            fp.flags = L.DDGI_UBO_DDGI_FLAG | L.DDGI_UBO_DDGI_MULTI_FLAG
+            fp.rotation[:] = scenes.rotation(w.seed, 0).tolist()
+            fp.layer = -1
+            g.trace(s, fp)
+            outs.append((g.ray_rad.copy(), g.hits.copy()))
+        (full, hits0), (half, hits1) = outs
+        assert np.array_equal(hits0, hits1)
+        want = full[..., :3].astype(np.float32).astype(np.float16).astype(np.float64)
+        assert np.array_equal(half[..., :3], want)
+        assert np.array_equal(half[..., 3], full[..., 3])
+        assert not np.array_equal(half, full)
+    finally:
+        s.close()
