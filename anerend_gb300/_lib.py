@@ -111,7 +111,12 @@ class BatchStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memoryBudget", C.c_uint64), ("maxBatch", C.c_int32), ("inFlight", C.c_int32),
-                ("convMode", C.c_int32), ("maxBatchMRays", C.c_uint32), ("reserved", C.c_int32 * 4)]
+                ("convMode", C.c_int32), ("maxBatchMRays", C.c_uint32), ("policy", C.c_int32),
+                ("agingMs", C.c_float), ("reserved", C.c_int32 * 2)]
+
+
+DDGI_SERVE_FIFO = 0
+DDGI_SERVE_SHORTEST_FIRST = 1
 
 
 class Request(C.Structure):

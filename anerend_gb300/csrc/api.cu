@@ -136,6 +136,9 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
   std::vector<int> order(g->g.N);
   if (t.rayOrder == 1) order = mortonRayOrder(g->g.N);
   else for (int i = 0; i < g->g.N; ++i) order[i] = i;
+  // the inverse after it: the shading walks rays in direction order and finds each one's trace slot
+  order.resize(2 * (size_t)g->g.N);
+  for (int i = 0; i < g->g.N; ++i) order[g->g.N + order[i]] = i;
   if (g->asyncAlloc)  // pageable source: the call returns once the data is staged
     CK(cudaMemcpyAsync(g->order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, g->allocStream),
        "ray order upload");
@@ -156,6 +159,13 @@ int frameToGPU(DdgiContext* ctx, const DdgiFrame* f, FrameGPU& out) {
   out.skyColor = f3(f->skyColor[0], f->skyColor[1], f->skyColor[2]);
   out.sunIntensity = f->sunIntensity;
   out.skyIntensity = f->skyIntensity;
+  // the miss shader's sky (rmiss:20): toLinear (bindless.glsl:240-247) of skyIntensity * skyColor
+  float sky[3];
+  for (int k = 0; k < 3; ++k) {
+    const float c = f->skyColor[k] * f->skyIntensity;
+    sky[k] = c < 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
+  }
+  out.skyLinear = f3(sky[0], sky[1], sky[2]);
   out.flags = f->flags;
   for (int i = 0; i < 3; ++i) out.bakeTile[i] = f->bakeTileInfo[i];
   if ((f->flags & DDGI_UBO_BAKE_MODE_ON_FLAG) && f->bakeTileInfo[2] <= 0)
@@ -301,7 +311,7 @@ uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds) {
   uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rayTexel = g.rayFmt == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rays = (uint64_t)g.rayW * g.bh * g.Z * g.Y;
-  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + rayTexel * rays + 16ull * g.N + 4ull * g.N +
+  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + rayTexel * rays + 16ull * g.N + 8ull * g.N +
                    4ull * g.N * kOctTexels + 4ull * kOctTexels;
   if (d->options & DDGI_GRID_WRITE_DIRS) bytes += rayTexel * rays;
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
@@ -335,7 +345,7 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
   if (e == cudaSuccess && (desc->options & DDGI_GRID_WRITE_DIRS)) e = gridAlloc(g, &g->rayDir, g->rayBytes);
   if (e == cudaSuccess && (desc->options & DDGI_GRID_RECORD_HITS)) e = gridAlloc(g, (void**)&g->rayHit, 4 * rayTexels);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->lattice, 16 * (size_t)g->g.N);
-  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, sizeof(int) * (size_t)g->g.N);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, 2 * sizeof(int) * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wt, 4 * (size_t)g->g.N * kOctTexels);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wsum, 4 * kOctTexels);
   if (!asyncAlloc) {  // closest-hit seeding for grids traced frame after frame

@@ -9,10 +9,12 @@
 // warp loads the three radiance tiles (64-row boxes, one or two per channel) and the 64 x 64 weight tile
 // (SWIZZLE_128B); one thread of the MMA warp issues 4 K-steps x 3 channels of tcgen05.mma (M = 128 probe
 // rows, N = 64 texels, K = 16) into FP32 accumulators in TMEM (3 x 64 columns, double-buffered = 384 of 512
-// columns); the rows of a one-unit tile past its 64 probes hold stale operands and are never read. Eight
-// epilogue warps read the accumulators with tcgen05.ld (thread = probe), stage them in shared memory and walk
-// the atlas coalesced (lanes = 4 probes x 8 texels of a row), normalising by the texel's weight sum and
-// applying the hysteresis blend (or the bake accumulation) in FP32 against the old atlas texel.
+// columns); the rows of a one-unit tile past its 64 probes hold stale operands and are never read. Sixteen
+// epilogue warps (four per TMEM lane quarter, one texel block of 16 texels each) read the accumulators with
+// tcgen05.ld (thread = probe), stage them in shared memory and walk the atlas coalesced (lanes = 4 probes x 8
+// texels of a row), normalising by the texel's weight sum and applying the hysteresis blend (or the bake
+// accumulation) in FP32 against the old atlas texel. The epilogue is bound by the latency of its atlas
+// read-modify-write, so its warps come before operand stages in the shared-memory budget: two stages.
 // A single-item launch carries its record and tensor maps in the kernel parameters (TcOne); a batch reads
 // its records from device memory (TcMany), so a captured launch sees per-frame values written between replays.
 //
@@ -36,18 +38,21 @@ namespace {
 constexpr int kTileP = 128;                  // probe rows per tile (MMA M)
 constexpr int kUnitP = 64;                   // probes per work unit (one TMA box of radiance rows)
 constexpr int kChunkK = 64;                  // rays per K-chunk (128 bytes of 16-bit values)
-constexpr int kStages = 3;  // 3 x 56 KB of operand staging
+constexpr int kStages = 2;  // 2 x 56 KB of operand staging (the epilogue's 16 staging areas take the rest)
 constexpr int kATileBytes = kTileP * kChunkK * 2;   // 16 KB per channel
 constexpr int kAUnitBytes = kUnitP * kChunkK * 2;   // 8 KB: one unit's rows of one channel
 constexpr int kWTileBytes = kOctTexels * kChunkK * 2;  // 8 KB
 constexpr int kStageBytes = 3 * kATileBytes + kWTileBytes;  // 56 KB
 constexpr int kTmemCols = 512;
-constexpr int kEpiWarps = 8;                 // two per TMEM lane quarter, each on half of the texel blocks
-constexpr int kThreadsTc = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int kEpiWarps = 16;                // four per TMEM lane quarter, one texel block each
+constexpr int kBlocksPerWarp = 16 / kEpiWarps;  // 16 (quarter, texel block) pairs per tile
+constexpr int kThreadsTc = 64 + 32 * kEpiWarps;  // warp 0 TMA, warp 1 MMA, warps 2-17 epilogue
 // epilogue staging: per epilogue warp, 3 channels x 32 probes x 16 texels of one texel block (row stride 17)
 constexpr int kStageRow = 17;
 constexpr int kStageWarpFloats = 3 * 32 * kStageRow;
 constexpr size_t kSmemTc = (size_t)kStages * kStageBytes + kEpiWarps * kStageWarpFloats * sizeof(float) + 1024;
+static_assert(kSmemTc <= 227 * 1024, "operand stages and epilogue staging exceed a CTA's shared memory");
+static_assert(kEpiWarps % 4 == 0 && 16 % kEpiWarps == 0, "epilogue warps cover the 4 lane quarters evenly");
 // attempts of a wait for the kernel's own copies and MMAs in flight before the CTA exits (after a timeout)
 constexpr uint32_t kDrainLimit = 1u << 22;
 
@@ -354,9 +359,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
     }
   } else {
-    // ---- epilogue: warps 2..9 ----
-    // A warp may read TMEM lanes 32q..32q+31 with q = warp % 4 (its probe rows); the two warps of a quarter
-    // split the four blocks of 16 texels between them. Per block (two texel rows)
+    // ---- epilogue: warps 2 .. 1 + kEpiWarps ----
+    // A warp may read TMEM lanes 32q..32q+31 with q = warp % 4 (its probe rows); the warps of a quarter
+    // split the four blocks of 16 texels between them (kBlocksPerWarp each). Per block (two texel rows)
     // it reads its rows' accumulators (thread = probe), stages them in shared memory and then walks the
     // atlas coalesced: per step its lanes cover 4 probes x the 8 texels of one row (4 runs of 128 bytes).
     // The old texels do not depend on the MMA, so their loads are issued before the accumulator wait. A warp
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     // arrivals on accEmpty stay in the phase of their tile.
     gridDependencyWait();  // the weight sums come from the kernel launched just before this one
     const int quarter = warp & 3;  // TMEM lane quarter this warp may access
-    const int half = (warp - 2) >> 2;  // which two texel blocks
+    const int blk0 = ((warp - 2) >> 2) * kBlocksPerWarp;  // its texel blocks: blk0 .. blk0 + kBlocksPerWarp - 1
     float* stage = reinterpret_cast<float*>(smem + (size_t)kStages * kStageBytes) + (warp - 2) * kStageWarpFloats;
     const int tx = lane & 7, pp = lane >> 3;
     int local = 0;
@@ -377,14 +382,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       const int tileEnd = min(it.pEnd, tile.p0 + tile.units * kUnitP);
       // atlas offsets of the 8 probes this lane visits (probe 4g + pp of the warp's 32), texel (tx, 0)
       const int warpProbe0 = tile.p0 + quarter * 32;
-      size_t base[8];
+      // texel indices fit 32 bits: an atlas holds at most 2^31 texels (checked when its grid is described)
+      uint32_t base[8];
       uint32_t liveMask = 0;
 #pragma unroll
       for (int g = 0; g < 8; ++g) {
         const int probe = warpProbe0 + 4 * g + pp;
         const bool live = probe < tileEnd;
         const int px = live ? probe % it.X : 0, pzAll = live ? probe / it.X : 0;  // pzAll = layer * Z + z
-        base[g] = (size_t)(kProbePix * pzAll + 1) * it.atlasW + (kProbePix * px + 1 + tx);
+        base[g] = (uint32_t)(kProbePix * pzAll + 1) * (uint32_t)it.atlasW + (uint32_t)(kProbePix * px + 1 + tx);
         liveMask |= (live ? 1u : 0u) << g;
       }
       const bool rowsLive = warpProbe0 < tileEnd;  // warp-uniform
@@ -405,16 +411,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         tcFenceAfter();
       }
 #pragma unroll 1
-      for (int blk = 2 * half; rowsLive && blk < 2 * half + 2; ++blk) {
-        // step k: probe group k >> 1, texel row ty = 2 blk + (k & 1)
-        float4 olds[16];
+      for (int blk = blk0; rowsLive && blk < blk0 + kBlocksPerWarp; ++blk) {
+        // step g of row r: probe 4g + pp, texel row ty = 2 blk + r. The first row's old texels are loaded
+        // before the accumulator wait, the second row's once the first row is written (register budget).
+        float4 olds[8];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const int g = k >> 1, ty = 2 * blk + (k & 1);
-          olds[k] = (liveMask >> g) & 1u ? loadTexel(it.atlas, it.atlasFmt, base[g] + (size_t)ty * it.atlasW)
+        for (int g = 0; g < 8; ++g)
+          olds[g] = (liveMask >> g) & 1u ? loadTexel(it.atlas, it.atlasFmt, base[g] + (uint32_t)(2 * blk) * it.atlasW)
                                          : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        if (blk == 2 * half) {
+        if (blk == blk0) {
           // warp-uniform outcome: the tcgen05.ld below is warp-collective
           if (!__all_sync(0xffffffffu, mbarWait(&accFull[b], accPhase, waits.spin))) {
             if (lane == 0) fail();
@@ -423,15 +428,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
           }
           tcFenceAfter();
         }
-        float cr[16], cg[16], cb[16];
-        tmemLoad16(laneAddr + 0 * kOctTexels + blk * 16, cr);
-        tmemLoad16(laneAddr + 1 * kOctTexels + blk * 16, cg);
-        tmemLoad16(laneAddr + 2 * kOctTexels + blk * 16, cb);
+        // one channel at a time, so only 16 accumulator values are live next to the old texels
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {  // thread = probe row `lane`: conflict-free (stride 17)
-          stage[0 * 32 * kStageRow + lane * kStageRow + i] = cr[i];
-          stage[1 * 32 * kStageRow + lane * kStageRow + i] = cg[i];
-          stage[2 * 32 * kStageRow + lane * kStageRow + i] = cb[i];
+        for (int c = 0; c < 3; ++c) {
+          float cv[16];
+          tmemLoad16(laneAddr + c * kOctTexels + blk * 16, cv);
+#pragma unroll
+          for (int i = 0; i < 16; ++i)  // thread = probe row `lane`: conflict-free (stride 17)
+            stage[c * 32 * kStageRow + lane * kStageRow + i] = cv[i];
         }
         __syncwarp();
         const int tex0 = 2 * blk * kOct + tx;  // texel (tx, 2 blk); + 8 for the second row
@@ -439,12 +443,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         const float s16b = __ldg(&it.wsum16[tex0 + kOct]), s32b = __ldg(&it.wsum32[tex0 + kOct]);
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-          const int g = k >> 1, row2 = k & 1, ty = 2 * blk + row2;
+          const int g = k & 7, row2 = k >> 3, ty = 2 * blk + row2;
+          if (k == 8) {  // the second row's old texels
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+              olds[q] = (liveMask >> q) & 1u ? loadTexel(it.atlas, it.atlasFmt, base[q] + (uint32_t)ty * it.atlasW)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
           if (!((liveMask >> g) & 1u)) continue;
           const int sp = (4 * g + pp) * kStageRow + row2 * kOct + tx;
           const float rr0 = stage[sp], gg0 = stage[32 * kStageRow + sp], bb0 = stage[2 * 32 * kStageRow + sp];
           const float s16 = row2 ? s16b : s16a, s32 = row2 ? s32b : s32a;
-          const float4 old = olds[k];
+          const float4 old = olds[g];
           float4 out;
           if (bake) {
             float tw = old.w + s32;
@@ -456,7 +466,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
             if (s16 > 1e-6f) { float inv = 1.0f / s16; rr *= inv; gg *= inv; bb *= inv; }
             out = make_float4(rr * a + old.x * h, gg * a + old.y * h, bb * a + old.z * h, s32 * a + old.w * h);
           }
-          storeTexel(it.atlas, it.atlasFmt, base[g] + (size_t)ty * it.atlasW, out);
+          storeTexel(it.atlas, it.atlasFmt, base[g] + (uint32_t)ty * it.atlasW, out);
         }
         __syncwarp();  // the stage is rewritten by the next block
       }

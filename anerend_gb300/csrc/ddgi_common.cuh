@@ -260,6 +260,7 @@ struct GridGPU {
 
 struct FrameGPU {
   float3 camPos, lightDir, skyColor;
+  float3 skyLinear;  // toLinear(skyIntensity * skyColor) (rmiss:20), computed once per frame on the host
   float sunIntensity, skyIntensity;
   uint32_t flags;
   int layerBegin, layerEnd;

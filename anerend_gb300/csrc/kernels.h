@@ -17,7 +17,7 @@ struct TraceItem {
   GridGPU g;
   FrameGPU f;
   const float4* lattice;  // written by the batched lattice kernel
-  const int* order;
+  const int* order;       // 2N ints: the trace's direction order, then its inverse (the position of each direction)
   const void* atlasPrev;
   void* rayRad;  // ray images in g.rayFmt texels
   void* rayDir;
@@ -45,11 +45,12 @@ cudaError_t launchShadingRecords(const SceneGPU& s, uint64_t numIndices, uint64_
 long long traceWarps(const GridGPU& g, const FrameGPU& f);
 // Device counters of one trace launch: closest-hit queue, shadow-list length, shadow queue, spare.
 constexpr int kTraceCounters = 4;
-// Scratch of one trace launch per ray slot: the hit record and the shadow-list entry (16 B each).
-constexpr size_t kTraceScratchPerRay = 32;
+// Scratch of one trace launch per ray slot: the hit record (16 B) and the shadow-list entry (32 B: the shadow
+// ray's origin and ray id, then the shadowed radiance and the candidate / found occluder).
+constexpr size_t kTraceScratchPerRay = 48;
 // Lattices of every item (rotation per item), then the wavefront trace of all items' ray slots:
-// closest-hit traversal, shading, shadow traversal, shadowed-ray resolve. dHits and dShadow hold
-// 32 * totalWarps float4 each. hItems / hRot: a single record and its rotation on the host, passed to every
+// closest-hit traversal, shading, shadow traversal, shadowed-ray resolve. dHits holds 32 * totalWarps float4,
+// dShadow twice that. hItems / hRot: a single record and its rotation on the host, passed to every
 // kernel by value (constant-bank reads; dItems and dRots are not read), otherwise the kernels read dItems and
 // dRots. The lattice kernel zeroes dCounters, so no copy or memset runs ahead of the launches.
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,

@@ -98,7 +98,7 @@ struct DdgiGrid {
   void* rayDir = nullptr;
   int* rayHit = nullptr;
   float4* lattice = nullptr;
-  int* order = nullptr;   // trace-kernel direction order (N ints)
+  int* order = nullptr;   // trace-kernel direction order (N ints), then its inverse (N ints)
   // closest-hit seeding (grids made by ddgi_grid_create; served grids trace once and keep none): the last
   // traced lattice, per direction the nearest direction of that lattice, and per (probe, direction) the
   // closest-hit record of the last trace (-1 for a miss)

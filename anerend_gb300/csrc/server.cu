@@ -1,7 +1,7 @@
 // Serving loop: continuous batching of probe-update requests over resident scenes.
 //
-// A worker thread owns the device side. Requests are admitted first-in first-out while their grids' memory
-// fits the budget and a launch slot is free; each admitted request gets a grid allocated stream-ordered on
+// A worker thread owns the device side. Requests are admitted, in arrival order or shortest first with aging
+// (DdgiServerConfig.policy), while their grids' memory fits the budget and a launch slot is free; each admitted request gets a grid allocated stream-ordered on
 // the slot's stream (no device synchronization), and the admitted set is launched as one batch (persistent
 // trace over all of their rays + one convolution launch). Up to `inFlight` batches run at once on separate
 // streams, so requests that arrive while others are on the GPU are admitted as slots and memory free up and
@@ -68,6 +68,50 @@ struct DdgiServer {
 
 namespace {
 
+// The next pending request to admit (its index in s->pending), or -1. FIFO: the head. Shortest first: the
+// smallest aged ray count, rays x max(0, 1 - wait / agingMs), ties to the older request. Either way the pick
+// must fit the memory budget, or nothing is admitted until memory frees up (a request that cannot fit now is
+// not overtaken, so it is not starved); with `capLeft` > 0 it must also fit the launch's remaining ray cap,
+// else the scan takes the next fitting one (the request waits for the next launch). Called with the lock held.
+long pickNext(const DdgiServer* s, uint64_t capLeft, bool capApplies, double now) {
+  if (s->pending.empty()) return -1;
+  if (s->cfg.policy != DDGI_SERVE_SHORTEST_FIRST) {
+    const Req* r = s->pending.front();
+    if (s->usedBytes + r->bytes > s->cfg.memoryBudget) return -1;
+    if (capApplies && r->rays > capLeft) return -1;
+    return 0;
+  }
+  const double aging = (s->cfg.agingMs > 0.f ? s->cfg.agingMs : 50.0f) * 1e-3;
+  long best = -1;
+  double bestKey = 0;
+  for (size_t i = 0; i < s->pending.size(); ++i) {
+    const Req* r = s->pending[i];
+    const double key = (double)r->rays * std::max(0.0, 1.0 - (now - r->tSubmit) / aging);
+    if (best < 0 || key < bestKey) {  // pending is in arrival order: ties keep the older request
+      best = (long)i;
+      bestKey = key;
+    }
+  }
+  const Req* r = s->pending[(size_t)best];
+  if (s->usedBytes + r->bytes > s->cfg.memoryBudget) return -1;
+  if (capApplies && r->rays > capLeft) {
+    // the top pick waits for the next launch; fill this one with the best that fits the remaining cap
+    long fit = -1;
+    double fitKey = 0;
+    for (size_t i = 0; i < s->pending.size(); ++i) {
+      const Req* q = s->pending[i];
+      if (q->rays > capLeft || s->usedBytes + q->bytes > s->cfg.memoryBudget) continue;
+      const double key = (double)q->rays * std::max(0.0, 1.0 - (now - q->tSubmit) / aging);
+      if (fit < 0 || key < fitKey) {
+        fit = (long)i;
+        fitKey = key;
+      }
+    }
+    return fit;
+  }
+  return best;
+}
+
 // Completes the batches whose events have fired; called with the lock held.
 void reap(DdgiServer* s) {
   for (Slot& sl : s->slots) {
@@ -109,11 +153,13 @@ void workerLoop(DdgiServer* s) {
     uint64_t batchRays = 0;
     const uint64_t rayCap = (uint64_t)s->cfg.maxBatchMRays * 1000000ull;
     if (free) {
+      const double tNow = s->now();
       while (!s->pending.empty() && (int)batch.size() < s->cfg.maxBatch) {
-        Req* r = s->pending.front();
-        if (s->usedBytes + r->bytes > s->cfg.memoryBudget) break;  // head of line waits for memory
-        if (rayCap && !batch.empty() && batchRays + r->rays > rayCap) break;  // the next launch takes it
-        s->pending.pop_front();
+        const bool capApplies = rayCap && !batch.empty();
+        const long pick = pickNext(s, capApplies ? rayCap - std::min(rayCap, batchRays) : 0, capApplies, tNow);
+        if (pick < 0) break;  // waits for memory, or for the next launch
+        Req* r = s->pending[(size_t)pick];
+        s->pending.erase(s->pending.begin() + pick);
         int rc = gridCreate(s->ctx, &r->r.grid, free->stream, true, &r->grid);
         if (!rc) rc = tuneGridForBatch(r->grid, s->tuning);
         if (rc) {
@@ -207,7 +253,10 @@ int ddgi_server_create(DdgiContext* ctx, const DdgiServerConfig* cfg, DdgiServer
   *out = nullptr;
   if (cfg->memoryBudget == 0) return fail(ctx, DDGI_EINVAL, "memoryBudget must be > 0");
   if (cfg->maxBatch < 1 || cfg->maxBatch > 64) return fail(ctx, DDGI_EINVAL, "maxBatch must be in [1, 64]");
-  if (cfg->inFlight < 1 || cfg->inFlight > 4) return fail(ctx, DDGI_EINVAL, "inFlight must be in [1, 4]");
+  if (cfg->inFlight < 1 || cfg->inFlight > 8) return fail(ctx, DDGI_EINVAL, "inFlight must be in [1, 8]");
+  if (cfg->policy != DDGI_SERVE_FIFO && cfg->policy != DDGI_SERVE_SHORTEST_FIRST)
+    return fail(ctx, DDGI_EINVAL, "serving policy %d unknown", cfg->policy);
+  if (!(cfg->agingMs >= 0.0f)) return fail(ctx, DDGI_EINVAL, "agingMs must be >= 0");
   DdgiBatchTuning t = defaultBatchTuning();
   t.convMode = cfg->convMode;
   t.useGraph = 0;  // a new item set per launch

@@ -36,21 +36,46 @@ __global__ void k_lattice(int n, Mat3 rot, float4* __restrict__ out) {
 // ---------------------------------------------------------------------------------------------------
 // Previous-frame probe lookup: sampleSingleProbe / weightProbe / sampleProbe (pbr_light.glsl:168-363).
 // Bilinear filtering is done in texel space in FP32 (the reference's REPEAT + LINEAR sampler, so texel
-// indices wrap around the atlas; DDGI_GRID_EDGE_CLAMP clamps the probe index instead).
-DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int iy, int iz, float3 n) {
+// indices wrap around the atlas; DDGI_GRID_EDGE_CLAMP clamps the probe index instead). The octahedral
+// position of the normal, and so the texel offsets and bilinear weights inside a probe's block, are the same
+// for the eight probes of a lookup: OctTap holds them, computed once per lookup.
+struct OctTap {
+  int dx0, dy0;              // offset of the 2 x 2 footprint inside a probe's 10 x 10 block (from texel (1, 1))
+  float w00, w10, w01, w11;  // bilinear weights
+};
+
+DDGI_D OctTap octTap(float3 n) {
+  const float2 o = octEncode(normalize3(n));
+  const float ox = (o.x + 1.0f) * 0.5f * (float)(kOct - 1);
+  const float oy = (o.y + 1.0f) * 0.5f * (float)(kOct - 1);
+  const float fx0 = floorf(ox), fy0 = floorf(oy);
+  const float fx = ox - fx0, fy = oy - fy0;
+  OctTap t;
+  t.dx0 = (int)fx0;
+  t.dy0 = (int)fy0;
+  t.w00 = (1.0f - fx) * (1.0f - fy);
+  t.w10 = fx * (1.0f - fy);
+  t.w01 = (1.0f - fx) * fy;
+  t.w11 = fx * fy;
+  return t;
+}
+
+// Square root of a non-negative blend of texels (sqrt.approx.f32: within 2^-23 relative, one instruction);
+// the reference's shader sqrt is not correctly rounded either.
+DDGI_D float sqrtBlend(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int iy, int iz, const OctTap& tap) {
   if (g.options & DDGI_GRID_EDGE_CLAMP) {
     ix = min(max(ix, 0), g.X - 1);
     iy = min(max(iy, 0), g.Y - 1);
     iz = min(max(iz, 0), g.Z - 1);
   }
-  int sx = kProbePix * ix + 1;
-  int sy = kProbePix * g.Z * iy + kProbePix * iz + 1;
-  float2 o = octEncode(normalize3(n));
-  float ox = (o.x + 1.0f) * 0.5f * (float)(kOct - 1);
-  float oy = (o.y + 1.0f) * 0.5f * (float)(kOct - 1);
-  float fx0 = floorf(ox), fy0 = floorf(oy);
-  float fx = ox - fx0, fy = oy - fy0;
-  int x0 = sx + (int)fx0, y0 = sy + (int)fy0;
+  int x0 = kProbePix * ix + 1 + tap.dx0;
+  int y0 = kProbePix * g.Z * iy + kProbePix * iz + 1 + tap.dy0;
   int x1 = x0 + 1, y1 = y0 + 1;
   // The indices are never negative (ix, iy, iz >= 0; the octahedral offset is >= -1 and sx, sy >= 1) and
   // stay below W + 10 and H + 10 Z + 10 <= 3 H. REPEAT: conditional subtractions equal the modulo;
@@ -72,8 +97,7 @@ DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int
   float4 t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
   float4 t01 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x0);
   float4 t11 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x1);
-  float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
-  return xyz(t00) * w00 + xyz(t10) * w10 + xyz(t01) * w01 + xyz(t11) * w11;
+  return xyz(t00) * tap.w00 + xyz(t10) * tap.w10 + xyz(t01) * tap.w01 + xyz(t11) * tap.w11;
 }
 
 DDGI_D void probeFrame(const GridGPU& g, const FrameGPU& f, float3& stepv, float3& offv) {
@@ -102,6 +126,7 @@ DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas
   float3 alpha = clamp3((wp - base) / stepv, 0.0f, 1.0f);
   // corner order of pbr_light.glsl:318-355
   const int corners[8][3] = {{0, 0, 0}, {1, 1, 1}, {1, 1, 0}, {1, 0, 0}, {0, 1, 1}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}};
+  const OctTap tap = octTap(n);
   float sumW = 0.0f;
   float3 sumI = f3(0.f, 0.f, 0.f);
 #pragma unroll
@@ -115,12 +140,12 @@ DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas
     w = fmaxf(0.000001f, w);
     if (w < 0.2f) w *= w * w * (1.0f / (0.2f * 0.2f));
     w *= tri.x * tri.y * tri.z;
-    float3 irr = sampleSingleProbe(g, atlas, px + ox, py + oy, pz + oz, n);
-    irr = f3(sqrtf(irr.x), sqrtf(irr.y), sqrtf(irr.z));
+    float3 irr = sampleSingleProbe(g, atlas, px + ox, py + oy, pz + oz, tap);
+    irr = f3(sqrtBlend(irr.x), sqrtBlend(irr.y), sqrtBlend(irr.z));
     sumI += irr * w;
     sumW += w;
   }
-  float3 net = sumI / sumW;
+  float3 net = sumI * (1.0f / sumW);
   net = net * net;
   return net * 0.5f * kPiSampleProbe;
 }
@@ -187,6 +212,41 @@ DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restric
   r.px = p % g.X;
   r.pz = p / g.X;
   r.valid = true;
+  return r;
+}
+
+// A ray by its natural id: the item-local index ((layer - layerBegin) * PG * WP + q) * N + j over the layer's
+// probes q (padded to whole probe groups, as the trace slots are) and the directions j. Consecutive ids are
+// consecutive directions of one probe, so the per-ray outputs indexed by (probe, direction) are written
+// coalesced by the shading kernels, which walk rays in this order. `slot` is the ray's item-local trace slot
+// (raySlot's inverse): warp ((layer - layerBegin) * PG + q / WP) * (N / D) + pos / D, lane (q % WP) * D + pos % D,
+// with pos the direction's position in the trace order (order[N + j]). N, WP and D are powers of two.
+struct NaturalRay {
+  RaySlot rs;
+  uint32_t slot;
+};
+
+DDGI_D NaturalRay naturalRay(const GridGPU& g, const FrameGPU& f, const int* __restrict__ order, uint32_t local) {
+  NaturalRay r;
+  r.rs.valid = false;
+  r.slot = 0;
+  const uint32_t lgN = (uint32_t)(__ffs(g.N) - 1), lgWP = (uint32_t)(__ffs(g.warpProbes) - 1), lgD = 5u - lgWP;
+  const uint32_t XZ = (uint32_t)(g.X * g.Z);
+  const uint32_t PG = (XZ + (uint32_t)g.warpProbes - 1u) >> lgWP;
+  const uint32_t perLayer = PG << (lgWP + lgN);
+  const uint32_t lq = local / perLayer;
+  const uint32_t rem = local - lq * perLayer;
+  const uint32_t q = rem >> lgN, j = rem & ((uint32_t)g.N - 1u);
+  const int layer = f.layerBegin + (int)lq;
+  if (layer >= f.layerEnd || q >= XZ) return r;
+  const uint32_t pos = (uint32_t)__ldg(&order[g.N + (int)j]);
+  const uint32_t pg = q >> lgWP, qq = q & ((uint32_t)g.warpProbes - 1u);
+  r.slot = (((lq * PG + pg) << (lgN - lgD)) + (pos >> lgD)) * 32u + (qq << lgD) + (pos & ((1u << lgD) - 1u));
+  r.rs.layer = layer;
+  r.rs.j = (int)j;
+  r.rs.px = (int)(q % (uint32_t)g.X);
+  r.rs.pz = (int)(q / (uint32_t)g.X);
+  r.rs.valid = true;
   return r;
 }
 
@@ -449,36 +509,42 @@ cudaError_t launchShadingRecords(const SceneGPU& s, uint64_t numIndices, uint64_
   return cudaGetLastError();
 }
 
-// Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray slot. A hit's radiance is
-// computed both lit and shadowed, in the reference's order of operations; the lit value is stored and the
-// shadow ray is appended to shadowList (counters[1]) with the shadowed value parked in the hit record.
+// Hit shading (rchit:134-221) and misses (rmiss:17-21), one thread per ray in natural order (consecutive
+// threads = consecutive directions of one probe, so the ray image, the 16-bit radiance and the hit memo are
+// written coalesced; each thread reads its ray's hit record from the trace slot naturalRay gives). A hit's
+// radiance is computed both lit and shadowed, in the reference's order of operations; the lit value is stored
+// and the shadow ray is appended to shadowList (counters[1]) as two records: its origin and natural ray id,
+// then the shadowed value and the candidate occluder.
 template <class Src>
 __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src src, long long totalRays,
-                                               float4* __restrict__ hits, float4* __restrict__ shadowList,
+                                               const float4* __restrict__ hits, float4* __restrict__ shadowList,
                                                unsigned long long* __restrict__ counters) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < totalRays;
        id += (long long)gridDim.x * blockDim.x) {
-    const float4 hr = hits[id];
-    const int leaf = __float_as_int(hr.x);
     bool cast = false;
-    float3 so = f3(0.f, 0.f, 0.f);
-    if (leaf != kNoRay) {
-      const long long warp = id >> 5;
-      const TraceItem& T = src.at(warp);
+    float3 so = f3(0.f, 0.f, 0.f), Ls = f3(0.f, 0.f, 0.f);
+    int occ = -1;
+    const long long warp = id >> 5;  // natural ids share the items' slot ranges
+    const TraceItem& T = src.at(warp);
+    const NaturalRay nr = naturalRay(T.g, T.f, T.order, (uint32_t)(id - 32 * T.warpBegin));
+    if (nr.rs.valid) {
       const SceneGPU& s = T.s;
       const GridGPU& g = T.g;
       const FrameGPU& f = T.f;
-      const RaySlot rs = raySlot(g, f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
+      const RaySlot& rs = nr.rs;
+      const float4 hr = hits[32 * T.warpBegin + nr.slot];
+      const int leaf = __float_as_int(hr.x);
       const float3 origin = probeOrigin(g, f, rs);
       const float3 dir = xyz(__ldg(&T.lattice[rs.j]));
+      const size_t pj = (((size_t)rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N;
       if (T.hitMemo)  // this trace's closest-hit record, the next trace's seed candidate
-        T.hitMemo[(((size_t)rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N + rs.j] = leaf >= 0 ? leaf : -1;
+        T.hitMemo[pj + rs.j] = leaf >= 0 ? leaf : -1;
       float3 L;
       int hitCode = -1;
       if (leaf < 0) {
-        L = toLinear(f.skyColor * f.skyIntensity);  // rmiss:20
+        L = f.skyLinear;  // rmiss:20
       } else {
         float4 r0;
         const HitSurface h = shadeSurface(s, leaf, hr.z, hr.w, r0);
@@ -493,7 +559,6 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         }
         // lit: L = calcLight; shadowed: L = 0; then += indirect, += emissive (rchit:195-214)
         L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, pos, origin, f.lightDir, f.sunIntensity);
-        float3 Ls = f3(0.f, 0.f, 0.f);
         if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG) {
           const float3 ind = calcIndirectDiffuse(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
           L += ind;
@@ -506,14 +571,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         // is cast only when the values differ or the caller records per-ray hit codes (their shadow bit).
         cast = T.rayHit != nullptr || __float_as_uint(L.x) != __float_as_uint(Ls.x) ||
                __float_as_uint(L.y) != __float_as_uint(Ls.y) || __float_as_uint(L.z) != __float_as_uint(Ls.z);
-        // the shadowed value, and in .w the shadow ray's candidate occluder (the last trace's occluder in the
-        // nearest previous direction, -1 for none)
-        int occ = -1;
-        if (cast && T.seedOn) {
-          const size_t pj = (((size_t)rs.layer * g.Z + rs.pz) * g.X + rs.px) * g.N;
-          occ = __ldg(&T.occMemo[pj + __ldg(&T.seedDir[rs.j])]);
-        }
-        hits[id] = make_float4(Ls.x, Ls.y, Ls.z, __int_as_float(occ));
+        // the shadow ray's candidate occluder: the last trace's occluder in the nearest previous direction
+        if (cast && T.seedOn) occ = __ldg(&T.occMemo[pj + __ldg(&T.seedDir[rs.j])]);
         hitCode = __float_as_int(r0.w) * 2;
       }
       // stores (rgen:108-109)
@@ -523,7 +582,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
       if (T.rayHit) T.rayHit[idx] = hitCode;
       if (g.rad16) storeRad16(g, rs, L);
     }
-    // append the shadow rays of this warp's slots with one atomic
+    // append the shadow rays of this warp's rays with one atomic
     const unsigned act = __activemask();
     const unsigned want = __ballot_sync(act, cast);
     if (want) {
@@ -531,24 +590,29 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(&counters[1], (unsigned long long)__popc(want));
       base = __shfl_sync(act, base, leader);
-      if (cast) shadowList[base + __popc(want & below)] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)id));
+      if (cast) {
+        const unsigned long long k = base + __popc(want & below);
+        shadowList[2 * k] = make_float4(so.x, so.y, so.z, __uint_as_float((uint32_t)id));
+        shadowList[2 * k + 1] = make_float4(Ls.x, Ls.y, Ls.z, __int_as_float(occ));
+      }
     }
   }
 }
 
 // Shadow rays (rchit:155-176): any hit in [0.1, 50] toward the sun; a shadowed ray gets the top bit of its
-// shadow record's slot id set, and k_shadow_resolve gives it the shadowed radiance. Keeping the output
-// writes out of this kernel keeps its finishing lanes (a few per warp at a time) to one store.
+// shadow record's ray id set and its occluder in the second record, and k_shadow_resolve gives it the
+// shadowed radiance. Keeping the output writes out of this kernel keeps its finishing lanes (a few per warp at
+// a time) to two stores.
 // kLightSpace: every item's shadow rays run in its light-space BVH along +z (shadowMode 1).
 template <bool kWide, bool kLightSpace, class Src>
 __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlocks : DDGI_TRACE_MIN_BLOCKS)
-    k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList, float4* __restrict__ hits,
+    k_trace_shadow(const __grid_constant__ Src src, float4* __restrict__ shadowList,
                    unsigned long long* __restrict__ counters, int refillLanes, uint32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const long long total = (long long)counters[1];
   long long id = -1;  // shadow record index of this lane's ray
-  uint32_t slot = 0;
+  uint32_t rayId = 0;  // its natural ray id
   bool drained = total == 0;
   BvhRef bvh;
   WRay ray;
@@ -566,15 +630,15 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
       if ((long long)base + need >= total) drained = true;
       const long long k = (long long)base + __popc(idle & below);
       if (id < 0 && k < total) {
-        const float4 rec = shadowList[k];
+        const float4 rec = shadowList[2 * k];
         id = k;
-        slot = __float_as_uint(rec.w);
-        const TraceItem& T = src.at((long long)(slot >> 5));
+        rayId = __float_as_uint(rec.w);
+        const TraceItem& T = src.at((long long)(rayId >> 5));
         bvh = kLightSpace ? T.s.shadow : T.s.bvh;
         ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
         if (!finished) {  // the candidate occluder k_shade parked: if it is hit, the ray is shadowed
-          const int c = __float_as_int(hits[slot].w);
+          const int c = __float_as_int(shadowList[2 * k + 1].w);
           if ((unsigned)c < (unsigned)bvh.numTris) finished = testTri<true>(bvh, ray, c, kTMin, hit);
         }
       }
@@ -582,33 +646,32 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
     if (id >= 0 && !finished) finished = travStep<kWide, true, kLightSpace>(bvh, ray, st, hit, err);
     if (id >= 0 && finished) {
       if (hit.leaf >= 0) {
-        reinterpret_cast<uint32_t*>(shadowList + id)[3] = slot | 0x80000000u;
-        reinterpret_cast<int*>(hits + slot)[3] = hit.leaf;  // the occluder, for the memo
+        reinterpret_cast<uint32_t*>(shadowList + 2 * id)[3] = rayId | 0x80000000u;
+        reinterpret_cast<int*>(shadowList + 2 * id + 1)[3] = hit.leaf;  // the occluder, for the memo
       }
       id = -1;
     }
   }
 }
 
-// Shadowed rays' outputs, one thread per shadow record: the shadowed radiance k_shade parked in the hit
-// record replaces the lit one in the ray image (and the planar 16-bit copy), and the hit code gets its
+// Shadowed rays' outputs, one thread per shadow record pair: the shadowed radiance k_shade parked in the
+// second record replaces the lit one in the ray image (and the planar 16-bit copy), and the hit code gets its
 // shadow bit.
 template <class Src>
 __global__ void __launch_bounds__(256) k_shadow_resolve(const __grid_constant__ Src src,
                                                         const float4* __restrict__ shadowList,
-                                                        const unsigned long long* __restrict__ counters,
-                                                        const float4* __restrict__ hits) {
+                                                        const unsigned long long* __restrict__ counters) {
   const long long total = (long long)counters[1];
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
        k += (long long)gridDim.x * blockDim.x) {
-    const uint32_t u = __float_as_uint(shadowList[k].w);
+    const uint32_t u = __float_as_uint(shadowList[2 * k].w);
     const uint32_t id = u & 0x7fffffffu;
     const long long warp = id >> 5;
     const TraceItem& T = src.at(warp);
     const bool shadowed = (u & 0x80000000u) != 0;
     if (!shadowed && !T.occMemo) continue;
-    const RaySlot rs = raySlot(T.g, T.f, T.order, (uint32_t)(warp - T.warpBegin), (int)(id & 31));
-    const float4 hr = hits[id];
+    const RaySlot rs = naturalRay(T.g, T.f, T.order, (uint32_t)(id - 32 * T.warpBegin)).rs;
+    const float4 hr = shadowList[2 * k + 1];
     if (T.occMemo)  // the occluder of this shadow ray (-1: unshadowed), the next trace's candidate
       T.occMemo[(((size_t)rs.layer * T.g.Z + rs.pz) * T.g.X + rs.px) * T.g.N + rs.j] =
           shadowed ? __float_as_int(hr.w) : -1;
@@ -823,7 +886,7 @@ __global__ void __launch_bounds__(256) k_mirror_shade(SceneGPU s, GridGPU g, Fra
     float4 lit = make_float4(0.f, 0.f, 0.f, 0.f), dark = lit, sp = make_float4(0.f, 0.f, 0.f, 1.f);
     if (p.sky == 0.0f) {
       if (hr.triangle < 0) {
-        const float3 sky = toLinear(f.skyColor * f.skyIntensity);
+        const float3 sky = f.skyLinear;
         lit = dark = make_float4(sky.x, sky.y, sky.z, 1e6f);
       } else {
         const float3 origin = f3(p.position[0], p.position[1], p.position[2]);
@@ -984,8 +1047,8 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
   auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, Src> : k_trace_shadow<true, false, Src>)
                      : (lightSpace ? k_trace_shadow<false, true, Src> : k_trace_shadow<false, false, Src>);
   const int shadowBlocks = lightSpace ? blocks * kShadowLightBlocks / DDGI_TRACE_MIN_BLOCKS : blocks;
-  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dHits, dCounters, refill, err);
-  k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters, dHits);
+  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
+  k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters);
 }
 
 }  // namespace

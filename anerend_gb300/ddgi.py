@@ -367,7 +367,8 @@ class Server:
     batches, up to `in_flight` launches overlapping on the device."""
 
     def __init__(self, ctx: Context, memory_budget: int, max_batch: int = 64, in_flight: int = 2,
-                 conv_mode: int = 0, max_batch_mrays: int = 0):
+                 conv_mode: int = 0, max_batch_mrays: int = 0, policy: int = L.DDGI_SERVE_FIFO,
+                 aging_ms: float = 0.0):
         self.ctx = ctx
         cfg = L.ServerConfig()
         cfg.memoryBudget = int(memory_budget)
@@ -375,6 +376,8 @@ class Server:
         cfg.inFlight = in_flight
         cfg.convMode = conv_mode
         cfg.maxBatchMRays = max_batch_mrays
+        cfg.policy = policy
+        cfg.agingMs = aging_ms
         h = C.c_void_p()
         ctx.check(ctx.lib.ddgi_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h

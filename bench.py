@@ -424,6 +424,8 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
         return {"precision_tc": measure_precision(ctx, stream)}
     if only == "batched":
         return measure_batched(ctx, stream, serving=False)
+    if only == "batched_launches":
+        return batched_launches(ctx, stream)
     rays = w.probes * w.rays
     g = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis)
 
@@ -496,6 +498,37 @@ def measure_mirror(ctx, scene, w, stream):
     return {"points": n, "ms": ms, "reflected_rays_per_s": n / ms * 1e3, "hit_fraction": hit}
 
 
+def batched_launches(ctx, stream, updates=4):
+    """A few eager updates of the 64-grid batched workload (FP16 tensor-core convolution, the autotuned launch
+    shape of its last measurement), for a per-kernel launch list under ncu: the per-phase split of the batched
+    form. Returns the CUDA-event time of the last update."""
+    import torch
+
+    from anerend_gb300 import ddgi, scenes
+
+    bwl = scenes.BATCHED
+    tris, specs = scenes.batch_layout(bwl)
+    scs = [ddgi.Scene(ctx, scenes.build_scene_tris(t, 1000 + i, bwl.box_lo, bwl.box_hi)) for i, t in enumerate(tris)]
+    grids = [ddgi.ProbeGrid(ctx, sp.dims, sp.step, sp.rays, sp.origin_y, sp.hysteresis) for sp in specs]
+    batch = ddgi.Batch(ctx, [(g, scs[sp.scene]) for g, sp in zip(grids, specs)])
+    batch.set_tuning(conv_mode=1, use_graph=0, bvh_width=8, refill_lanes=16, blocks_per_sm=8, warp_probes=4,
+                     ray_order=1, shadow_mode=1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for f in range(updates):
+        frames = [ddgi.FrameParams(camera_pos=sp.camera, rotation=scenes.rotation(i, f)) for i, sp in enumerate(specs)]
+        e0.record()
+        batch.update(frames, stream)
+        e1.record()
+    torch.cuda.synchronize()
+    out = {"batched_launches": {"updates": updates, "last_update_ms": e0.elapsed_time(e1)}}
+    batch.close()
+    for g in grids:
+        g.close()
+    for sc in scs:
+        sc.close()
+    return out
+
+
 def _batched_conv_error(ctx, stream, specs, scs, tuning, conv_mode, picks=8, probes_per_grid=256):
     """Per-texel error of a batched update's convolution against the FP64 oracle: hysteresis-0 copies of a
     seeded subset of the batched grids run two batched updates with `conv_mode`; on up to probes_per_grid
@@ -537,6 +570,7 @@ def measure_batched(ctx, stream, serving=True):
     loop over the same resident scenes."""
     import torch
 
+    from anerend_gb300 import _lib as L
     from anerend_gb300 import ddgi, scenes
 
     out = {}
@@ -617,10 +651,15 @@ def measure_batched(ctx, stream, serving=True):
                    ddgi.FrameParams(camera_pos=(0.0, 0.0, 0.0), rotation=scenes.rotation(0, 0)))
     srv.drain(600.0)
     srv.close()
-    serv = {"scenes": len(scs), "triangles": sum(stris), "triangles_min": min(stris), "triangles_max": max(stris)}
-    for rate, dur in ((2000.0, 1.5), (1000.0, 1.5), (500.0, 2.0), (200.0, 2.0)):
+    serv = {"scenes": len(scs), "triangles": sum(stris), "triangles_min": min(stris), "triangles_max": max(stris),
+            "conv_mode": "FP16 tensor cores", "policy": "shortest rays first, aging 50 ms", "in_flight": 4,
+            "max_batch_mrays": 8}
+    runs = [(2000.0, 1.5, L.DDGI_SERVE_FIFO, 2, "fifo_2000"), (1000.0, 1.5, L.DDGI_SERVE_FIFO, 2, "fifo_1000")]
+    runs += [(r, 1.5, L.DDGI_SERVE_SHORTEST_FIRST, 4, f"rate_{int(r)}") for r in (2000.0, 1500.0, 1000.0, 750.0, 500.0)]
+    for rate, dur, policy, slots, key in runs:
         reqs = scenes.serving_requests(sw, int(rate * dur), rate)
-        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=2, conv_mode=1, max_batch_mrays=8)
+        srv = ddgi.Server(ctx, sw.budget, max_batch=64, in_flight=slots, conv_mode=1, max_batch_mrays=8,
+                          policy=policy, aging_ms=50.0)
         t0 = time.perf_counter()
         for (ta, si, dms, rr, cam, k) in reqs:
             now = time.perf_counter() - t0
@@ -632,11 +671,14 @@ def measure_batched(ctx, stream, serving=True):
         wall = time.perf_counter() - t0
         st = srv.stats
         offered = sum(int(np.prod(dm)) * rr for (_, _, dm, rr, _, _) in reqs)
-        serv[f"rate_{int(rate)}"] = {"requests": len(reqs), "completed": int(st.completed), "batches": int(st.batches),
+        serv[key] = {"requests": len(reqs), "completed": int(st.completed), "batches": int(st.batches),
                                      "offered_rays_per_s": offered / max(reqs[-1][0], 1e-9),
                                      "served_rays_per_s": st.rays / wall, "p50_ms": st.p50LatencyMs,
                                      "p99_ms": st.p99LatencyMs, "peak_gb": st.peakBytes / 2**30}
         srv.close()
+    # the knee: the highest offered rate (of those run, shortest first) whose p99 stays within one 30 Hz period
+    ok = [r for r in (2000, 1500, 1000, 750, 500) if serv[f"rate_{r}"]["p99_ms"] < 33.0]
+    serv["knee_req_per_s"] = max(ok) if ok else None
     out["serving"] = serv
     for sc in scs:
         sc.close()
@@ -823,7 +865,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the other forms (batched, precision, serving)")
-    ap.add_argument("--form", choices=["precision", "batched"], help="run only this form and print its measurements")
+    ap.add_argument("--form", choices=["precision", "batched", "batched_launches"],
+                    help="run only this form and print its measurements (batched_launches: four eager batched updates, "
+                         "for an ncu launch list)")
     ap.add_argument("--bvh-width", type=int, default=8, choices=[2, 8], help="traversal tree (8-wide or binary)")
     ap.add_argument("--refill-lanes", type=int, default=8, help="idle lanes before a traversal warp refills (1..32)")
     ap.add_argument("--warp-probes", type=int, default=2, help="probes per traversal warp (1, 2, 4, ... 32)")

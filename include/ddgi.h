@@ -457,15 +457,22 @@ int  ddgi_batch_update(DdgiBatch* batch, const DdgiFrame* frames, void* stream);
 
 typedef struct DdgiServer DdgiServer;
 
+#define DDGI_SERVE_FIFO           0  /* admit in arrival order */
+#define DDGI_SERVE_SHORTEST_FIRST 1  /* admit the request with the fewest rays first; a request's ray count is
+                                        scaled down as it waits (aging), so large ones are not starved */
+
 typedef struct DdgiServerConfig {
   uint64_t memoryBudget;  /* device bytes of request grids admitted at once (ddgi_grid_footprint less the seeding records) */
   int32_t  maxBatch;      /* requests per launch (1..64) */
-  int32_t  inFlight;      /* launches running at once, each on its own stream (1..4) */
+  int32_t  inFlight;      /* launches running at once, each on its own stream (1..8) */
   int32_t  convMode;      /* DdgiTuning.convMode of the served grids */
   uint32_t maxBatchMRays; /* rays per launch, in millions, admitted at most (a request larger than that runs
                              alone); 0: no limit. Short launches free their slot sooner, so later arrivals
                              wait less behind large ones */
-  int32_t  reserved[4];
+  int32_t  policy;        /* DDGI_SERVE_*; 0 is FIFO */
+  float    agingMs;       /* shortest-first: a request that has waited w ms ranks as rays x max(0, 1 - w / agingMs),
+                             so after agingMs it goes ahead of every younger request (0: 50 ms) */
+  int32_t  reserved[2];
 } DdgiServerConfig;
 
 /* One probe update of a grid of its own over a resident scene. The grid starts cleared, is translated,

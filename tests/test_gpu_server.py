@@ -20,8 +20,9 @@ def _scenes(ctx):
     return [ddgi.Scene(ctx, a) for a in arrays]
 
 
-def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30):
-    srv = ddgi.Server(ctx, budget, max_batch=max_batch, in_flight=in_flight, conv_mode=conv_mode)
+def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30, policy=L.DDGI_SERVE_FIFO):
+    srv = ddgi.Server(ctx, budget, max_batch=max_batch, in_flight=in_flight, conv_mode=conv_mode, policy=policy,
+                      aging_ms=50.0)
     # outputs and descriptions first, so the requests arrive back to back (a pinned allocation between two
     # submissions would let each request finish before the next one arrives)
     outs = [torch.empty(10 * dims[0] * 10 * dims[2] * dims[1] * 4, dtype=torch.float32).pin_memory()
@@ -45,13 +46,14 @@ def _serve(ctx, scs, max_batch, in_flight, conv_mode, budget=8 << 30):
         srv.close()
 
 
-# 1 (FP16 tensor cores) is the mode the serving bench runs
-@pytest.mark.parametrize("conv_mode", [0, 1, 2])
-def test_request_alone_equals_in_the_mix(ctx, conv_mode):
+# 1 (FP16 tensor cores) with shortest-first admission over four slots is what the serving bench runs
+@pytest.mark.parametrize("conv_mode,policy,slots", [(0, L.DDGI_SERVE_FIFO, 2), (1, L.DDGI_SERVE_FIFO, 2),
+                                                    (2, L.DDGI_SERVE_FIFO, 2), (1, L.DDGI_SERVE_SHORTEST_FIRST, 4)])
+def test_request_alone_equals_in_the_mix(ctx, conv_mode, policy, slots):
     scs = _scenes(ctx)
     try:
         alone, st1 = _serve(ctx, scs, max_batch=1, in_flight=1, conv_mode=conv_mode)
-        mixed, st2 = _serve(ctx, scs, max_batch=64, in_flight=2, conv_mode=conv_mode)
+        mixed, st2 = _serve(ctx, scs, max_batch=64, in_flight=slots, conv_mode=conv_mode, policy=policy)
         assert st1.batches == len(REQS)
         assert st2.batches < len(REQS)  # requests shared launches
         for i, (a, b) in enumerate(zip(alone, mixed)):
@@ -123,3 +125,35 @@ def test_ray_cap_splits_launches(ctx):
     finally:
         for s in scs:
             s.close()
+
+
+@pytest.mark.parametrize("aging_ms,order", [(1e6, ["small", "medium", "large"]), (1e-3, ["large", "small", "medium"])])
+def test_shortest_first_admission_and_aging(ctx, aging_ms, order):
+    """With one slot and one request per launch, requests queued behind a running one are admitted shortest
+    first; with an aging time far below the queueing time every request has aged fully and they go in
+    arrival order."""
+    scs = _scenes(ctx)
+    blocker = ddgi.grid_desc((32, 8, 32), rays_per_probe=512)  # 4.2 M rays: the others queue behind it
+    sizes = {"large": ((16, 4, 16), 256), "small": ((4, 2, 4), 64), "medium": ((8, 4, 8), 128)}
+    descs = {k: ddgi.grid_desc(dims, rays_per_probe=n) for k, (dims, n) in sizes.items()}
+    srv = ddgi.Server(ctx, 8 << 30, max_batch=1, in_flight=1, policy=L.DDGI_SERVE_SHORTEST_FIRST, aging_ms=aging_ms)
+    try:
+        fp = ddgi.FrameParams(rotation=scenes.rotation(1, 1))
+        srv.submit(scs[0], blocker, fp)
+        ids = {k: srv.submit(scs[0], descs[k], fp) for k in ("large", "small", "medium")}  # arrival order
+        srv.drain(120.0)
+        admitted = sorted(ids, key=lambda k: srv.status(ids[k]).admitSeconds)
+        assert admitted == order, [(k, srv.status(ids[k]).admitSeconds) for k in ids]
+        assert srv.stats.completed == 4
+    finally:
+        srv.close()
+        for s in scs:
+            s.close()
+
+
+def test_server_config_is_validated(ctx):
+    for kw in (dict(policy=7), dict(in_flight=9), dict(aging_ms=-1.0)):
+        with pytest.raises(L.DdgiError) as e:
+            ddgi.Server(ctx, 1 << 30, **kw)
+        assert e.value.code == L.DDGI_EINVAL
+    ddgi.Server(ctx, 1 << 30, in_flight=8, policy=L.DDGI_SERVE_SHORTEST_FIRST).close()
