@@ -31,6 +31,7 @@ struct LaunchState {
   long long rayCap = 0;
   StagingRing ring;  // pinned host images of the record block
   std::vector<TcItemHost> tcHost;
+  std::vector<long long> begins;  // the records' first warps, in launch order
   cudaStream_t captureStream = nullptr;  // the caller's stream may be the uncapturable legacy stream
   cudaGraphExec_t exec = nullptr;
   std::vector<long long> shape, lastShape;
@@ -119,7 +120,8 @@ int issue(LaunchState* S, const DdgiBatchTuning& t, int n, int maxN, long long t
   DdgiContext* ctx = S->ctx;
   int blocks = ctx->numSms * t.blocksPerSm;
   CK(launchTraceBatch(S->dTrace(), S->dRots(), n, maxN, totalWarps, S->dQueue, S->dHits, S->dShadow, blocks,
-                      t.refillLanes, t.bvhWidth != 2, t.shadowMode == 1, ctx->dErr, st),
+                      t.refillLanes, t.bvhWidth != 2, t.shadowMode == 1, ctx->dErr, st, nullptr, nullptr,
+                      S->begins.data()),
      "batched trace");
   if (t.convMode != 0) {
     int fmt = t.convMode == 1 ? DDGI_ELEM_F16 : DDGI_ELEM_BF16;
@@ -145,13 +147,20 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
   if (tc && (int)S->tcHost.size() < n) S->tcHost.resize(n);
   long long warps = 0, groups = 0, rays = 0;
   int units = 0, maxN = 0, moved = 0;
+  S->begins.assign(n, 0);
   int slot = 0;
   unsigned char* rec = S->ring.acquire(&slot);
   TraceItem* hTrace = reinterpret_cast<TraceItem*>(rec);
   Mat3* hRots = reinterpret_cast<Mat3*>(rec + S->offRots);
   ConvItem* hConv = reinterpret_cast<ConvItem*>(rec + S->offConv);
   unsigned char* hTc = rec + S->offTc;
-  for (int i = 0; i < n; ++i) {
+  // launch order: the items grouped by scene (stable), so the rays in flight at any time, and the hits being
+  // shaded, share one scene's BVH and records in L2; each item's results do not depend on the order
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return scenes[a] < scenes[b]; });
+  for (int k = 0; k < n; ++k) {
+    const int i = perm[k];
     DdgiGrid* g = grids[i];
     DdgiScene* sc = scenes[i];
     const DdgiFrame& fr = frames[i];
@@ -183,7 +192,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
       gg.rad16Fmt = fmt;
       gg.pTotal = g->g.X * g->g.Y * g->g.Z;
     }
-    TraceItem& ti = hTrace[i];
+    TraceItem& ti = hTrace[k];
     ti.s = view;
     ti.g = gg;
     ti.f = f;
@@ -194,6 +203,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.rayDir = g->rayDir;
     ti.rayHit = g->rayHit;
     ti.warpBegin = warps;
+    S->begins[k] = warps;
     ti.latticePrev = g->latticePrev;
     ti.seedDir = g->seedDir;
     ti.hitMemo = g->hitMemo;
@@ -201,17 +211,17 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.seedOn = g->memoValid ? 1 : 0;
     warps += traceWarps(gg, f);
     rays += (long long)(le - lb) * g->g.X * g->g.Z * g->g.N;
-    memcpy(hRots[i].m, fr.rotation, sizeof(float) * 9);
+    memcpy(hRots[k].m, fr.rotation, sizeof(float) * 9);
     maxN = std::max(maxN, g->g.N);
     if (tc) {
-      TcItemHost& h = S->tcHost[i];
+      TcItemHost& h = S->tcHost[k];
       if (!tcPrepareItem(g->g, fmt, g->rad16, gg.pTotal, g->lattice, g->tcScratch, g->atlas[g->cur], lb, le,
                          g->desc.hysteresis, fr.flags, units, &h))
         return fail(ctx, DDGI_EINVAL, "tensor-core item %d could not be prepared", i);
-      memcpy(hTc + 128 * (size_t)i, h.item, 128);
+      memcpy(hTc + 128 * (size_t)k, h.item, 128);
       units += h.units;
     } else {
-      ConvItem& ci = hConv[i];
+      ConvItem& ci = hConv[k];
       ci.g = g->g;
       ci.rayRad = g->rayRad;
       ci.dirs = g->lattice;
@@ -240,6 +250,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
   }
   // the captured sequence depends only on these (per-item values live in the device records)
   S->shape = {n, maxN, warps, groups, units, t.convMode, t.blocksPerSm, t.refillLanes, t.bvhWidth};
+  S->shape.insert(S->shape.end(), S->begins.begin(), S->begins.end());  // captured in the trace's parameters
   const bool stable = allowGraph && t.useGraph && S->shape == S->lastShape;
   if (stable && !S->exec) {
     cudaGraph_t graph = nullptr;

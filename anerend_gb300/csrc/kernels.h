@@ -48,15 +48,20 @@ constexpr int kTraceCounters = 4;
 // Scratch of one trace launch per ray slot: the hit record (16 B) and the shadow-list entry (32 B: the shadow
 // ray's origin and ray id, then the shadowed radiance and the candidate / found occluder).
 constexpr size_t kTraceScratchPerRay = 48;
+// Records of a batched trace whose first warps travel in the kernel parameters (ItemsGlobal, trace.cu).
+constexpr int kParamItems = 64;
 // Lattices of every item (rotation per item), then the wavefront trace of all items' ray slots:
 // closest-hit traversal, shading, shadow traversal, shadowed-ray resolve. dHits holds 32 * totalWarps float4,
 // dShadow twice that. hItems / hRot: a single record and its rotation on the host, passed to every
 // kernel by value (constant-bank reads; dItems and dRots are not read), otherwise the kernels read dItems and
-// dRots. The lattice kernel zeroes dCounters, so no copy or memset runs ahead of the launches.
+// dRots. The lattice kernel zeroes dCounters, so no copy or memset runs ahead of the launches. hBegins: the
+// records' first warps on the host (at most kParamItems of them are passed in the parameters; a captured
+// launch must be re-captured when they change).
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
-                             const TraceItem* hItems = nullptr, const Mat3* hRot = nullptr);
+                             const TraceItem* hItems = nullptr, const Mat3* hRot = nullptr,
+                             const long long* hBegins = nullptr);
 
 
 // Ray queries on one BVH: DdgiRay -> DdgiHit (closest or any hit), or, with `points`, the RT shadow pass's

@@ -265,10 +265,23 @@ DDGI_D int findItem(const TraceItem* __restrict__ items, int numItems, long long
 // reads become constant-bank reads at fixed offsets; ItemsGlobal points at the table in global memory (a
 // by-value table of many records, indexed at run time, measured no faster than the L1-resident table).
 // at(warp) is the record that owns ray-slot warp `warp`.
+// For a launch of at most kParamItems records the first warps of the records also travel in the parameters, so
+// the per-ray search for a ray's record reads the constant bank (uniform over a warp) instead of the records'
+// scattered warpBegin fields.
 struct ItemsGlobal {
   const TraceItem* items;
   int n;
-  DDGI_D const TraceItem& at(long long warp) const { return items[findItem(items, n, warp)]; }
+  int inParams;  // begins[] holds the n records' first warps
+  long long begins[kParamItems];
+  DDGI_D const TraceItem& at(long long warp) const {
+    if (!inParams) return items[findItem(items, n, warp)];
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (begins[mid] <= warp) lo = mid; else hi = mid - 1;
+    }
+    return items[lo];
+  }
 };
 struct ItemsOne {
   TraceItem it;
@@ -1056,7 +1069,7 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
 cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int numItems, int maxN, long long totalWarps,
                              unsigned long long* dCounters, float4* dHits, float4* dShadow, int blocks,
                              int refillLanes, bool wide, bool lightSpace, uint32_t* err, cudaStream_t stream,
-                             const TraceItem* hItems, const Mat3* hRot) {
+                             const TraceItem* hItems, const Mat3* hRot, const long long* hBegins) {
   // one item given on the host with its rotation: every kernel takes it in its parameters, and dItems /
   // dRots are not read
   const bool byValue = hItems && hRot && numItems == 1;
@@ -1078,7 +1091,13 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
     launchWavefront(ItemsOne{hItems[0]}, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide, lightSpace,
                     err, stream);
   } else {
-    launchWavefront(ItemsGlobal{dItems, numItems}, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide,
+    ItemsGlobal src{};
+    src.items = dItems;
+    src.n = numItems;
+    src.inParams = hBegins && numItems <= kParamItems ? 1 : 0;
+    if (src.inParams)
+      for (int i = 0; i < numItems; ++i) src.begins[i] = hBegins[i];
+    launchWavefront(src, rays, dCounters, dHits, dShadow, blocks, refill, shadeBlocks, wide,
                     lightSpace, err, stream);
   }
   return cudaGetLastError();

@@ -326,12 +326,16 @@ DDGI_HD uint32_t slotsToKeys(uint32_t x, uint32_t oct) {
 
 // node: the next wide node to test, -1 when the stack is exhausted. tMask: the last tested node's hit leaf
 // slots still to test (bits 0-7) and that node's leaf-slot mask (bits 8-15), or 0 when none is left; the
-// record of leaf slot k is tBase + (leaf slots below k). A step tests one of them.
+// record of leaf slot k is tBase + (leaf slots below k). A step tests one of them. Stack entries are
+// {childBase, (internal-slot mask << 8) | remaining keys}; the top entry is held in registers (`top`, {0, 0}
+// when the stack is empty) and the ones below it in `stack` (sp of them), so a pop reads and updates
+// registers, and the entry below is loaded when the top runs out, a step before it is needed.
 struct WideTrav {
   int node, sp;
   uint32_t oct;
   uint32_t tBase, tMask;
-  uint2 stack[kWideStack];  // {childBase, (internal-slot mask << 8) | remaining keys}
+  uint2 top;
+  uint2 stack[kWideStack];
 };
 
 template <bool kAnyHit>
@@ -343,25 +347,27 @@ DDGI_HD bool wideInit(const BvhRef& b, const WRay& r, float tmax, WideTrav& s, H
   s.sp = 0;
   s.tBase = 0;
   s.tMask = 0;
+  s.top = make_uint2(0u, 0u);
   s.oct = (r.invd.x < 0.f ? 1u : 0u) | (r.invd.y < 0.f ? 2u : 0u) | (r.invd.z < 0.f ? 4u : 0u);
   return b.numTris <= 0;
 }
 
-// The next node from the stack into s.node (-1 when it is empty).
+// The next node from the stack into s.node (-1 when it is empty). The top entry is empty only when the whole
+// stack is: an exhausted top is replaced at once by the entry below it.
 DDGI_HD void widePop(WideTrav& s) {
-  if (s.sp == 0) {
+  uint32_t keys = s.top.y & 0xffu;
+  if (keys == 0u) {
     s.node = -1;
     return;
   }
-  uint2& top = s.stack[s.sp - 1];
-  uint32_t keys = top.y & 0xffu;
-  const uint32_t tim = top.y >> 8;
+  const uint32_t tim = s.top.y >> 8;
   const int key = lowestBit(keys);
   keys &= keys - 1u;
   const uint32_t slot = (uint32_t)key ^ s.oct;
-  s.node = (int)(top.x + (uint32_t)popc(tim & ((1u << slot) - 1u)));
-  if (keys) top.y = (tim << 8) | keys;
-  else --s.sp;
+  s.node = (int)(s.top.x + (uint32_t)popc(tim & ((1u << slot) - 1u)));
+  if (keys) s.top.y = (tim << 8) | keys;
+  else if (s.sp > 0) s.top = s.stack[--s.sp];
+  else s.top = make_uint2(0u, 0u);
 }
 
 // One step: a lane with pending triangles tests one of them; otherwise it tests the 8 child boxes of its
@@ -397,6 +403,7 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
     flagError(err, DDGI_DEVERR_BOUNDS);
     s.node = -1;
     s.sp = 0;
+    s.top = make_uint2(0u, 0u);
     return;
   }
   const uint32_t oct = s.oct;
@@ -511,6 +518,7 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
       flagError(err, DDGI_DEVERR_BOUNDS);
       s.node = -1;
       s.sp = 0;
+      s.top = make_uint2(0u, 0u);
       return;
     }
     s.tBase = hd.y;
@@ -523,14 +531,18 @@ DDGI_HD void wideNodeTest(const BvhRef& b, const WRay& r, float tmin, WideTrav& 
     const uint32_t slot = (uint32_t)key ^ oct;
     const int next = (int)(hd.x + (uint32_t)popc(imask & ((1u << slot) - 1u)));
     if (ihits) {
-      if (s.sp >= kWideStack) {
-        flagError(err, DDGI_DEVERR_STACK_OVERFLOW);
-        s.node = -1;
-        s.sp = 0;
-        s.tMask = 0;
-        return;
+      if (s.top.y & 0xffu) {  // the current top goes below the new one
+        if (s.sp >= kWideStack) {
+          flagError(err, DDGI_DEVERR_STACK_OVERFLOW);
+          s.node = -1;
+          s.sp = 0;
+          s.top = make_uint2(0u, 0u);
+          s.tMask = 0;
+          return;
+        }
+        s.stack[s.sp++] = s.top;
       }
-      s.stack[s.sp++] = make_uint2(hd.x, (imask << 8) | ihits);
+      s.top = make_uint2(hd.x, (imask << 8) | ihits);
     }
     s.node = next;
     return;
