@@ -173,6 +173,39 @@ def test_cpu_reference_workload_8_frames(ctx, tuning):
     assert np.percentile(err, 99.9) <= 1e-3, np.percentile(err, [50, 99, 99.9, 100])
 
 
+def test_cpu_reference_workload_lockstep_clean_texels(ctx):
+    """The 8x4x8 / 64-ray workload with the oracle started every frame from the device's atlas: every texel of a
+    probe whose 64 rays the oracle marks certain within 1e-4 (floor 1e-3), frame after frame, beside the 99.9th
+    percentile over all texels (1e-3). The free-running comparison above excuses 0.1 % of texels; this one
+    bounds the maximum wherever no uncertain ray reached."""
+    w = scenes.CPU_REFERENCE
+    arrays = scenes.build_scene(w)
+    scene = ddgi.Scene(ctx, arrays)
+    grid = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, options=L.DDGI_GRID_RECORD_HITS)
+    osc = oracle.OracleScene(arrays, L.SceneDesc)
+    og = oracle.OracleGrid(grid.desc)
+    X, Y, Z = w.dims
+    bw, bh = og.geom.block
+    try:
+        for f in range(w.frames):
+            fp = ddgi.FrameParams(camera_pos=scenes.camera(w, f), rotation=scenes.rotation(w.seed, f))
+            og.atlas = grid.download_atlas().astype(np.float64)
+            grid.update(scene, fp)
+            og.update(osc, fp.to_c())
+            ctx.sync()
+            atlas = grid.download_atlas().astype(np.float64)
+            err = rel_err(atlas, og.atlas, 1e-3)
+            tainted = (og.uncertain != 0).reshape(Y, Z, bh, X, bw).any(axis=(2, 4)).reshape(Y * Z, X)
+            clean = ~np.repeat(np.repeat(tainted, 10, axis=0), 10, axis=1)
+            assert clean.mean() > 0.5, f
+            assert err[clean].max() <= 1e-4, (f, float(err[clean].max()))
+            assert np.percentile(err, 99.9) <= 1e-3, (f, float(np.percentile(err, 99.9)))
+    finally:
+        osc.close()
+        grid.close()
+        scene.close()
+
+
 def test_round_robin_layers_and_edge_clamp(ctx):
     w = scenes.Workload("rr_6x3x5_n128", (6, 3, 5), (1.0, 1.5, 1.0), -1.0, 128, 2000, (-6, -4, -6), (6, 4, 6),
                         4, 0, -3.0, 8.0, 6, 0.96)
