@@ -83,7 +83,8 @@ GridGPU makeGridGPU(const DdgiGridDesc& d) {
   g.rayW = g.bw * g.X;
   g.rayFmt = (d.options & DDGI_GRID_RAYS_RGBA16F) ? DDGI_FORMAT_RGBA16F : DDGI_FORMAT_RGBA32F;
   g.options = d.options;
-  g.warpProbes = 1;
+  g.magicX = divMagic((uint32_t)g.X);
+  setGridWarpProbes(g, 1);
   return g;
 }
 
@@ -147,7 +148,7 @@ int applyTuning(DdgiGrid* g, const DdgiTuning& t) {
   g->tuning = t;
   if (g->tuning.bvhWidth == 0) g->tuning.bvhWidth = 8;
   if (g->tuning.refillLanes == 0) g->tuning.refillLanes = 8;
-  g->g.warpProbes = t.warpProbes;
+  setGridWarpProbes(g->g, t.warpProbes);
   g->g.bvhWide = g->tuning.bvhWidth == 8 ? 1 : 0;
   return DDGI_OK;
 }

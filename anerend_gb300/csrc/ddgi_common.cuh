@@ -252,11 +252,34 @@ struct GridGPU {
   uint32_t options;
   int bvhWide;     // 1: traverse the 8-wide BVH, 0: the binary one
   int warpProbes;  // probes per warp (power of two, 32 / warpProbes <= N)
+  int probeGroups;   // ceil(X Z / warpProbes): probe groups (of warpProbes probes) per layer
+  uint32_t magicX, magicPG;  // divMagic(X), divMagic(probeGroups): divisions of the ray-slot mapping
   void* rad16;     // when set, the trace also writes planar 16-bit radiance (row c * pTotal + p, N per row)
   int rad16Fmt;    // 0 FP16, 1 BF16
   int pTotal;      // probes of the grid (rows per channel of rad16)
   int samplerClamp;  // atlas sampler addressing: 0 REPEAT (the trace pass), 1 CLAMP_TO_EDGE (the deferred pass)
 };
+
+// Division by an invariant d >= 1 for dividends below 2^31: with m = divMagic(d) = floor((2^32 - 1) / d),
+// q = the high word of a m is floor(a / d) or one less (a m / 2^32 > a / d - a / (d 2^32) - a / 2^32 >
+// a / d - 1), so one correction gives the exact quotient. Replaces the integer division of the per-ray
+// slot mapping (about twenty instructions each) by four.
+DDGI_HD uint32_t divMagic(uint32_t d) { return 0xFFFFFFFFu / d; }
+DDGI_HD uint32_t divFast(uint32_t a, uint32_t d, uint32_t m) {
+#ifdef __CUDA_ARCH__
+  uint32_t q = __umulhi(a, m);
+#else
+  uint32_t q = (uint32_t)(((uint64_t)a * m) >> 32);
+#endif
+  if (a - q * d >= d) ++q;
+  return q;
+}
+
+inline void setGridWarpProbes(GridGPU& g, int warpProbes) {
+  g.warpProbes = warpProbes;
+  g.probeGroups = (g.X * g.Z + warpProbes - 1) / warpProbes;
+  g.magicPG = divMagic((uint32_t)g.probeGroups);
+}
 
 struct FrameGPU {
   float3 camPos, lightDir, skyColor;

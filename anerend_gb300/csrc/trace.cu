@@ -197,20 +197,20 @@ DDGI_D RaySlot raySlot(const GridGPU& g, const FrameGPU& f, const int* __restric
                        int lane) {
   RaySlot r;
   r.valid = false;
-  const int D = 32 / g.warpProbes;
-  const uint32_t dirChunks = (uint32_t)(g.N / D);
-  const uint32_t probeGroups = (uint32_t)((g.X * g.Z + g.warpProbes - 1) / g.warpProbes);
-  const uint32_t rest = warp / dirChunks;
-  const int dc = (int)(warp - rest * dirChunks);
-  const uint32_t lq = rest / probeGroups;
-  const int pg = (int)(rest - lq * probeGroups);
+  const uint32_t lgN = (uint32_t)(__ffs(g.N) - 1), lgWP = (uint32_t)(__ffs(g.warpProbes) - 1), lgD = 5u - lgWP;
+  const uint32_t lgChunks = lgN - lgD;  // N / D direction chunks per probe group
+  const uint32_t rest = warp >> lgChunks;
+  const int dc = (int)(warp & ((1u << lgChunks) - 1u));
+  const uint32_t lq = divFast(rest, (uint32_t)g.probeGroups, g.magicPG);
+  const int pg = (int)(rest - lq * (uint32_t)g.probeGroups);
   r.layer = f.layerBegin + (int)lq;
   if (r.layer >= f.layerEnd) return r;
-  const int p = pg * g.warpProbes + lane / D;
+  const int p = (pg << lgWP) + (lane >> lgD);
   if (p >= g.X * g.Z) return r;
-  r.j = __ldg(&order[dc * D + lane % D]);
-  r.px = p % g.X;
-  r.pz = p / g.X;
+  r.j = __ldg(&order[(dc << lgD) + (lane & ((1 << lgD) - 1))]);
+  const uint32_t pz = divFast((uint32_t)p, (uint32_t)g.X, g.magicX);
+  r.px = p - (int)pz * g.X;
+  r.pz = (int)pz;
   r.valid = true;
   return r;
 }
@@ -232,9 +232,9 @@ DDGI_D NaturalRay naturalRay(const GridGPU& g, const FrameGPU& f, const int* __r
   r.slot = 0;
   const uint32_t lgN = (uint32_t)(__ffs(g.N) - 1), lgWP = (uint32_t)(__ffs(g.warpProbes) - 1), lgD = 5u - lgWP;
   const uint32_t XZ = (uint32_t)(g.X * g.Z);
-  const uint32_t PG = (XZ + (uint32_t)g.warpProbes - 1u) >> lgWP;
+  const uint32_t PG = (uint32_t)g.probeGroups;
   const uint32_t perLayer = PG << (lgWP + lgN);
-  const uint32_t lq = local / perLayer;
+  const uint32_t lq = divFast(local >> (lgWP + lgN), PG, g.magicPG);
   const uint32_t rem = local - lq * perLayer;
   const uint32_t q = rem >> lgN, j = rem & ((uint32_t)g.N - 1u);
   const int layer = f.layerBegin + (int)lq;
@@ -244,8 +244,9 @@ DDGI_D NaturalRay naturalRay(const GridGPU& g, const FrameGPU& f, const int* __r
   r.slot = (((lq * PG + pg) << (lgN - lgD)) + (pos >> lgD)) * 32u + (qq << lgD) + (pos & ((1u << lgD) - 1u));
   r.rs.layer = layer;
   r.rs.j = (int)j;
-  r.rs.px = (int)(q % (uint32_t)g.X);
-  r.rs.pz = (int)(q / (uint32_t)g.X);
+  const uint32_t pz = divFast(q, (uint32_t)g.X, g.magicX);
+  r.rs.px = (int)(q - pz * (uint32_t)g.X);
+  r.rs.pz = (int)pz;
   r.rs.valid = true;
   return r;
 }

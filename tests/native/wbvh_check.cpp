@@ -255,3 +255,22 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
   stats[7] = err;
   return (int)(stats[2] + stats[3] + stats[4] + stats[5] + (err ? 1 : 0));
 }
+
+// divFast (the ray-slot mapping's division by an invariant divisor) against integer division: random
+// dividends below 2^31 and divisors up to 2^24, and dividends at the multiples of the divisor and one below.
+extern "C" long long divfast_check(int numCases, uint64_t seed) {
+  Rng rng{seed};
+  long long bad = 0;
+  for (int c = 0; c < numCases; ++c) {
+    const uint32_t d = (c % 3 == 0) ? 1u + (uint32_t)(rng.next() % 64) : 1u + (uint32_t)(rng.next() % (1u << 24));
+    const uint32_t m = divMagic(d);
+    uint32_t as[4];
+    as[0] = (uint32_t)(rng.next() % (1ull << 31));
+    const uint32_t k = (uint32_t)(rng.next() % ((1ull << 31) / d));
+    as[1] = k * d;
+    as[2] = k * d ? k * d - 1 : 0;
+    as[3] = 0x7fffffffu;
+    for (uint32_t a : as) bad += divFast(a, d, m) != a / d;
+  }
+  return bad;
+}

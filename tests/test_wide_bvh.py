@@ -40,6 +40,8 @@ def lib(request, tmp_path_factory):
     lib.wbvh_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                ctypes.POINTER(ctypes.c_longlong)]
     lib.wbvh_check.restype = ctypes.c_int
+    lib.divfast_check.argtypes = [ctypes.c_int, ctypes.c_uint64]
+    lib.divfast_check.restype = ctypes.c_longlong
     return lib
 
 
@@ -62,3 +64,9 @@ def test_larger_trees(lib, n, dup):
     assert st[6] > 1000  # enough rays hit something for the comparison to mean something
     # an 8-wide tree has far fewer nodes than the binary tree (n - 1)
     assert st[0] < n // 3
+
+
+def test_invariant_divisor_division_is_exact(lib):
+    """divFast, the ray-slot mapping's division by a per-grid reciprocal, equals integer division for every
+    dividend below 2^31 tried, including the divisor's multiples and the values one below them."""
+    assert lib.divfast_check(300000, 99) == 0
