@@ -199,6 +199,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.lattice = g->lattice;
     ti.order = g->order;
     ti.atlasPrev = g->atlas[g->cur];
+    ti.atlasPairs = g->g.atlasFmt == DDGI_FORMAT_RGBA32F && ((uintptr_t)ti.atlasPrev & 31) == 0;
     ti.rayRad = g->rayRad;
     ti.rayDir = g->rayDir;
     ti.rayHit = g->rayHit;

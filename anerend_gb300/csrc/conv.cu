@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kTileThreads, 4) k_conv_fp32_batch(const ConvI
     float4 rn[kRLoads], wn[kWLoads];
     auto fetch = [&](int j0) {
       const int j = j0 + tg;
-      const long long off = (long long)(j / g.bw) * g.rayW + (j % g.bw);
+      const long long off = (long long)(j >> (__ffs(g.bw) - 1)) * g.rayW + (j & (g.bw - 1));  // bw: a power of two
 #pragma unroll
       for (int k = 0; k < kRLoads; ++k) {
         if (rsrc[k] < 0) {

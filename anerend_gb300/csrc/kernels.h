@@ -19,6 +19,7 @@ struct TraceItem {
   const float4* lattice;  // written by the batched lattice kernel
   const int* order;       // 2N ints: the trace's direction order, then its inverse (the position of each direction)
   const void* atlasPrev;
+  int atlasPairs;         // atlasPrev is RGBA32F and 32-byte aligned: the lookups load texel pairs
   void* rayRad;  // ray images in g.rayFmt texels
   void* rayDir;
   int* rayHit;

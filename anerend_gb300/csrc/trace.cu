@@ -68,6 +68,24 @@ DDGI_D float sqrtBlend(float x) {
   return r;
 }
 
+// The texels x0 and x1 of an RGBA32F atlas row (x1 = x0 + 1, or its REPEAT / CLAMP_TO_EDGE replacement). For an
+// even x0 both lie in the aligned 32-byte pair at x0 (the row length is even, so x1 = x0 + 1 there): one 32-byte
+// load. An odd x0 is the second texel of its pair, and x1 comes from a second load made only by such lanes.
+// Half the lanes thus issue one load per row instead of two. row: the row's first texel; the atlas base is
+// 32-byte aligned.
+DDGI_D void loadRowPair(const float4* row, int x0, int x1, float4& t0, float4& t1) {
+  float4 p0, p1;
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(p0.x), "=f"(p0.y), "=f"(p0.z), "=f"(p0.w), "=f"(p1.x), "=f"(p1.y), "=f"(p1.z), "=f"(p1.w)
+      : "l"(row + (x0 & ~1)));
+  const bool odd = (x0 & 1) != 0;
+  float4 q = p1;
+  if (odd) q = __ldg(row + x1);
+  t0 = odd ? p1 : p0;
+  t1 = q;
+}
+
+template <bool kPairs = false>
 DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int iy, int iz, const OctTap& tap) {
   if (g.options & DDGI_GRID_EDGE_CLAMP) {
     ix = min(max(ix, 0), g.X - 1);
@@ -93,10 +111,17 @@ DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int
     if (y1 >= g.atlasH) y1 -= g.atlasH;
     if (y1 >= g.atlasH) y1 -= g.atlasH;
   }
-  float4 t00 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x0);
-  float4 t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
-  float4 t01 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x0);
-  float4 t11 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x1);
+  float4 t00, t10, t01, t11;
+  if (kPairs && g.atlasFmt == DDGI_FORMAT_RGBA32F) {
+    const float4* a = reinterpret_cast<const float4*>(atlas);
+    loadRowPair(a + (size_t)y0 * g.atlasW, x0, x1, t00, t10);
+    loadRowPair(a + (size_t)y1 * g.atlasW, x0, x1, t01, t11);
+  } else {
+    t00 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x0);
+    t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
+    t01 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x0);
+    t11 = loadTexel(atlas, g.atlasFmt, (size_t)y1 * g.atlasW + x1);
+  }
   return xyz(t00) * tap.w00 + xyz(t10) * tap.w10 + xyz(t01) * tap.w01 + xyz(t11) * tap.w11;
 }
 
@@ -116,6 +141,7 @@ DDGI_D void probeFrame(const GridGPU& g, const FrameGPU& f, float3& stepv, float
   }
 }
 
+template <bool kPairs = false>
 DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas, float3 wp, float3 n) {
   float3 stepv, offv;
   probeFrame(g, f, stepv, offv);
@@ -140,7 +166,7 @@ DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas
     w = fmaxf(0.000001f, w);
     if (w < 0.2f) w *= w * w * (1.0f / (0.2f * 0.2f));
     w *= tri.x * tri.y * tri.z;
-    float3 irr = sampleSingleProbe(g, atlas, px + ox, py + oy, pz + oz, tap);
+    float3 irr = sampleSingleProbe<kPairs>(g, atlas, px + ox, py + oy, pz + oz, tap);
     irr = f3(sqrtBlend(irr.x), sqrtBlend(irr.y), sqrtBlend(irr.z));
     sumI += irr * w;
     sumW += w;
@@ -151,13 +177,14 @@ DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas
 }
 
 // calcIndirectDiffuseLight (pbr_light.glsl:365-388)
+template <bool kPairs = false>
 DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const void* atlas, float3 n,
                                   float3 albedo, float metallic, float roughness, float3 wp, float3 viewPos) {
   float3 V = normalize3(viewPos - wp);
   float3 F0 = mixF0(albedo, metallic);
   float3 kS = fresnelSchlickRoughness(fmaxf(dot3(n, V), 0.0f), F0, roughness * roughness);
   float3 kD = (f3(1.f, 1.f, 1.f) - kS) * (1.0f - metallic);
-  float3 irr = sampleProbe(g, f, atlas, wp, n);
+  float3 irr = sampleProbe<kPairs>(g, f, atlas, wp, n);
   return kD * (irr * albedo);
 }
 
@@ -297,8 +324,9 @@ DDGI_D float3 probeOrigin(const GridGPU& g, const FrameGPU& f, const RaySlot& rs
 }
 
 DDGI_D size_t rayIndex(const GridGPU& g, const RaySlot& rs) {
-  const int rx = rs.px * g.bw + (rs.j % g.bw);
-  const int ry = (rs.layer * g.Z + rs.pz) * g.bh + (rs.j / g.bw);
+  const int lgBw = __ffs(g.bw) - 1;  // bw is a power of two
+  const int rx = rs.px * g.bw + (rs.j & (g.bw - 1));
+  const int ry = (rs.layer * g.Z + rs.pz) * g.bh + (rs.j >> lgBw);
   return (size_t)ry * g.rayW + rx;
 }
 
@@ -574,7 +602,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(const __grid_constant__ Src sr
         // lit: L = calcLight; shadowed: L = 0; then += indirect, += emissive (rchit:195-214)
         L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, pos, origin, f.lightDir, f.sunIntensity);
         if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG) {
-          const float3 ind = calcIndirectDiffuse(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
+          const float3 ind =
+              T.atlasPairs ? calcIndirectDiffuse<true>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin)
+                           : calcIndirectDiffuse<false>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
           L += ind;
           Ls += ind;
         }
