@@ -1031,9 +1031,14 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
 
 // Seed map of the items that seed their closest hits: for each direction of the new lattice the nearest
 // direction of the last traced one (largest dot product, the lowest index on ties). Any choice is exact; a
-// near direction makes the candidate likely to be hit.
+// near direction makes the candidate likely to be hit. kSeedLanes lanes share a direction: lane l scans the
+// previous directions l, l + kSeedLanes, ..., and a shuffle reduction keeps the best (dot, index) pair, so a
+// lattice of N directions runs on N * kSeedLanes threads.
 constexpr int kSeedStageMax = 1024;  // raysPerProbe is at most 1024 (validated when a grid is created)
-__global__ void k_seed_dirs(const TraceItem* __restrict__ items, const __grid_constant__ TraceItem one) {
+constexpr int kSeedLanes = 8;
+constexpr int kSeedThreads = 128;  // kSeedThreads / kSeedLanes directions per block
+__global__ void __launch_bounds__(kSeedThreads) k_seed_dirs(const TraceItem* __restrict__ items,
+                                                            const __grid_constant__ TraceItem one) {
   __shared__ float4 sPrev[kSeedStageMax];
   const TraceItem& it = items ? items[blockIdx.y] : one;
   if (!it.seedOn) return;  // the same for the whole block
@@ -1045,20 +1050,31 @@ __global__ void k_seed_dirs(const TraceItem* __restrict__ items, const __grid_co
   if (staged)
     for (int i = threadIdx.x; i < n; i += blockDim.x) sPrev[i] = __ldg(&prev[i]);
   __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  const float4 d = it.lattice[j];
+  const int sub = threadIdx.x % kSeedLanes;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) / kSeedLanes;
+  const bool live = j < n;  // lanes past the lattice still take part in the shuffles
+  const float4 d = live ? it.lattice[j] : make_float4(0.f, 0.f, 0.f, 0.f);
   float best = -3.0f;
-  int bi = 0;
-  for (int i = 0; i < n; ++i) {
-    const float4 q = staged ? sPrev[i] : __ldg(&prev[i]);
-    const float c = d.x * q.x + d.y * q.y + d.z * q.z;
-    if (c > best) {
-      best = c;
-      bi = i;
+  int bi = 0x7fffffff;
+  if (live)
+    for (int i = sub; i < n; i += kSeedLanes) {
+      const float4 q = staged ? sPrev[i] : __ldg(&prev[i]);
+      const float c = d.x * q.x + d.y * q.y + d.z * q.z;
+      if (c > best) {  // increasing i within a lane: the first of equal values stays
+        best = c;
+        bi = i;
+      }
+    }
+#pragma unroll
+  for (int off = kSeedLanes / 2; off > 0; off >>= 1) {
+    const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
     }
   }
-  it.seedDir[j] = bi;
+  if (live && sub == 0) it.seedDir[j] = bi == 0x7fffffff ? 0 : bi;  // no comparable direction: any is exact
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -1106,9 +1122,11 @@ cudaError_t launchTraceBatch(const TraceItem* dItems, const Mat3* dRots, int num
   const bool byValue = hItems && hRot && numItems == 1;
   const TraceItem one = byValue ? hItems[0] : TraceItem{};
   const Mat3 rotOne = byValue ? *hRot : Mat3{};
-  dim3 lg((maxN + 127) / 128, numItems);
-  k_lattice_batch<<<lg, 128, 0, stream>>>(byValue ? nullptr : dItems, dRots, one, rotOne, dCounters);
-  k_seed_dirs<<<lg, 128, 0, stream>>>(byValue ? nullptr : dItems, one);
+  // one warp per block: the FP64 lattice of a grid spreads over N / 32 SMs
+  dim3 lg((maxN + 31) / 32, numItems);
+  k_lattice_batch<<<lg, 32, 0, stream>>>(byValue ? nullptr : dItems, dRots, one, rotOne, dCounters);
+  dim3 sg((maxN * kSeedLanes + kSeedThreads - 1) / kSeedThreads, numItems);
+  k_seed_dirs<<<sg, kSeedThreads, 0, stream>>>(byValue ? nullptr : dItems, one);
   if (totalWarps <= 0) return cudaGetLastError();
   const long long rays = totalWarps * 32;
   if (rays > 0x7fffffffll) return cudaErrorInvalidValue;  // shadow records carry 31-bit slot ids + a flag
