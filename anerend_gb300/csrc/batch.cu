@@ -197,6 +197,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.g = gg;
     ti.f = f;
     ti.lattice = g->lattice;
+    ti.latticeUnit = g->latticeUnit;
     ti.order = g->order;
     ti.atlasPrev = g->atlas[g->cur];
     ti.atlasPairs = g->g.atlasFmt == DDGI_FORMAT_RGBA32F && ((uintptr_t)ti.atlasPrev & 31) == 0;

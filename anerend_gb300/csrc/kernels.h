@@ -17,6 +17,7 @@ struct TraceItem {
   GridGPU g;
   FrameGPU f;
   const float4* lattice;  // written by the batched lattice kernel
+  const double* latticeUnit;  // when set: the unrotated FP64 unit lattice (3 per direction), rotated per frame
   const int* order;       // 2N ints: the trace's direction order, then its inverse (the position of each direction)
   const void* atlasPrev;
   int atlasPairs;         // atlasPrev is RGBA32F and 32-byte aligned: the lookups load texel pairs
@@ -38,6 +39,9 @@ struct TraceItem {
 };
 
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream);
+// The unrotated unit lattice of n directions in FP64 (3 doubles each), the part of every frame's lattice that
+// does not depend on the rotation.
+cudaError_t launchLatticeUnit(int n, double* out, cudaStream_t stream);
 // Shading records (SceneGPU::shade) of the scene BVH's records, from the scene's index, vertex, mesh and
 // instance records; `out` holds 3 * bvh.numTris float4.
 cudaError_t launchShadingRecords(const SceneGPU& s, uint64_t numIndices, uint64_t numVerts, float4* out,

@@ -16,17 +16,27 @@
 namespace ddgi {
 
 // ---------------------------------------------------------------------------------------------------
+// Fibonacci direction i of n before the rotation, normalised (rgen:35-46), in FP64.
+DDGI_D void unitLatticeDir(int i, int n, double v[3]) {
+  double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
+  double phi = acos(1.0 - 2.0 * ((double)i + 0.5) / (double)n);
+  double sp = sin(phi);
+  v[0] = cos(theta) * sp;
+  v[1] = sin(theta) * sp;
+  v[2] = cos(phi);
+  double len = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  v[0] /= len;
+  v[1] /= len;
+  v[2] /= len;
+}
+
 // Golden-angle lattice (worldDirFromFibonacciIndex, rgen:35-46) rotated by mat3(randomRot) (rgen:87-88),
 // in FP64. rot is column-major: out_r = sum_c rot[3c + r] * d_c.
 __global__ void k_lattice(int n, Mat3 rot, float4* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
-  double phi = acos(1.0 - 2.0 * ((double)i + 0.5) / (double)n);
-  double sp = sin(phi);
-  double v[3] = {cos(theta) * sp, sin(theta) * sp, cos(phi)};
-  double len = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-  v[0] /= len; v[1] /= len; v[2] /= len;
+  double v[3];
+  unitLatticeDir(i, n, v);
   double r[3];
   for (int row = 0; row < 3; ++row)
     r[row] = (double)rot.m[row] * v[0] + (double)rot.m[3 + row] * v[1] + (double)rot.m[6 + row] * v[2];
@@ -1005,7 +1015,18 @@ cudaError_t launchMirror(const SceneGPU& s, const GridGPU& g, const FrameGPU& f,
   return cudaGetLastError();
 }
 
-// Rotated lattices of many grids: one block row per item.
+__global__ void k_lattice_unit(int n, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v[3];
+  unitLatticeDir(i, n, v);
+  out[3 * i] = v[0];
+  out[3 * i + 1] = v[1];
+  out[3 * i + 2] = v[2];
+}
+
+// Rotated lattices of many grids: one block row per item. The unrotated unit lattice comes from the grid's
+// FP64 table when it has one (the same values unitLatticeDir gives), else it is computed here.
 // Records from `items` and `rots` in device memory, or `one` and `rotOne` when items is null. Block (0, 0)
 // also zeroes the trace counters, which the wavefront kernels launched after this one use.
 __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3* __restrict__ rots,
@@ -1015,12 +1036,14 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
   const TraceItem& it = items ? items[blockIdx.y] : one;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= it.g.N) return;
-  double theta = 2.0 * kPiRgen * (double)i / kGoldenRatio;
-  double phi = acos(1.0 - 2.0 * ((double)i + 0.5) / (double)it.g.N);
-  double sp = sin(phi);
-  double v[3] = {cos(theta) * sp, sin(theta) * sp, cos(phi)};
-  double len = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-  v[0] /= len; v[1] /= len; v[2] /= len;
+  double v[3];
+  if (it.latticeUnit) {
+    v[0] = it.latticeUnit[3 * i];
+    v[1] = it.latticeUnit[3 * i + 1];
+    v[2] = it.latticeUnit[3 * i + 2];
+  } else {
+    unitLatticeDir(i, it.g.N, v);
+  }
   const float* m = items ? rots[blockIdx.y].m : rotOne.m;
   double r[3];
   for (int row = 0; row < 3; ++row)
@@ -1078,6 +1101,11 @@ __global__ void __launch_bounds__(kSeedThreads) k_seed_dirs(const TraceItem* __r
 }
 
 // ---------------------------------------------------------------------------------------------------
+cudaError_t launchLatticeUnit(int n, double* out, cudaStream_t stream) {
+  k_lattice_unit<<<(n + 31) / 32, 32, 0, stream>>>(n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launchLattice(int n, const float rot[9], float4* out, cudaStream_t stream) {
   Mat3 m;
   for (int i = 0; i < 9; ++i) m.m[i] = rot[i];
