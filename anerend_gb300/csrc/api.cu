@@ -818,6 +818,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   FrameGPU f{};
   int rc = frameToGPU(ctx, frame, f);
   if (rc) return rc;
+  setFrameGrid(f, g->g);
   int b, e;
   rc = layerRange(g, frame->layer, true, b, e);
   if (rc) return rc;
@@ -1074,6 +1075,7 @@ int ddgi_query_irradiance(DdgiGrid* g, const DdgiFrame* frame, const DdgiSurface
   FrameGPU f{};
   int rc = frameToGPU(ctx, frame, f);
   if (rc) return rc;
+  setFrameGrid(f, g->g);
   CK(launchQueryIrradiance(g->g, f, g->atlas[g->cur], points, (long long)count, (float4*)ambient,
                            (cudaStream_t)stream),
      "irradiance query");
@@ -1092,6 +1094,7 @@ int ddgi_mirror_reflections(DdgiGrid* g, DdgiScene* sc, const DdgiFrame* frame, 
   FrameGPU f{};
   int rc = frameToGPU(ctx, frame, f);
   if (rc) return rc;
+  setFrameGrid(f, g->g);
   cudaStream_t st = (cudaStream_t)stream;
   // shadow rays in the light-space BVH of this frame's light when the grid traces its shadows there
   SceneGPU view = sc->view;

@@ -167,6 +167,7 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     FrameGPU f{};
     rc = frameToGPU(ctx, &fr, f);
     if (rc) return rc;
+    setFrameGrid(f, g->g);
     if (!(fr.flags & DDGI_UBO_BAKE_MODE_ON_FLAG)) {  // the translation pass (TranslationPass.cpp:59)
       int mv = 0;
       rc = translateGrid(g, fr.cameraPos, &mv, st);

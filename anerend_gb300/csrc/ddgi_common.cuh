@@ -288,6 +288,14 @@ struct FrameGPU {
   uint32_t flags;
   int layerBegin, layerEnd;
   int bakeTile[3];
+  int camIdx[2];  // (int)(camPos.x / step.x), (int)(camPos.z / step.z) of the frame's grid (setFrameGrid)
 };
+
+// The camera's probe indices of a grid (rgen:75-83: int() of the FP32 quotient), once per frame on the host:
+// IEEE division there gives the quotient the shaders' division gives.
+inline void setFrameGrid(FrameGPU& f, const GridGPU& g) {
+  f.camIdx[0] = (int)(f.camPos.x / g.step.x);
+  f.camIdx[1] = (int)(f.camPos.z / g.step.z);
+}
 
 }  // namespace ddgi

@@ -143,8 +143,7 @@ DDGI_D void probeFrame(const GridGPU& g, const FrameGPU& f, float3& stepv, float
     offv = f3((float)f.bakeTile[0] * tSize, g.originY, (float)f.bakeTile[1] * tSize);
   } else {
     // camera-relative grid, int() truncation of the camera probe index (rgen:75-83, pbr_light.glsl:294-308)
-    int camX = (int)(f.camPos.x / g.step.x);
-    int camZ = (int)(f.camPos.z / g.step.z);
+    const int camX = f.camIdx[0], camZ = f.camIdx[1];
     stepv = g.step;
     offv = f3((float)camX * g.step.x - g.step.x * (float)g.X / 2.0f, g.originY,
               (float)camZ * g.step.z - g.step.z * (float)g.Z / 2.0f);
