@@ -312,7 +312,7 @@ uint64_t gridFootprint(const DdgiGridDesc* d, int convMode, bool hitSeeds) {
   uint64_t texel = d->atlasFormat == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rayTexel = g.rayFmt == DDGI_FORMAT_RGBA32F ? 16 : 8;
   uint64_t rays = (uint64_t)g.rayW * g.bh * g.Z * g.Y;
-  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + rayTexel * rays + 16ull * g.N + 24ull * g.N +
+  uint64_t bytes = 2 * (uint64_t)g.atlasW * g.atlasH * texel + rayTexel * rays + 16ull * g.N + 24ull * g.N + 32ull * g.N +
                    8ull * g.N + 4ull * g.N * kOctTexels + 4ull * kOctTexels;
   if (d->options & DDGI_GRID_WRITE_DIRS) bytes += rayTexel * rays;
   if (d->options & DDGI_GRID_RECORD_HITS) bytes += 4 * rays;
@@ -348,6 +348,7 @@ int gridCreate(DdgiContext* ctx, const DdgiGridDesc* desc, cudaStream_t st, bool
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->lattice, 16 * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->latticeUnit, 3 * sizeof(double) * (size_t)g->g.N);
   if (e == cudaSuccess) e = launchLatticeUnit(g->g.N, g->latticeUnit, st);
+  if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->rayDirs, 2 * sizeof(float4) * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->order, 2 * sizeof(int) * (size_t)g->g.N);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wt, 4 * (size_t)g->g.N * kOctTexels);
   if (e == cudaSuccess) e = gridAlloc(g, (void**)&g->wsum, 4 * kOctTexels);
@@ -390,6 +391,7 @@ void gridDestroy(DdgiGrid* g) {
   gridFree(g, g->rayHit);
   gridFree(g, g->lattice);
   gridFree(g, g->latticeUnit);
+  gridFree(g, g->rayDirs);
   gridFree(g, g->order);
   gridFree(g, g->latticePrev);
   gridFree(g, g->seedDir);
@@ -850,6 +852,7 @@ int ddgi_trace(DdgiGrid* g, const DdgiScene* scene, const DdgiFrame* frame, void
   ti.f = f;
   ti.lattice = g->lattice;
   ti.latticeUnit = g->latticeUnit;
+  ti.rayDirs = g->rayDirs;
   ti.order = g->order;
   ti.atlasPrev = g->atlas[g->cur];
   ti.atlasPairs = g->g.atlasFmt == DDGI_FORMAT_RGBA32F && ((uintptr_t)ti.atlasPrev & 31) == 0;

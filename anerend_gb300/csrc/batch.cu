@@ -199,6 +199,9 @@ int batchLaunch(DdgiContext* ctx, LaunchState* S, const DdgiBatchTuning& t, Ddgi
     ti.f = f;
     ti.lattice = g->lattice;
     ti.latticeUnit = g->latticeUnit;
+    // no direction records: with the records in global memory a batched refill reads the item's record for
+    // them, which measured slower than computing the direction part of each ray
+    ti.rayDirs = nullptr;
     ti.order = g->order;
     ti.atlasPrev = g->atlas[g->cur];
     ti.atlasPairs = g->g.atlasFmt == DDGI_FORMAT_RGBA32F && ((uintptr_t)ti.atlasPrev & 31) == 0;

@@ -18,6 +18,7 @@ struct TraceItem {
   FrameGPU f;
   const float4* lattice;  // written by the batched lattice kernel
   const double* latticeUnit;  // when set: the unrotated FP64 unit lattice (3 per direction), rotated per frame
+  const float4* rayDirs;      // when set: 2 float4 per direction, its ray record (packRayDir), written with the lattice
   const int* order;       // 2N ints: the trace's direction order, then its inverse (the position of each direction)
   const void* atlasPrev;
   int atlasPairs;         // atlasPrev is RGBA32F and 32-byte aligned: the lookups load texel pairs

@@ -99,6 +99,7 @@ struct DdgiGrid {
   int* rayHit = nullptr;
   float4* lattice = nullptr;
   double* latticeUnit = nullptr;  // the unrotated unit lattice in FP64, 3 per direction, computed once
+  float4* rayDirs = nullptr;      // per direction of the lattice its ray record (2 float4, packRayDir)
   int* order = nullptr;   // trace-kernel direction order (N ints), then its inverse (N ints)
   // closest-hit seeding (grids made by ddgi_grid_create; served grids trace once and keep none): the last
   // traced lattice, per direction the nearest direction of that lattice, and per (probe, direction) the

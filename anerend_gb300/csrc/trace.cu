@@ -10,6 +10,7 @@
 #include "ddgi_common.cuh"
 #include "kernels.h"
 #include "traverse.cuh"
+#include <type_traits>
 
 #include <climits>
 
@@ -400,7 +401,14 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
         if (!rs.valid) {
           hits[cand] = make_float4(__int_as_float(kNoRay), 0.f, 0.f, 0.f);
         } else {
-          ray = makeRay(probeOrigin(T.g, T.f, rs), xyz(__ldg(&T.lattice[rs.j])));
+          if (std::is_same<Src, ItemsOne>::value && T.rayDirs) {  // a single record's direction records
+            RayDirRec p;
+            p.a = __ldg(&T.rayDirs[2 * rs.j]);
+            p.b = __ldg(&T.rayDirs[2 * rs.j + 1]);
+            ray = makeRayPacked(probeOrigin(T.g, T.f, rs), p);
+          } else {
+            ray = makeRay(probeOrigin(T.g, T.f, rs), xyz(__ldg(&T.lattice[rs.j])));
+          }
           bvh = T.s.bvh;
           if (travInit<kWide, false>(bvh, ray, st, hit)) {
             hits[cand] = make_float4(__int_as_float(hit.leaf), hit.t, hit.b1, hit.b2);
@@ -1048,7 +1056,13 @@ __global__ void k_lattice_batch(const TraceItem* __restrict__ items, const Mat3*
   for (int row = 0; row < 3; ++row)
     r[row] = (double)m[row] * v[0] + (double)m[3 + row] * v[1] + (double)m[6 + row] * v[2];
   if (it.latticePrev) it.latticePrev[i] = it.lattice[i];  // the last traced lattice, for the seed map
-  const_cast<float4*>(it.lattice)[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
+  const float4 d = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
+  const_cast<float4*>(it.lattice)[i] = d;
+  if (it.rayDirs) {  // the direction's ray record, which the closest-hit traversal's rays of direction i share
+    const RayDirRec p = packRayDir(xyz(d));
+    const_cast<float4*>(it.rayDirs)[2 * i] = p.a;
+    const_cast<float4*>(it.rayDirs)[2 * i + 1] = p.b;
+  }
 }
 
 // Seed map of the items that seed their closest hits: for each direction of the new lattice the nearest

@@ -105,6 +105,55 @@ struct WRay {
   float Sx, Sy, Sz;
 };
 
+// The direction-only part of a ray: the watertight test's axis permutation and shear constants and the box
+// test's reciprocals, as two float4: (invd.xyz, Sx), (Sy, Sz, kx | ky << 2 | kz << 4 as bits, 0). Rays that
+// share a direction (a probe grid's rays of one lattice direction) share it, so it is computed once per direction.
+struct RayDirRec {
+  float4 a, b;
+};
+
+DDGI_HD RayDirRec packRayDir(float3 d) {
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1; if (kx == 3) kx = 0;
+  int ky = kx + 1; if (ky == 3) ky = 0;
+  float dz = get(d, kz);
+  if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
+  const float Sx = get(d, kx) / dz, Sy = get(d, ky) / dz, Sz = 1.0f / dz;
+  // box-test reciprocals; a zero component becomes a tiny same-signed value so (lo - o) * invd is finite
+  float3 dd = f3(d.x != 0.f ? d.x : copysignf(1e-20f, d.x), d.y != 0.f ? d.y : copysignf(1e-20f, d.y),
+                 d.z != 0.f ? d.z : copysignf(1e-20f, d.z));
+  RayDirRec p;
+  p.a = make_float4(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z, Sx);
+  p.b = make_float4(Sy, Sz, asFloatHd((uint32_t)(kx | (ky << 2) | (kz << 4))), 0.0f);
+  return p;
+}
+
+// A ray from its origin and its direction record (packRayDir).
+DDGI_HD WRay makeRayPacked(float3 o, const RayDirRec& p) {
+  WRay r;
+  r.o = o;
+  const uint32_t k = asUint(p.b.z);
+  r.kx = (int)(k & 3u);
+  r.ky = (int)((k >> 2) & 3u);
+  r.kz = (int)((k >> 4) & 3u);
+  r.Sx = p.a.w;
+  r.Sy = p.b.x;
+  r.Sz = p.b.y;
+  r.invd = f3(p.a.x, p.a.y, p.a.z);
+  // margin 2^-21 |o * invd| (8 units of rounding) covers the rounding of o * invd and of the additions,
+  // leaving one rounding of the FMA, within the conservative far-distance factor of the slab test
+  const float wx = o.x * r.invd.x, wy = o.y * r.invd.y, wz = o.z * r.invd.z;
+  const float ex = fabsf(wx) * 4.76837158203125e-7f, ey = fabsf(wy) * 4.76837158203125e-7f,
+              ez = fabsf(wz) * 4.76837158203125e-7f;
+  r.nAdd = f3(-wx - ex, -wy - ey, -wz - ez);
+  r.fAdd = f3(-wx + ex, -wy + ey, -wz + ez);
+  r.invd15 = r.invd * 32768.0f;
+  r.invdM = f3(fabsf(r.invd.x), fabsf(r.invd.y), fabsf(r.invd.z)) * 4.76837158203125e-7f;
+  return r;
+}
+
+// The same ray from its direction (packRayDir and makeRayPacked in one, the same arithmetic).
 DDGI_HD WRay makeRay(float3 o, float3 d) {
   WRay r;
   r.o = o;
@@ -118,12 +167,9 @@ DDGI_HD WRay makeRay(float3 o, float3 d) {
   r.Sx = get(d, kx) / dz;
   r.Sy = get(d, ky) / dz;
   r.Sz = 1.0f / dz;
-  // box-test reciprocals; a zero component becomes a tiny same-signed value so (lo - o) * invd is finite
   float3 dd = f3(d.x != 0.f ? d.x : copysignf(1e-20f, d.x), d.y != 0.f ? d.y : copysignf(1e-20f, d.y),
                  d.z != 0.f ? d.z : copysignf(1e-20f, d.z));
   r.invd = f3(1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z);
-  // margin 2^-21 |o * invd| (8 units of rounding) covers the rounding of o * invd and of the additions,
-  // leaving one rounding of the FMA, within the conservative far-distance factor of the slab test
   const float wx = o.x * r.invd.x, wy = o.y * r.invd.y, wz = o.z * r.invd.z;
   const float ex = fabsf(wx) * 4.76837158203125e-7f, ey = fabsf(wy) * 4.76837158203125e-7f,
               ez = fabsf(wz) * 4.76837158203125e-7f;
