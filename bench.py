@@ -813,6 +813,11 @@ def run_ours(args, rank, local, world):
         v, dt, cores = cpu_sample(w, arrays, frames)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{frames} full probe updates ({frames * rays_per_step} rays), FP64 oracle, {dt:.1f} s"}
+        # the CPU reference workload run in full (8x4x8 probes, 64 rays, 4,098 triangles, all 8 frames)
+        w1 = scenes.CPU_REFERENCE
+        v1, dt1, _ = cpu_sample(w1, scenes.build_scene(w1), w1.frames)
+        cpu["cpu_reference_workload_full"] = {"value": v1, "unit": UNIT, "frames": w1.frames,
+                                              "rays": w1.frames * w1.probes * w1.rays, "seconds": dt1}
     forms = None
     if rank == 0 and world == 1 and not args.no_extras:
         forms = measure_forms(ctx, scene, w, stream, bvh_width=args.bvh_width)
