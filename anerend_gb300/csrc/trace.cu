@@ -1148,7 +1148,8 @@ void launchWavefront(const Src& src, long long rays, unsigned long long* dCounte
   auto shadow = wide ? (lightSpace ? k_trace_shadow<true, true, Src> : k_trace_shadow<true, false, Src>)
                      : (lightSpace ? k_trace_shadow<false, true, Src> : k_trace_shadow<false, false, Src>);
   const int shadowBlocks = lightSpace ? blocks * kShadowLightBlocks / DDGI_TRACE_MIN_BLOCKS : blocks;
-  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill, err);
+  // the shadow rays' traversal refills at half the closest-hit threshold (their rays are shorter)
+  shadow<<<shadowBlocks, kTraceThreads, 0, stream>>>(src, dShadow, dCounters, refill > 1 ? refill / 2 : 1, err);
   k_shadow_resolve<Src><<<(unsigned)shadeBlocks, 256, 0, stream>>>(src, dShadow, dCounters);
 }
 
