@@ -164,8 +164,8 @@ typedef struct DdgiTuning {
                            accumulation and the hysteresis blend stay FP32 */
   int32_t bvhWidth;     /* traversal tree: 8 = 8-wide BVH collapsed from the LBVH (default; 0 means 8);
                            2 = the binary LBVH. Both give the same hits */
-  int32_t refillLanes;  /* a warp of the persistent traversals takes new rays once this many of its lanes are
-                           idle (1..32; default 8; 0 means 8) */
+  int32_t refillLanes;  /* a warp of the closest-hit traversal takes new rays once this many of its lanes are
+                           idle, the shadow traversal's at half as many (1..32; default 8; 0 means 8) */
   int32_t reserved[2];
 } DdgiTuning;
 
@@ -428,8 +428,8 @@ typedef struct DdgiBatchTuning {
   int32_t shadowMode;    /* as DdgiTuning.shadowMode (default 1) */
   int32_t convMode;      /* as DdgiTuning.convMode (default 0); tensor-core batches hold at most 64 items */
   int32_t blocksPerSm;   /* resident 128-thread blocks per SM of the persistent trace (1..8, default 8) */
-  int32_t refillLanes;   /* a warp of the persistent traversals takes new rays from the queue once this many of
-                            its 32 lanes are idle (1..32, default 8) */
+  int32_t refillLanes;   /* a warp of the closest-hit traversal takes new rays from the queue once this many of
+                            its 32 lanes are idle, the shadow traversal's at half as many (1..32, default 8) */
   int32_t useGraph;      /* capture the launch sequence into a CUDA graph once its shape repeats (default 1) */
   int32_t bvhWidth;      /* as DdgiTuning.bvhWidth (default 8) */
 } DdgiBatchTuning;
