@@ -274,3 +274,25 @@ extern "C" long long divfast_check(int numCases, uint64_t seed) {
   }
   return bad;
 }
+
+// makeRay against makeRayPacked(packRayDir(d)) (the per-direction record the lattice kernel writes): every field
+// bit for bit, on random directions and on directions with zero, signed-zero and tied components.
+extern "C" long long raydir_check(int numCases, uint64_t seed) {
+  Rng rng{seed};
+  long long bad = 0;
+  auto same = [](float a, float b) { uint32_t x, y; std::memcpy(&x, &a, 4); std::memcpy(&y, &b, 4); return x == y; };
+  auto same3 = [&](float3 a, float3 b) { return same(a.x, b.x) && same(a.y, b.y) && same(a.z, b.z); };
+  for (int c = 0; c < numCases; ++c) {
+    float3 d = f3(2.0f * rng.uni() - 1.0f, 2.0f * rng.uni() - 1.0f, 2.0f * rng.uni() - 1.0f);
+    if (c % 5 == 1) d.x = (c & 8) ? -0.0f : 0.0f;
+    if (c % 7 == 2) d.y = d.z;
+    if (c % 11 == 3) d = f3(0.0f, 0.0f, (c & 16) ? -1.0f : 1.0f);
+    const float3 o = f3(20.0f * rng.uni() - 10.0f, 20.0f * rng.uni() - 10.0f, 20.0f * rng.uni() - 10.0f);
+    const WRay a = makeRay(o, d), b = makeRayPacked(o, packRayDir(d));
+    const bool ok = same3(a.o, b.o) && same3(a.invd, b.invd) && same3(a.nAdd, b.nAdd) && same3(a.fAdd, b.fAdd) &&
+                    same3(a.invd15, b.invd15) && same3(a.invdM, b.invdM) && a.kx == b.kx && a.ky == b.ky &&
+                    a.kz == b.kz && same(a.Sx, b.Sx) && same(a.Sy, b.Sy) && same(a.Sz, b.Sz);
+    bad += !ok;
+  }
+  return bad;
+}

@@ -42,6 +42,8 @@ def lib(request, tmp_path_factory):
     lib.wbvh_check.restype = ctypes.c_int
     lib.divfast_check.argtypes = [ctypes.c_int, ctypes.c_uint64]
     lib.divfast_check.restype = ctypes.c_longlong
+    lib.raydir_check.argtypes = [ctypes.c_int, ctypes.c_uint64]
+    lib.raydir_check.restype = ctypes.c_longlong
     return lib
 
 
@@ -70,3 +72,9 @@ def test_invariant_divisor_division_is_exact(lib):
     """divFast, the ray-slot mapping's division by a per-grid reciprocal, equals integer division for every
     dividend below 2^31 tried, including the divisor's multiples and the values one below them."""
     assert lib.divfast_check(300000, 99) == 0
+
+
+def test_direction_records_build_the_same_ray(lib):
+    """A ray built from its direction's record (packRayDir, written once per lattice direction) equals the ray
+    built from the direction itself, every field bit for bit."""
+    assert lib.raydir_check(200000, 5) == 0
