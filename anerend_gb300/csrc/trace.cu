@@ -684,6 +684,7 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
   uint32_t rayId = 0;  // its natural ray id
   bool drained = total == 0;
   BvhRef bvh;
+  const BvhRef* bvhp = nullptr;  // as in k_trace_closest: a launch over many records steps through a pointer
   WRay ray;
   HitInfo hit;
   typename TravOf<kWide>::T st;
@@ -704,6 +705,7 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
         rayId = __float_as_uint(rec.w);
         const TraceItem& T = src.at((long long)(rayId >> 5));
         bvh = kLightSpace ? T.s.shadow : T.s.bvh;
+        bvhp = kLightSpace ? &T.s.shadow : &T.s.bvh;
         ray = makeRay(xyz(rec), kLightSpace ? f3(0.f, 0.f, 1.f) : normalize3(-T.f.lightDir));
         finished = travInit<kWide, true>(bvh, ray, st, hit);
         if (!finished) {  // the candidate occluder k_shade parked: if it is hit, the ray is shadowed
@@ -712,7 +714,8 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
         }
       }
     }
-    if (id >= 0 && !finished) finished = travStep<kWide, true, kLightSpace>(bvh, ray, st, hit, err);
+    if (id >= 0 && !finished)
+      finished = travStep<kWide, true, kLightSpace>(std::is_same<Src, ItemsOne>::value ? bvh : *bvhp, ray, st, hit, err);
     if (id >= 0 && finished) {
       if (hit.leaf >= 0) {
         reinterpret_cast<uint32_t*>(shadowList + 2 * id)[3] = rayId | 0x80000000u;
