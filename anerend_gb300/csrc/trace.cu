@@ -372,9 +372,9 @@ DDGI_D bool travInit(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& 
   if constexpr (kWide) return wideInit<kAnyHit>(b, r, kTMax, s, hit);
   else return binInit<kAnyHit>(b, r, kTMin, kTMax, s, hit);
 }
-template <bool kWide, bool kAnyHit, bool kPlusZ = false>
+template <bool kWide, bool kAnyHit, bool kPlusZ = false, bool kNodeScale = false>
 DDGI_D bool travStep(const BvhRef& b, const WRay& r, typename TravOf<kWide>::T& s, HitInfo& hit, uint32_t* err) {
-  if constexpr (kWide) return wideStep<kAnyHit, kPlusZ>(b, r, kTMin, s, hit, err);
+  if constexpr (kWide) return wideStep<kAnyHit, kPlusZ, kNodeScale>(b, r, kTMin, s, hit, err);
   else return binStep<kAnyHit>(b, r, kTMin, s, hit, err);
 }
 
@@ -390,7 +390,11 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
   bool drained = false;
   // the lane's BVH: a single record's launch keeps a register copy; a launch over many records keeps a pointer
   // to the lane's record's BVH instead, whose fields the steps re-read from L1, which frees nine registers of
-  // the 64-register traversal (measured 1.4 % faster on the 64-grid batch)
+  // the 64-register traversal (measured 1.4 % faster on the 64-grid batch). Such a launch also forms the
+  // quantized nodes' scale from the node (kNodeScale): three registers fewer per ray take away the last 24
+  // bytes of spills (1.5 % faster on that batch); the single record's kernel, which does not spill, measured
+  // 1.2 % slower with it and keeps the ray's scale.
+  constexpr bool kManyItems = !std::is_same<Src, ItemsOne>::value;
   BvhRef bvh;
   const BvhRef* bvhp = nullptr;
   WRay ray;
@@ -436,7 +440,7 @@ __global__ void __launch_bounds__(kTraceThreads, DDGI_TRACE_MIN_BLOCKS)
         }
       }
     }
-    if (id >= 0 && travStep<kWide, false>(std::is_same<Src, ItemsOne>::value ? bvh : *bvhp, ray, st, hit, err)) {
+    if (id >= 0 && travStep<kWide, false, false, kManyItems>(kManyItems ? *bvhp : bvh, ray, st, hit, err)) {
       hits[id] = make_float4(__int_as_float(hit.leaf), hit.t, hit.b1, hit.b2);
       id = -1;
     }
@@ -693,7 +697,9 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
   uint32_t rayId = 0;  // its natural ray id
   bool drained = total == 0;
   BvhRef bvh;
-  const BvhRef* bvhp = nullptr;  // as in k_trace_closest: a launch over many records steps through a pointer
+  // as in k_trace_closest: a launch over many records steps through a pointer and forms the node scale
+  constexpr bool kManyItems = !std::is_same<Src, ItemsOne>::value;
+  const BvhRef* bvhp = nullptr;
   WRay ray;
   HitInfo hit;
   typename TravOf<kWide>::T st;
@@ -724,7 +730,7 @@ __global__ void __launch_bounds__(kTraceThreads, kLightSpace ? kShadowLightBlock
       }
     }
     if (id >= 0 && !finished)
-      finished = travStep<kWide, true, kLightSpace>(std::is_same<Src, ItemsOne>::value ? bvh : *bvhp, ray, st, hit, err);
+      finished = travStep<kWide, true, kLightSpace, kManyItems>(kManyItems ? *bvhp : bvh, ray, st, hit, err);
     if (id >= 0 && finished) {
       if (hit.leaf >= 0) {
         reinterpret_cast<uint32_t*>(shadowList + 2 * id)[3] = rayId | 0x80000000u;

@@ -235,8 +235,11 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
     traverse<false>(bref, r, 0.1f, 50.0f, h2, &err);
     traverseWide<false>(bref, r, 0.1f, 50.0f, hw, &err);
     bool any = traverseWide<true>(bref, r, 0.1f, 50.0f, ha, &err);
+    HitInfo hs;  // the node test with the scale formed from the node's exponent
+    traverseWide<false, false, true>(bref, r, 0.1f, 50.0f, hs, &err);
     if (!sameHit(bf, h2)) stats[2]++;
     if (!sameHit(bf, hw)) stats[3]++;
+    if (!sameHit(hw, hs)) stats[3]++;
     if (any != (bf.leaf >= 0) || (any && !(ha.t >= 0.1f && ha.t <= 50.0f))) stats[4]++;
     if (bf.leaf >= 0) stats[6]++;
     // the same origin along exactly +z through the specialised box test (light-space shadow rays)
@@ -248,7 +251,10 @@ extern "C" int wbvh_check(int numTris, int numRays, uint64_t seed, int dupEvery,
       HitInfo hz, az;
       traverseWide<false, true>(bref, rz, 0.1f, 50.0f, hz, &err);
       bool anyz = traverseWide<true, true>(bref, rz, 0.1f, 50.0f, az, &err);
+      HitInfo sz;
+      const bool anys = traverseWide<true, true, true>(bref, rz, 0.1f, 50.0f, sz, &err);
       if (!sameHit(bz, hz)) stats[3]++;
+      if (anys != anyz) stats[4]++;
       if (anyz != (bz.leaf >= 0)) stats[4]++;
     }
   }
