@@ -655,7 +655,7 @@ def measure_batched(ctx, stream, serving=True):
     serv = {"scenes": len(scs), "triangles": sum(stris), "triangles_min": min(stris), "triangles_max": max(stris),
             "conv_mode": "FP16 tensor cores", "policy": "shortest rays first, aging 50 ms", "in_flight": 2,
             "max_batch_mrays": 8, "baseline_policy": "arrival order (fifo_<rate>), same slots"}
-    sjf_rates = (2000, 1000, 750, 650, 600, 500)
+    sjf_rates = (2000, 1000, 900, 850, 750, 650, 600, 500)
     runs = [(float(r), 1.5, L.DDGI_SERVE_FIFO, 2, f"fifo_{r}") for r in (2000, 1000, 750, 500)]
     runs += [(float(r), 1.5, L.DDGI_SERVE_SHORTEST_FIRST, 2, f"rate_{r}") for r in sjf_rates]
     for rate, dur, policy, slots, key in runs:
