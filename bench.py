@@ -446,6 +446,14 @@ def measure_forms(ctx, scene, w, stream, only=None, bvh_width=8):
     g.close()
     out["single_grid_speedup_vs_plain"] = (out["single_grid_plain_fp32"]["ms_per_update"]
                                            / out["single_grid_tuned_fp32"]["ms_per_update"])
+    # the reference's own formats: RGBA16F atlas and RGBA16F ray images, tuned, FP32 convolution
+    g = ddgi.ProbeGrid(ctx, w.dims, w.step, w.rays, w.origin_y, w.hysteresis, atlas_format=L.DDGI_FORMAT_RGBA16F,
+                       options=L.DDGI_GRID_RAYS_RGBA16F)
+    g.set_tuning(**dict(tuned, conv_mode=0))
+    ms = _time_updates(torch, single, frames1, 5)
+    out["single_grid_tuned_fp32_rgba16f"] = {"ms_per_update": ms, "rays_per_s": rays / ms * 1e3,
+                                             "formats": "RGBA16F atlas and ray images (the reference's)"}
+    g.close()
 
     out["precision_tc"] = measure_precision(ctx, stream)
     out["mirror"] = measure_mirror(ctx, scene, w, stream)
