@@ -21,7 +21,7 @@ struct TraceItem {
   const float4* rayDirs;      // when set: 2 float4 per direction, its ray record (packRayDir), written with the lattice
   const int* order;       // 2N ints: the trace's direction order, then its inverse (the position of each direction)
   const void* atlasPrev;
-  int atlasPairs;         // atlasPrev is RGBA32F and 32-byte aligned: the lookups load texel pairs
+  int atlasPairs;         // atlasPrev is aligned to a texel pair (32 B RGBA32F, 16 B RGBA16F): the lookups load pairs
   void* rayRad;  // ray images in g.rayFmt texels
   void* rayDir;
   int* rayHit;

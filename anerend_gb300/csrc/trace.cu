@@ -96,7 +96,25 @@ DDGI_D void loadRowPair(const float4* row, int x0, int x1, float4& t0, float4& t
   t1 = q;
 }
 
-template <bool kPairs = false>
+// The same for an RGBA16F atlas: an aligned pair of 8-byte texels is one 16-byte load. row: the row's first
+// texel; the atlas base is 16-byte aligned (the row length 10 X is even, so every row starts aligned).
+DDGI_D float4 halfTexel(uint32_t lo, uint32_t hi) {
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&lo));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&hi));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+DDGI_D void loadRowPairHalf(const uint2* row, int x0, int x1, float4& t0, float4& t1) {
+  const uint4 p = __ldg(reinterpret_cast<const uint4*>(row + (x0 & ~1)));
+  const bool odd = (x0 & 1) != 0;
+  uint2 q = make_uint2(p.z, p.w);
+  if (odd) q = __ldg(row + x1);
+  t0 = odd ? halfTexel(p.z, p.w) : halfTexel(p.x, p.y);
+  t1 = halfTexel(q.x, q.y);
+}
+
+// kPairs: 0 loads every texel alone; 1 loads texel pairs from an RGBA32F atlas (other formats alone); 2 also
+// loads them from an RGBA16F atlas. The caller passes 1 or 2 only for an atlas aligned to a texel pair.
+template <int kPairs = 0>
 DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int iy, int iz, const OctTap& tap) {
   if (g.options & DDGI_GRID_EDGE_CLAMP) {
     ix = min(max(ix, 0), g.X - 1);
@@ -123,10 +141,14 @@ DDGI_D float3 sampleSingleProbe(const GridGPU& g, const void* atlas, int ix, int
     if (y1 >= g.atlasH) y1 -= g.atlasH;
   }
   float4 t00, t10, t01, t11;
-  if (kPairs && g.atlasFmt == DDGI_FORMAT_RGBA32F) {
+  if (kPairs >= 1 && g.atlasFmt == DDGI_FORMAT_RGBA32F) {
     const float4* a = reinterpret_cast<const float4*>(atlas);
     loadRowPair(a + (size_t)y0 * g.atlasW, x0, x1, t00, t10);
     loadRowPair(a + (size_t)y1 * g.atlasW, x0, x1, t01, t11);
+  } else if (kPairs == 2) {
+    const uint2* a = reinterpret_cast<const uint2*>(atlas);
+    loadRowPairHalf(a + (size_t)y0 * g.atlasW, x0, x1, t00, t10);
+    loadRowPairHalf(a + (size_t)y1 * g.atlasW, x0, x1, t01, t11);
   } else {
     t00 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x0);
     t10 = loadTexel(atlas, g.atlasFmt, (size_t)y0 * g.atlasW + x1);
@@ -154,7 +176,7 @@ DDGI_D void probeFrame(const GridGPU& g, const FrameGPU& f, float3& stepv, float
 // kUnroll: how far the 8-probe loop is unrolled. The batch's shading kernel (80 registers, its records mostly
 // missing L2) runs it unrolled by 2, measured 1 % faster there; the single record's stays fully unrolled (the
 // rolled loop was 0.4 % slower on the single grid). Both sum the probes in the same order.
-template <bool kPairs = false, int kUnroll = 8>
+template <int kPairs = 0, int kUnroll = 8>
 DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas, float3 wp, float3 n) {
   float3 stepv, offv;
   probeFrame(g, f, stepv, offv);
@@ -195,7 +217,7 @@ DDGI_D float3 sampleProbe(const GridGPU& g, const FrameGPU& f, const void* atlas
 }
 
 // calcIndirectDiffuseLight (pbr_light.glsl:365-388)
-template <bool kPairs = false, int kUnroll = 8>
+template <int kPairs = 0, int kUnroll = 8>
 DDGI_D float3 calcIndirectDiffuse(const GridGPU& g, const FrameGPU& f, const void* atlas, float3 n,
                                   float3 albedo, float metallic, float roughness, float3 wp, float3 viewPos) {
   float3 V = normalize3(viewPos - wp);
@@ -599,6 +621,9 @@ __global__ void __launch_bounds__(256, std::is_same<Src, ItemsOne>::value ? 4 : 
                                                const float4* __restrict__ hits, float4* __restrict__ shadowList,
                                                unsigned long long* __restrict__ counters) {
   constexpr int kProbeUnroll = std::is_same<Src, ItemsOne>::value ? 8 : 2;
+  // texel pairs from RGBA16F atlases too in the single record's kernel (1.2 % faster per update on an RGBA16F
+  // grid); the batch's kernel keeps them to RGBA32F atlases (the RGBA16F path's registers cost it 0.25 %)
+  constexpr int kPairMode = std::is_same<Src, ItemsOne>::value ? 2 : 1;
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < totalRays;
@@ -641,8 +666,8 @@ __global__ void __launch_bounds__(256, std::is_same<Src, ItemsOne>::value ? 4 : 
         L = calcLightDirectional(h.normal, h.color, h.metallic, h.roughness, pos, origin, f.lightDir, f.sunIntensity);
         if (f.flags & DDGI_UBO_DDGI_MULTI_FLAG) {
           const float3 ind =
-              T.atlasPairs ? calcIndirectDiffuse<true, kProbeUnroll>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin)
-                           : calcIndirectDiffuse<false, kProbeUnroll>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
+              T.atlasPairs ? calcIndirectDiffuse<kPairMode, kProbeUnroll>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin)
+                           : calcIndirectDiffuse<0, kProbeUnroll>(g, f, T.atlasPrev, h.normal, h.color, h.metallic, h.roughness, pos, origin);
           L += ind;
           Ls += ind;
         }
